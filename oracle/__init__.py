@@ -1,0 +1,212 @@
+"""CPU oracle for the TOED hot path -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg use
+this package, and only as the checker (or, for the CPU baseline, as the timed
+restatement of the reference's OpenMP path).  The CUDA library never imports
+it; its product path fails loudly when the CUDA extension is missing.
+
+Two native libraries sit behind it:
+
+* ``oracle/liboracle.so`` -- the C restatement ``oracle/toed_oracle.c`` of the
+  reference's FP64 CPU path (cpu_toed.cpp:128-545 and
+  subpix_TO_correction/subpix_to_correction.cpp:195-736).  Built from
+  committed source on any host (x86 here, aarch64 on the GPU host).
+* ``oracle/_ref/libref_toed.so`` -- the reference's own cpu_toed.cpp and
+  subpix_to_correction.cpp compiled where they lie (``make -C oracle ref``),
+  only where the reference sources exist.  Used to pin the restatement and to
+  generate the committed golden fixtures under tests/golden/.
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import subprocess
+import tempfile
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+_LIB = None
+_REF = None
+
+_dp = ctypes.POINTER(ctypes.c_double)
+_i64p = ctypes.POINTER(ctypes.c_int64)
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(_dp)
+
+
+def build(ref: bool = False) -> None:
+    """Compile liboracle.so (and, if ``ref``, the reference build)."""
+    subprocess.run(["make", "-s", "-C", _HERE], check=True)
+    if ref:
+        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+
+
+def lib():
+    global _LIB
+    if _LIB is None:
+        path = os.path.join(_HERE, "liboracle.so")
+        if not os.path.exists(path):
+            build()
+        L = ctypes.CDLL(path)
+        L.toed_oracle_taps.argtypes = [ctypes.c_double, ctypes.c_int, _dp]
+        L.toed_oracle_detect.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, ctypes.c_double,
+            ctypes.c_int, _dp, ctypes.c_long, _dp, _dp, _i64p]
+        L.toed_oracle_detect.restype = ctypes.c_long
+        L.toed_oracle_planes.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
+        L.subpix_oracle_run.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
+            ctypes.c_int, _dp, ctypes.c_long, _dp, _dp, _dp, _dp, _dp]
+        L.subpix_oracle_run.restype = ctypes.c_long
+        L.subpix_oracle_kernels.argtypes = [ctypes.c_double, _dp]
+        L.subpix_oracle_kernels.restype = ctypes.c_int
+        _LIB = L
+    return _LIB
+
+
+def default_radius(sigma: float) -> int:
+    """Half-width r = ceil(4 sigma) (17 taps at sigma 2, cpu_toed.cpp:131)."""
+    return int(math.ceil(4.0 * sigma))
+
+
+def taps(sigma: float, r: int | None = None) -> np.ndarray:
+    """(8, 2r+3) tap block: G, Gx, Gxx, Gxxx, then the +0.5-shifted set."""
+    r = default_radius(sigma) if r is None else r
+    out = np.zeros((8, 2 * r + 3), np.float64)
+    lib().toed_oracle_taps(float(sigma), int(r), _ptr(out))
+    return out
+
+
+def detect(img, sigma: float = 2.0, r: int | None = None, tap_block=None, threshold: float = 2.0,
+           nthreads: int = 0, planes: bool = False):
+    """FP64 TOED.  Returns dict(edges=(N,4), index=(N,) 2x-grid linear index
+    [, planes=(4,2H,2W) Ix/Iy/mag/ori, posmaps=(3,2H,2W)])."""
+    img = np.ascontiguousarray(img, dtype=np.float64)
+    H, W = img.shape
+    r = default_radius(sigma) if r is None else r
+    tb = None
+    if tap_block is not None:
+        tb = np.ascontiguousarray(tap_block, dtype=np.float64)
+        assert tb.shape == (8, 2 * r + 3)
+    cap = 4 * H * W
+    edges = np.zeros((cap, 4), np.float64)
+    index = np.zeros(cap, np.int64)
+    pl = np.zeros((4, 2 * H, 2 * W), np.float64) if planes else None
+    pm = np.zeros((3, 2 * H, 2 * W), np.float64) if planes else None
+    n = lib().toed_oracle_detect(_ptr(img), H, W, float(sigma), int(r), _ptr(tb), float(threshold),
+                                 int(nthreads), _ptr(edges), cap, _ptr(pl), _ptr(pm),
+                                 index.ctypes.data_as(_i64p))
+    out = {"edges": edges[:n].copy(), "index": index[:n].copy()}
+    if planes:
+        out["planes"] = pl
+        out["posmaps"] = pm
+    return out
+
+
+def planes9(img, sigma: float = 2.0, r: int | None = None, nthreads: int = 0):
+    """All nine derivative planes on the 2x grid: (9, 2H, 2W) in the order
+    fx, fy, fxx, fxy, fyy, fxxy, fxyy, fxxx, fyyy."""
+    img = np.ascontiguousarray(img, dtype=np.float64)
+    H, W = img.shape
+    r = default_radius(sigma) if r is None else r
+    tb = taps(sigma, r)
+    d9 = np.zeros((9, 2 * H, 2 * W), np.float64)
+    lib().toed_oracle_planes(_ptr(img), H, W, int(r), _ptr(tb), int(nthreads), None, None, None,
+                             None, _ptr(d9))
+    return d9
+
+
+def subpix_to_correct(E, thresh: float = 0.1, sigma: float = 2.0, nbr_radius: float = 2.0,
+                      theta=None, nthreads: int = 0, dense: bool = False, debug: bool = False):
+    """FP64 subpixel TO correction (interp_n = 0).  Returns dict(edges=(N,4)
+    [, TO_E, TO_O] [, nms=(4,h,w), theta=(h,w), planes10=(10,h,w)])."""
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    h, w = E.shape
+    th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+    cap = h * w
+    edges = np.zeros((cap, 4), np.float64)
+    TE = np.zeros((h, w)) if dense else None
+    TO = np.zeros((h, w)) if dense else None
+    nms = np.zeros((4, h, w)) if debug else None
+    tho = np.zeros((h, w)) if debug else None
+    p10 = np.zeros((10, h, w)) if debug else None
+    n = lib().subpix_oracle_run(_ptr(E), h, w, float(thresh), float(sigma), float(nbr_radius),
+                                _ptr(th), int(nthreads), _ptr(edges), cap, _ptr(TE), _ptr(TO),
+                                _ptr(nms), _ptr(tho), _ptr(p10))
+    out = {"edges": edges[:n].copy()}
+    if dense:
+        out["TO_E"], out["TO_O"] = TE, TO
+    if debug:
+        out["nms"], out["theta"], out["planes10"] = nms, tho, p10
+    return out
+
+
+# --------------------------------------------------------------------------
+# The reference itself (only where its sources exist: make -C oracle ref)
+# --------------------------------------------------------------------------
+def ref_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libref_toed.so"))
+
+
+def ref_lib():
+    global _REF
+    if _REF is None:
+        L = ctypes.CDLL(os.path.join(_HERE, "_ref", "libref_toed.so"))
+        L.ref_toed_detect_u8.argtypes = [
+            ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _dp,
+            ctypes.c_long, _dp, _dp, _dp]
+        L.ref_toed_detect_u8.restype = ctypes.c_long
+        L.ref_subpix_to_correct.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+            ctypes.c_double, _dp, ctypes.c_char_p, _dp, ctypes.c_long, _dp, _dp, _dp, _dp]
+        L.ref_subpix_to_correct.restype = ctypes.c_long
+        _REF = L
+    return _REF
+
+
+def ref_detect_u8(img_u8, nthreads: int = 0, planes: bool = False):
+    """The reference's ThirdOrderEdgeDetectionCPU<double> at sigma 2 / kernel 17."""
+    img = np.ascontiguousarray(img_u8, dtype=np.uint8)
+    H, W = img.shape
+    cap = 4 * H * W
+    edges = np.zeros((cap, 4), np.float64)
+    pl = np.zeros((4, 2 * H, 2 * W)) if planes else None
+    pm = np.zeros((3, 2 * H, 2 * W)) if planes else None
+    t = np.zeros(2)
+    nt = nthreads if nthreads > 0 else os.cpu_count()
+    with tempfile.TemporaryDirectory() as d:
+        n = ref_lib().ref_toed_detect_u8(img.ctypes.data, H, W, nt, d.encode(), _ptr(edges), cap,
+                                         _ptr(pl), _ptr(pm), _ptr(t))
+    if n < 0:
+        raise RuntimeError("reference harness IO error")
+    out = {"edges": edges[:n].copy(), "time_conv": t[0], "time_nms": t[1]}
+    if planes:
+        out["planes"], out["posmaps"] = pl, pm
+    return out
+
+
+def ref_subpix_to_correct(E, thresh=0.1, sigma=2.0, nbr_radius=2.0, theta=None, nthreads=0,
+                          dense=False):
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    h, w = E.shape
+    th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+    cap = h * w
+    edges = np.zeros((cap, 4))
+    TE = np.zeros((h, w)) if dense else None
+    TO = np.zeros((h, w)) if dense else None
+    tho = np.zeros((h, w))
+    times = np.zeros(4)
+    nt = nthreads if nthreads > 0 else os.cpu_count()
+    with tempfile.TemporaryDirectory() as d:
+        n = ref_lib().ref_subpix_to_correct(_ptr(E), h, w, float(thresh), float(sigma), nt,
+                                            float(nbr_radius), _ptr(th), d.encode(), _ptr(edges),
+                                            cap, _ptr(TE), _ptr(TO), _ptr(tho), _ptr(times))
+    out = {"edges": edges[:n].copy(), "theta": tho, "times": times}
+    if dense:
+        out["TO_E"], out["TO_O"] = TE, TO
+    return out
