@@ -1,0 +1,148 @@
+/*
+ * toed_gb300.h -- C ABI of the GB300-native Third-Order Edge Detector (TOED).
+ *
+ * Plain C: pointers, sizes and a cudaStream_t; no C++ or framework types.
+ * Every entry point returns a toed_status immediately (host-side argument
+ * and launch errors).  Device-side conditions (an image with more edgels
+ * than its capacity, a staging overflow) are recorded in device flags that
+ * toed_device_flags() reads back.
+ *
+ * Reference interfaces replaced (paths relative to the reference project):
+ *   toed_detect / toed_detect_batch
+ *       ThirdOrderEdgeDetectionGPU<T>::convolve_img()            gpu_toed.hpp:340-413
+ *       ThirdOrderEdgeDetectionGPU<T>::non_maximum_suppresion()  gpu_toed.hpp:415-441
+ *       (with the host compaction build_edge_list               gpu_toed.hpp:313-338)
+ *       and its CPU twin ThirdOrderEdgeDetectionCPU<T>          cpu_toed.cpp:128-545
+ *       Output: N x 4 edgels [x, y, orientation, strength], row-major over
+ *       the 2x grid, x = (pos_x - 1)/2, y = (pos_y - 1)/2 (cpu_toed.cpp:510-538).
+ *   toed_convolve_planes
+ *       gpu_convolve(device_id, h, w, interp_h, interp_w, dev_img, dev_Ix, ...)
+ *                                                               gpu_kernels.hpp:24-45
+ *   toed_nms_planes
+ *       gpu_nms(device_id, interp_h, interp_w, dev_Ix, dev_Iy, dev_I_grad_mag,
+ *               dev_subpix_pos_x_map, dev_subpix_pos_y_map)     gpu_kernels.hpp:48-63
+ *   toed_subpix_to_correct_batch
+ *       SubpixelTOCorrectionCPU<T>::estimate_orientation() / run()
+ *                                     subpix_TO_correction/subpix_to_correction.hpp:80-96
+ *   toed_backward
+ *       no reference counterpart (the reference has no gradients); adjoint of
+ *       toed_detect with the selection mask held fixed.
+ */
+#ifndef TOED_GB300_H
+#define TOED_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+#include <cuda_runtime_api.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TOED_ABI_VERSION 1
+#define TOED_MAX_RADIUS 12 /* kernel half-width r = ceil(4 sigma) <= 12, i.e. sigma <= 3 */
+
+typedef enum toed_status {
+    TOED_OK = 0,
+    TOED_ERR_INVALID_ARG = 1, /* null pointer, bad size, sigma <= 0, r out of range ... */
+    TOED_ERR_CAPACITY = 2,    /* scratch or output capacity too small (counts stay exact) */
+    TOED_ERR_CUDA = 3,        /* a CUDA runtime call failed; see toed_last_cuda_error */
+    TOED_ERR_TIMEOUT = 4,     /* a bounded device wait gave up */
+    TOED_ERR_UNSUPPORTED = 5, /* e.g. radius above TOED_MAX_RADIUS, dtype not handled */
+    TOED_ERR_CAPTURE = 6      /* scratch would have to grow while the stream is being captured */
+} toed_status;
+
+typedef enum toed_dtype {
+    TOED_U8 = 0,  /* unsigned 8-bit pixels (the reference's input, cpu_toed.cpp:68,103) */
+    TOED_F32 = 1, /* float32 pixels */
+    TOED_F64 = 2  /* float64 (edgel output and compatibility planes only) */
+} toed_dtype;
+
+typedef enum toed_precision {
+    TOED_HYBRID = 0, /* FP32 convolutions; FP64 peak fit and TO orientation per edgel */
+    TOED_FP32 = 1    /* everything FP32 (precision-study mode) */
+} toed_precision;
+
+/* Device flags (toed_device_flags) */
+#define TOED_FLAG_OVER_CAPACITY 0x1 /* some image found more edgels than its capacity */
+#define TOED_FLAG_STAGING_FULL 0x2  /* the context staging buffer overflowed */
+
+typedef struct toed_ctx toed_ctx;
+
+/* One image of a detection batch.  All pointers are device pointers. */
+typedef struct toed_image {
+    const void* pixels; /* height x pitch elements of `dtype`, row-major */
+    int height;
+    int width;
+    int pitch;          /* elements between row starts, >= width */
+    int dtype;          /* TOED_U8 or TOED_F32 */
+    void* edgels;       /* capacity x 4 of params->out_dtype: x, y, orientation, strength */
+    int capacity;       /* edgels the buffer holds; the reference sizes it (2H)(2W) */
+    int* count;         /* 1 int: number of edgels found (exact even when > capacity) */
+    int* grid_index;    /* optional (NULL): per edgel, 2x-grid linear index row*(2W)+col */
+} toed_image;
+
+typedef struct toed_params {
+    float sigma;       /* Gaussian scale (reference: int 2, main_cpu_DP.cpp:183) */
+    int radius;        /* half-width r; 0 -> ceil(4 sigma) (kernel 17 at sigma 2) */
+    float threshold;   /* |grad I| <= threshold is skipped; reference literal 2 (cpu_toed.cpp:403) */
+    int border;        /* NMS skips a border of this many 2x-grid points; reference 10 (cpu_toed.cpp:400) */
+    int out_dtype;     /* TOED_F32 (16-byte edgels) or TOED_F64 (32-byte edgels) */
+    int precision;     /* toed_precision */
+} toed_params;
+
+/* Fill `p` with the reference's configuration for a given sigma. */
+void toed_params_default(toed_params* p, float sigma);
+
+const char* toed_status_string(toed_status s);
+const char* toed_last_cuda_error(void); /* text of the last CUDA error seen by this thread */
+
+/* Context: per-device scratch (work queue, staging, row-segment table).
+ * Replaces the buffers ThirdOrderEdgeDetectionGPU allocates in its
+ * constructor (gpu_toed.hpp:79-135); callers own images and outputs. */
+toed_status toed_create(toed_ctx** ctx, int device);
+toed_status toed_destroy(toed_ctx* ctx);
+/* Pre-size scratch so that later calls (e.g. under stream capture) never
+ * allocate: total pixels, total edgel capacity and images per call. */
+toed_status toed_reserve(toed_ctx* ctx, long long max_pixels, long long max_edgels, int max_images);
+
+/* Fused detection of one image / a batch of images of any sizes in one
+ * persistent launch (plus a short ordering pass).  Asynchronous on
+ * `stream`; graph-capturable once scratch is reserved. */
+toed_status toed_detect(toed_ctx* ctx, const toed_image* image, const toed_params* params,
+                        cudaStream_t stream);
+toed_status toed_detect_batch(toed_ctx* ctx, const toed_image* images, int n_images,
+                              const toed_params* params, cudaStream_t stream);
+
+/* Synchronises `stream` and returns the OR of the device flags of the last
+ * detection on this context (0 = all images fit their capacities). */
+toed_status toed_device_flags(toed_ctx* ctx, cudaStream_t stream, int* flags);
+
+/* Measurement hooks (used by bench.py).
+ * toed_profile_events: when both events are non-null, every following
+ * detection on `ctx` records `start` just before and `stop` just after its
+ * fused detection kernel (on the call's stream), so the kernel's own device
+ * time can be read with cudaEventElapsedTime; pass NULLs to stop.
+ * toed_peak_probe: times a register-resident FMA loop on all SMs and returns
+ * the sustained FP32 (kind 0) or FP64 (kind 1) rate in TFLOP/s -- the
+ * denominator of the FP32 roofline, measured at the clocks of the run. */
+toed_status toed_profile_events(toed_ctx* ctx, cudaEvent_t start, cudaEvent_t stop);
+toed_status toed_peak_probe(int kind, int iters, cudaStream_t stream, double* tflops);
+
+/* Compatibility: the reference's dense two-kernel form.
+ * toed_convolve_planes writes Ix, Iy, |grad I| and the TO orientation on the
+ * 2x grid ((2h) x (2w) row-major, dtype planes_dtype = TOED_F32 or TOED_F64,
+ * the latter computed in FP64 throughout); toed_nms_planes writes the subpixel
+ * position maps (zero where no edgel), as gpu_convolve / gpu_nms do. */
+toed_status toed_convolve_planes(const void* pixels, int dtype, int h, int w, int pitch,
+                                 float sigma, int radius, int planes_dtype, void* Ix, void* Iy,
+                                 void* grad_mag, void* orient, cudaStream_t stream);
+toed_status toed_nms_planes(int planes_dtype, int interp_h, int interp_w, const void* Ix,
+                            const void* Iy, const void* grad_mag, float threshold, int border,
+                            void* pos_x_map, void* pos_y_map, cudaStream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TOED_GB300_H */

@@ -1,0 +1,188 @@
+"""GPU parity of the fused detection path (toed_detect / toed_detect_batch)
+against the FP64 oracle and the reference's golden fixtures.
+
+Tolerances (the targets of the FP32-convolution / FP64-epilogue design):
+edgel-set agreement >= 99.9 % (matched by 2x-grid index), position error
+<= 1e-3 px, orientation error <= 1e-4 rad (wrapped), strength relative error
+<= 1e-4.  Small fixtures must agree exactly as sets.
+"""
+import glob
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, compare_edgels, golden
+
+pytestmark = pytest.mark.gpu
+
+AGREE, POS, ORI, STR = 0.999, 1e-3, 1e-4, 1e-4
+
+
+def _torch():
+    import torch
+    return torch
+
+
+def _run(detector, img, sigma, **kw):
+    t = _torch()
+    x = t.as_tensor(np.ascontiguousarray(img)).cuda()
+    r = detector.detect(x, sigma=sigma, **kw)
+    e = r["edgels"].double().cpu().numpy()
+    i = r["index"].cpu().numpy()
+    return r["count"], e, i
+
+
+def _check(ref, got_e, got_i, exact_set=False, agree=AGREE):
+    m = compare_edgels(ref["edges"], ref["index"], got_e, got_i)
+    if exact_set:
+        assert m["n_ref"] == m["n_got"] == m["n_common"], m
+    assert m["agreement"] >= agree, m
+    assert m["pos_max"] <= POS, m
+    assert m["ori_max"] <= ORI, m
+    assert m["str_rel_max"] <= STR, m
+    return m
+
+
+TOED_CASES = sorted(os.path.basename(p)[5:-4] for p in glob.glob(os.path.join(GOLDEN, "toed_*.npz")))
+
+
+@pytest.mark.parametrize("case", TOED_CASES)
+def test_golden_fixtures(detector, oracle, case):
+    g = golden("toed_" + case)
+    img = g["image"]
+    # the oracle reproduces the fixture bit for bit; it supplies the indices
+    ref = oracle.detect(img.astype(np.float64), 2.0)
+    assert np.nanmax(np.abs(ref["edges"] - g["edges"])) < 1e-10 if len(g["edges"]) else True
+    n, e, i = _run(detector, img, 2.0)
+    assert n == len(e)
+    _check(ref, e, i, exact_set=img.size <= 128 * 128)
+    # row-major order over the 2x grid, as the reference emits
+    assert np.all(np.diff(i) > 0)
+
+
+@pytest.mark.parametrize("sigma", [1.0, 1.5, 2.0, 2.5, 3.0])
+@pytest.mark.parametrize("dtype", [np.uint8, np.float32])
+def test_sigma_and_dtype(detector, oracle, synth, sigma, dtype):
+    img = synth.shapes_image(150, 211, seed=int(sigma * 10) + (dtype == np.uint8), dtype=dtype).image
+    ref = oracle.detect(img.astype(np.float64), sigma)
+    n, e, i = _run(detector, img, sigma)
+    _check(ref, e, i)
+
+
+@pytest.mark.parametrize("radius", [1, 2, 3, 5, 7, 9, 10, 11, 12])
+def test_every_radius(detector, oracle, synth, radius):
+    sigma = radius / 4.0
+    img = synth.shapes_image(96, 100, seed=300 + radius, dtype=np.float32).image
+    ref = oracle.detect(img.astype(np.float64), sigma, radius)
+    n, e, i = _run(detector, img, sigma, radius=radius)
+    _check(ref, e, i)
+
+
+def test_config1_752x480(detector, oracle, synth):
+    img = synth.shapes_image(480, 752, seed=1).image
+    for sigma in (1.0, 2.0):
+        ref = oracle.detect(img.astype(np.float64), sigma)
+        n, e, i = _run(detector, img, sigma)
+        m = _check(ref, e, i)
+        assert m["n_ref"] > 1000
+
+
+@pytest.mark.parametrize("H,W", [(1, 1), (5, 7), (11, 11), (12, 40), (31, 29), (33, 61), (17, 300),
+                                 (300, 17), (64, 30), (64, 31), (126, 30), (127, 91)])
+def test_ragged_sizes(detector, oracle, synth, H, W):
+    img = synth.shapes_image(H, W, seed=H * 1000 + W, n_shapes=3, radius_range=(3, 20),
+                             scale_to_base=False, dtype=np.float32).image
+    ref = oracle.detect(img.astype(np.float64), 1.5)
+    n, e, i = _run(detector, img, 1.5)
+    _check(ref, e, i, exact_set=True)
+
+
+def test_threshold_and_border(detector, oracle, synth):
+    img = synth.shapes_image(90, 120, seed=77, dtype=np.float32).image
+    for thr, border in [(0.5, 10), (5.0, 10), (2.0, 25)]:
+        ref = oracle.detect(img.astype(np.float64), 1.5, threshold=thr)
+        if border != 10:
+            H2, W2 = 180, 240
+            rows, cols = ref["index"] // W2, ref["index"] % W2
+            # the oracle's border is the reference literal 10; a wider border is a subset
+            keep = (rows >= border) & (rows < H2 - border) & (cols >= border) & (cols < W2 - border)
+            ref = {"edges": ref["edges"][keep], "index": ref["index"][keep]}
+        n, e, i = _run(detector, img, 1.5, threshold=thr, border=border)
+        _check(ref, e, i)
+
+
+def test_pitch_and_batch(detector, oracle, synth):
+    t = _torch()
+    sizes = [(64, 100), (200, 47), (33, 33), (257, 129), (90, 301)]
+    imgs = [synth.shapes_image(h, w, seed=900 + k, dtype=np.float32).image for k, (h, w) in enumerate(sizes)]
+    # image 0 lives inside a wider buffer (pitch > width)
+    big = t.zeros((64, 160), dtype=t.float32, device="cuda")
+    big[:, :100] = t.as_tensor(imgs[0])
+    tens = [big[:, :100]] + [t.as_tensor(im).cuda() for im in imgs[1:]]
+    res = detector.detect_batch(tens, sigma=1.5)
+    for im, r in zip(imgs, res):
+        ref = oracle.detect(im.astype(np.float64), 1.5)
+        _check(ref, r["edgels"].double().cpu().numpy(), r["index"].cpu().numpy())
+    # a batch equals the same images run one by one, bit for bit
+    for im, r in zip(tens, res):
+        s = detector.detect(im.contiguous(), sigma=1.5)
+        assert t.equal(s["edgels"], r["edgels"]) and t.equal(s["index"], r["index"])
+
+
+def test_f64_output_and_fp32_mode(detector, oracle, synth, toed):
+    img = synth.shapes_image(120, 160, seed=55, dtype=np.float32).image
+    ref = oracle.detect(img.astype(np.float64), 2.0)
+    n, e, i = _run(detector, img, 2.0, out_dtype=toed.TOED_F64)
+    m64 = _check(ref, e, i)
+    n, e, i = _run(detector, img, 2.0, precision=toed.TOED_FP32)
+    m32 = _check(ref, e, i)
+    assert m64["n_common"] > 100 and m32["n_common"] > 100
+
+
+def test_capacity_overflow(detector, synth, toed):
+    t = _torch()
+    img = t.as_tensor(synth.shapes_image(100, 100, seed=5).image).cuda()
+    full = detector.detect(img, sigma=1.0)
+    n = full["count"]
+    assert n > 20
+    part = detector.detect(img, sigma=1.0, capacity=10)
+    assert part["count"] == n  # exact count even past capacity
+    assert t.equal(part["edgels"], full["edgels"][:10])
+    assert detector.flags() & toed.TOED_FLAG_OVER_CAPACITY
+    detector.detect(img, sigma=1.0)
+    assert detector.flags() == 0
+
+
+def test_deterministic(detector, synth):
+    t = _torch()
+    img = t.as_tensor(synth.shapes_image(300, 400, seed=8, dtype=np.float32).image).cuda()
+    a = detector.detect(img, sigma=1.5)
+    b = detector.detect(img, sigma=1.5)
+    assert t.equal(a["edgels"], b["edgels"]) and t.equal(a["index"], b["index"])
+
+
+def test_invalid_arguments(detector, toed):
+    t = _torch()
+    img = t.zeros((16, 16), dtype=t.float32, device="cuda")
+    with pytest.raises(toed.ToedError):
+        detector.detect(img, sigma=0.0)
+    with pytest.raises(toed.ToedError):
+        detector.detect(img, sigma=4.0)  # r = 16 > 12
+    with pytest.raises(ValueError):
+        detector.detect(img.double(), sigma=1.0)
+
+
+def test_reference_class_mirror(toed, oracle, synth, tmp_path):
+    img = synth.shapes_image(80, 120, seed=9).image
+    d = toed.ThirdOrderEdgeDetectionGPU(0, 80, 120, 17, 2, dtype="double")
+    d.set_output_dir(str(tmp_path))
+    d.preprocessing(img)
+    d.convolve_img()
+    buf = np.zeros((4 * 80 * 120, 4))
+    n = d.non_maximum_suppresion(buf)
+    ref = oracle.detect(img.astype(np.float64), 2.0)
+    assert n == len(ref["edges"])
+    assert np.abs(buf[:n, :2] - ref["edges"][:, :2]).max() < 1e-3
+    assert os.path.exists(os.path.join(str(tmp_path), "data_final_output_gpu.txt"))
+    assert d.time_conv > 0

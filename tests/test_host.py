@@ -1,0 +1,96 @@
+"""CPU-only tests: the C ABI library builds for sm_103a, loads without a GPU
+and exports every symbol include/toed_gb300.h declares; the ctypes mirror of
+the ABI structs matches the C layout; host-side helpers behave."""
+import ctypes
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+HEADER = os.path.join(ROOT, "include", "toed_gb300.h")
+
+
+def _declared_functions():
+    src = open(HEADER).read()
+    src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+    return sorted(set(re.findall(r"\b(toed_[a-z_0-9]+)\s*\(", src)))
+
+
+def test_library_builds_and_exports_header_symbols(toed):
+    path = toed.build()
+    assert os.path.exists(path)
+    L = ctypes.CDLL(path)
+    decl = _declared_functions()
+    assert len(decl) >= 11
+    for name in decl:
+        assert hasattr(L, name), name
+    assert sorted(toed.C_SYMBOLS) == sorted(n for n in decl if n in toed.C_SYMBOLS)
+    assert set(decl) <= set(toed.C_SYMBOLS) | set(getattr(toed, "C_SYMBOLS_EXTRA", []))
+
+
+def test_status_strings(toed):
+    toed.build()
+    L = toed.lib()
+    for s in range(7):
+        assert toed.status_string(s)
+    assert L.toed_status_string(99).decode() == "unknown status"
+    p = toed.toed_params()
+    L.toed_params_default(ctypes.byref(p), ctypes.c_float(2.0))
+    assert (p.sigma, p.radius, p.threshold, p.border) == (2.0, 0, 2.0, 10)
+
+
+def test_struct_layout_matches_header(toed, tmp_path):
+    c = tmp_path / "layout.c"
+    c.write_text("""
+#include <stdio.h>
+#include <stddef.h>
+#include "toed_gb300.h"
+int main(void) {
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(toed_image), offsetof(toed_image, dtype),
+         offsetof(toed_image, edgels), offsetof(toed_image, capacity), offsetof(toed_image, count),
+         offsetof(toed_image, grid_index), sizeof(toed_params), offsetof(toed_params, precision));
+  return 0;
+}
+""")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), "-I/usr/local/cuda/include", str(c), "-o",
+                    str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
+    T, P = toed.toed_image, toed.toed_params
+    want = [ctypes.sizeof(T), T.dtype.offset, T.edgels.offset, T.capacity.offset, T.count.offset,
+            T.grid_index.offset, ctypes.sizeof(P), P.precision.offset]
+    assert got == want
+
+
+def test_no_cpu_fallback(toed, monkeypatch):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(RuntimeError, match="no CPU fallback"):
+        toed.Detector(0)
+
+
+def test_synth_deterministic(synth):
+    a = synth.shapes_image(60, 80, seed=3).image
+    b = synth.shapes_image(60, 80, seed=3).image
+    assert a.dtype == np.uint8 and np.array_equal(a, b)
+    f = synth.shapes_image(60, 80, seed=3, dtype=np.float32).image
+    assert f.dtype == np.float32 and f.min() >= 0 and f.max() <= 255
+    sizes = synth.uneven_batch_shapes()
+    assert len(sizes) == 64 and all(h % 4 == 0 and w % 4 == 0 and 256 <= h <= 2048 for h, w in sizes)
+    E = synth.ridge_map(64, 64, seed=1, n_curves=3)
+    assert E.min() >= 0 and E.max() <= 1
+
+
+def test_ellipse_distance(synth):
+    e = synth.Ellipse(10.0, 20.0, 8.0, 3.0, 0.3, 100.0)
+    t = np.linspace(0, 2 * np.pi, 50)
+    c, s = np.cos(e.theta), np.sin(e.theta)
+    bx = e.cx + e.a * np.cos(t) * c - e.b * np.sin(t) * s
+    by = e.cy + e.a * np.cos(t) * s + e.b * np.sin(t) * c
+    assert np.abs(synth.ellipse_distance(bx, by, e)).max() < 1e-9
+    assert abs(synth.ellipse_distance(np.array([10.0]), np.array([20.0]), e)[0] - 3.0) < 1e-9

@@ -1,0 +1,371 @@
+"""GB300-native Third-Order Edge Detector (TOED) hot path.
+
+Python host mirror of the reference's detection interface over the C ABI in
+include/toed_gb300.h.  The compute path is the CUDA library
+``libtoed_gb300.so`` built in-tree for sm_103a by ``build.py``; there is no
+CPU fallback: every entry point raises if the library is not built or no GPU
+is present.  PyTorch is used only for device memory and streams.
+
+Public API (names follow the reference):
+
+* ``ThirdOrderEdgeDetectionGPU``  -- class mirror of the reference's
+  ThirdOrderEdgeDetectionGPU<T> (gpu_toed.hpp:21-74): ctor(device, H, W,
+  kernel_size, sigma), preprocessing(image), convolve_img(),
+  non_maximum_suppresion() -> N, with ``TOED_edges`` / ``time_conv`` /
+  ``time_nms``.
+* ``detect`` / ``detect_batch``   -- functional form on torch tensors.
+* ``Detector``                    -- reusable context (scratch, CUDA graphs).
+"""
+from __future__ import annotations
+
+import ctypes
+import math
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libtoed_gb300.so")
+
+TOED_OK, TOED_ERR_INVALID_ARG, TOED_ERR_CAPACITY, TOED_ERR_CUDA, TOED_ERR_TIMEOUT, \
+    TOED_ERR_UNSUPPORTED, TOED_ERR_CAPTURE = range(7)
+TOED_U8, TOED_F32, TOED_F64 = 0, 1, 2
+TOED_HYBRID, TOED_FP32 = 0, 1
+TOED_FLAG_OVER_CAPACITY, TOED_FLAG_STAGING_FULL = 1, 2
+MAX_RADIUS = 12
+
+# exported C symbols (checked by tests against include/toed_gb300.h)
+C_SYMBOLS = [
+    "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
+    "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
+    "toed_convolve_planes", "toed_nms_planes", "toed_profile_events", "toed_peak_probe",
+]
+
+
+class ToedError(RuntimeError):
+    def __init__(self, status: int, what: str = ""):
+        self.status = status
+        super().__init__(f"{what}: {status_string(status)} ({status})")
+
+
+class toed_image(ctypes.Structure):
+    _fields_ = [
+        ("pixels", ctypes.c_void_p), ("height", ctypes.c_int), ("width", ctypes.c_int),
+        ("pitch", ctypes.c_int), ("dtype", ctypes.c_int), ("edgels", ctypes.c_void_p),
+        ("capacity", ctypes.c_int), ("count", ctypes.c_void_p), ("grid_index", ctypes.c_void_p),
+    ]
+
+
+class toed_params(ctypes.Structure):
+    _fields_ = [
+        ("sigma", ctypes.c_float), ("radius", ctypes.c_int), ("threshold", ctypes.c_float),
+        ("border", ctypes.c_int), ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+_LIB = None
+
+
+def build(verbose: bool = False) -> str:
+    """Compile libtoed_gb300.so (nvcc, sm_103a) in-tree."""
+    sys.path.insert(0, HERE)
+    try:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("_toed_build", os.path.join(HERE, "build.py"))
+        m = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(m)
+        return m.build(verbose=verbose)
+    finally:
+        sys.path.remove(HERE)
+
+
+def lib():
+    """The loaded CUDA library (raises if it has not been built)."""
+    global _LIB
+    if _LIB is None:
+        if not os.path.exists(LIB_PATH):
+            raise RuntimeError(f"CUDA library not built: {LIB_PATH} (call build())")
+        L = ctypes.CDLL(LIB_PATH)
+        vp, ip, i64 = ctypes.c_void_p, ctypes.c_int, ctypes.c_longlong
+        L.toed_status_string.restype = ctypes.c_char_p
+        L.toed_status_string.argtypes = [ip]
+        L.toed_last_cuda_error.restype = ctypes.c_char_p
+        L.toed_params_default.argtypes = [ctypes.POINTER(toed_params), ctypes.c_float]
+        L.toed_create.argtypes = [ctypes.POINTER(vp), ip]
+        L.toed_destroy.argtypes = [vp]
+        L.toed_reserve.argtypes = [vp, i64, i64, ip]
+        L.toed_detect.argtypes = [vp, ctypes.POINTER(toed_image), ctypes.POINTER(toed_params), vp]
+        L.toed_detect_batch.argtypes = [vp, ctypes.POINTER(toed_image), ip,
+                                        ctypes.POINTER(toed_params), vp]
+        L.toed_device_flags.argtypes = [vp, vp, ctypes.POINTER(ip)]
+        L.toed_convolve_planes.argtypes = [vp, ip, ip, ip, ip, ctypes.c_float, ip, ip, vp, vp, vp, vp,
+                                           vp]
+        L.toed_nms_planes.argtypes = [ip, ip, ip, vp, vp, vp, ctypes.c_float, ip, vp, vp, vp]
+        L.toed_profile_events.argtypes = [vp, vp, vp]
+        L.toed_peak_probe.argtypes = [ip, ip, vp, ctypes.POINTER(ctypes.c_double)]
+        for name in C_SYMBOLS:
+            if name not in ("toed_status_string", "toed_last_cuda_error", "toed_params_default"):
+                getattr(L, name).restype = ip
+        L.toed_params_default.restype = None
+        _LIB = L
+    return _LIB
+
+
+def status_string(st: int) -> str:
+    try:
+        return lib().toed_status_string(int(st)).decode()
+    except Exception:  # library not loadable: still give a readable message
+        return {0: "ok", 1: "invalid argument", 2: "capacity exceeded", 3: "CUDA error",
+                4: "device wait timed out", 5: "unsupported configuration",
+                6: "scratch must grow during stream capture"}.get(int(st), "unknown")
+
+
+def _check(st: int, what: str):
+    if st != TOED_OK:
+        msg = what
+        if st == TOED_ERR_CUDA:
+            msg += " [" + lib().toed_last_cuda_error().decode() + "]"
+        raise ToedError(st, msg)
+
+
+def peak_probe(kind: int = 0, iters: int = 200000, stream=None) -> float:
+    """Measured FP32 (kind 0) or FP64 (kind 1) FMA rate in TFLOP/s."""
+    t = _torch()
+    s = stream if stream is not None else t.cuda.current_stream()
+    out = ctypes.c_double(0.0)
+    _check(lib().toed_peak_probe(int(kind), int(iters), ctypes.c_void_p(s.cuda_stream), ctypes.byref(out)),
+           "toed_peak_probe")
+    return out.value
+
+
+def default_radius(sigma: float) -> int:
+    """r = ceil(4 sigma): kernel 17 at sigma 2 (cpu_toed.cpp:131, main_cpu_DP.cpp:182)."""
+    return int(math.ceil(4.0 * sigma))
+
+
+def _torch():
+    import torch
+    if not torch.cuda.is_available():
+        raise RuntimeError("TOED GB300 path needs a CUDA device; there is no CPU fallback")
+    return torch
+
+
+def make_params(sigma=2.0, radius=0, threshold=2.0, border=10, out_dtype=TOED_F32,
+                precision=TOED_HYBRID) -> toed_params:
+    return toed_params(float(sigma), int(radius), float(threshold), int(border), int(out_dtype),
+                       int(precision))
+
+
+class Detector:
+    """A detection context on one device: owns the scratch of the fused
+    kernel and (optionally) caches CUDA graphs of fixed batches."""
+
+    def __init__(self, device: int = 0):
+        self.torch = _torch()
+        self.device = int(device)
+        self._ctx = ctypes.c_void_p()
+        with self.torch.cuda.device(self.device):
+            _check(lib().toed_create(ctypes.byref(self._ctx), self.device), "toed_create")
+
+    def close(self):
+        if self._ctx:
+            lib().toed_destroy(self._ctx)
+            self._ctx = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def reserve(self, max_pixels: int, max_edgels: int, max_images: int):
+        _check(lib().toed_reserve(self._ctx, int(max_pixels), int(max_edgels), int(max_images)),
+               "toed_reserve")
+
+    def profile_events(self, start=None, stop=None):
+        """Record ``start``/``stop`` (torch.cuda.Event) around the fused
+        detection kernel of every following call; ``None`` disables."""
+        a = ctypes.c_void_p(start.cuda_event) if start is not None else None
+        b = ctypes.c_void_p(stop.cuda_event) if stop is not None else None
+        _check(lib().toed_profile_events(self._ctx, a, b), "toed_profile_events")
+
+    def flags(self, stream=None) -> int:
+        f = ctypes.c_int(0)
+        s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
+        _check(lib().toed_device_flags(self._ctx, ctypes.c_void_p(s.cuda_stream), ctypes.byref(f)),
+               "toed_device_flags")
+        return f.value
+
+    # ------------------------------------------------------------------
+    def alloc_outputs(self, shapes, capacity=None, out_dtype=TOED_F32, index=True):
+        """Edgel / count / index buffers for images of the given (H, W)."""
+        t = self.torch
+        dt = t.float64 if out_dtype == TOED_F64 else t.float32
+        outs = []
+        for (H, W) in shapes:
+            cap = int(capacity) if capacity is not None else 4 * H * W
+            outs.append({
+                "edgels": t.empty((max(cap, 1), 4), dtype=dt, device=f"cuda:{self.device}"),
+                "count": t.zeros(1, dtype=t.int32, device=f"cuda:{self.device}"),
+                "index": t.empty(max(cap, 1), dtype=t.int32, device=f"cuda:{self.device}")
+                if index else None,
+                "capacity": cap,
+            })
+        return outs
+
+    def _image_struct(self, img, out):
+        t = self.torch
+        if img.dim() != 2 or img.device.type != "cuda":
+            raise ValueError("images must be 2-D CUDA tensors")
+        if img.dtype == t.uint8:
+            dt = TOED_U8
+        elif img.dtype == t.float32:
+            dt = TOED_F32
+        else:
+            raise ValueError("image dtype must be uint8 or float32")
+        if img.stride(1) != 1:
+            raise ValueError("image rows must be contiguous")
+        H, W = img.shape
+        return toed_image(img.data_ptr(), H, W, img.stride(0), dt, out["edgels"].data_ptr(),
+                          out["capacity"], out["count"].data_ptr(),
+                          out["index"].data_ptr() if out.get("index") is not None else None)
+
+    def detect_into(self, images, outs, params: toed_params, stream=None):
+        """Launch detection of ``images`` into preallocated ``outs`` (async)."""
+        n = len(images)
+        arr = (toed_image * n)(*[self._image_struct(im, o) for im, o in zip(images, outs)])
+        s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
+        _check(lib().toed_detect_batch(self._ctx, arr, n, ctypes.byref(params),
+                                       ctypes.c_void_p(s.cuda_stream)), "toed_detect_batch")
+
+    def detect_batch(self, images, sigma=2.0, threshold=2.0, radius=0, border=10,
+                     out_dtype=TOED_F32, precision=TOED_HYBRID, capacity=None, index=True,
+                     stream=None):
+        """Detect edgels in a list of 2-D CUDA tensors.  Returns a list of
+        dicts with ``edgels`` (N x 4: x, y, orientation, strength) and,
+        with ``index``, the 2x-grid linear index of each edgel."""
+        p = make_params(sigma, radius, threshold, border, out_dtype, precision)
+        outs = self.alloc_outputs([tuple(im.shape) for im in images], capacity, out_dtype, index)
+        self.detect_into(images, outs, p, stream)
+        s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
+        s.synchronize()
+        res = []
+        for o in outs:
+            n = int(o["count"].item())
+            m = min(n, o["capacity"])
+            r = {"count": n, "edgels": o["edgels"][:m]}
+            if index:
+                r["index"] = o["index"][:m]
+            res.append(r)
+        return res
+
+    def detect(self, image, **kw):
+        return self.detect_batch([image], **kw)[0]
+
+
+_DEFAULT = {}
+
+
+def _default_detector(device: int = 0) -> Detector:
+    d = _DEFAULT.get(device)
+    if d is None:
+        d = _DEFAULT[device] = Detector(device)
+    return d
+
+
+def detect(image, sigma=2.0, **kw):
+    """Functional single-image detection on a CUDA tensor."""
+    dev = image.device.index or 0
+    return _default_detector(dev).detect(image, sigma=sigma, **kw)
+
+
+def detect_batch(images, sigma=2.0, **kw):
+    dev = images[0].device.index or 0
+    return _default_detector(dev).detect_batch(images, sigma=sigma, **kw)
+
+
+class ThirdOrderEdgeDetectionGPU:
+    """Mirror of the reference class ThirdOrderEdgeDetectionGPU<T>
+    (gpu_toed.hpp:21-74; ctor gpu_toed.hpp:79-135).
+
+    ``dtype`` plays the role of T: "float" gives float32 edgels, "double"
+    float64 edgels (x, y keep FP64 positions).  ``sigma`` may be fractional
+    (the reference stores an int, gpu_toed.hpp:30).  The file written by the
+    reference's non_maximum_suppresion (data_final_output_gpu.txt,
+    gpu_toed.hpp:439) is written only when ``output_dir`` is set.
+    """
+
+    num_of_edge_data = 4
+
+    def __init__(self, device: int, H: int, W: int, kernel_size: int = 17, sigma: float = 2,
+                 dtype: str = "float"):
+        self.torch = _torch()
+        self.device_id, self.img_height, self.img_width = int(device), int(H), int(W)
+        self.kernel_sz = int(kernel_size)
+        self.g_sig = sigma
+        self.dtype = dtype
+        self.edge_pt_list_idx = 0
+        self.time_conv = 0.0
+        self.time_nms = 0.0
+        self.output_dir = None
+        self.TOED_edges = None
+        self._det = _default_detector(self.device_id)
+        self._img = None
+        self._res = None
+
+    def set_output_dir(self, d: str):
+        self.output_dir = d or "./output_files"
+
+    def preprocessing(self, image):
+        """image: HxW uint8/float array or tensor (the reference reads uint8,
+        gpu_toed.hpp:141-231)."""
+        t = self.torch
+        if not isinstance(image, t.Tensor):
+            image = t.as_tensor(image)
+        if image.dtype not in (t.uint8, t.float32):
+            image = image.to(t.float32)
+        if tuple(image.shape) != (self.img_height, self.img_width):
+            raise ValueError("image shape does not match the constructor's H, W")
+        self._img = image.to(f"cuda:{self.device_id}").contiguous()
+
+    def convolve_img(self):
+        """Runs the fused detection (the reference's convolution + NMS
+        kernels); ``time_conv`` gets its device time in ms."""
+        t = self.torch
+        if self._img is None:
+            raise RuntimeError("preprocessing() must be called first")
+        r = (self.kernel_sz - 1) // 2
+        od = TOED_F64 if self.dtype == "double" else TOED_F32
+        p = make_params(self.g_sig, r, 2.0, 10, od, TOED_HYBRID)
+        outs = self._det.alloc_outputs([(self.img_height, self.img_width)], None, od, True)
+        st, en = t.cuda.Event(enable_timing=True), t.cuda.Event(enable_timing=True)
+        st.record()
+        self._det.detect_into([self._img], outs, p)
+        en.record()
+        en.synchronize()
+        self.time_conv = st.elapsed_time(en)
+        self._res = outs[0]
+
+    def non_maximum_suppresion(self, TOED_edges=None) -> int:
+        """Returns N and fills ``TOED_edges`` (N x 4; also copied into the
+        caller's array when one is passed, as gpu_toed.hpp:327-332)."""
+        if self._res is None:
+            raise RuntimeError("convolve_img() must be called first")
+        t0 = self.torch.cuda.Event(enable_timing=True)
+        t1 = self.torch.cuda.Event(enable_timing=True)
+        t0.record()
+        n = int(self._res["count"].item())
+        m = min(n, self._res["capacity"])
+        edges = self._res["edgels"][:m].cpu().numpy()
+        t1.record()
+        t1.synchronize()
+        self.time_nms = t0.elapsed_time(t1)
+        self.edge_pt_list_idx = n
+        self.TOED_edges = edges
+        if TOED_edges is not None:
+            TOED_edges[:m] = edges
+        if self.output_dir:
+            os.makedirs(self.output_dir, exist_ok=True)
+            with open(os.path.join(self.output_dir, "data_final_output_gpu.txt"), "w") as f:
+                for row in edges:
+                    f.write("".join(f"{v:.10g}\t" for v in row) + "\n")
+        return n

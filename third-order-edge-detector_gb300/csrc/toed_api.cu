@@ -1,0 +1,376 @@
+// toed_api.cu -- host implementation of the C ABI declared in
+// include/toed_gb300.h: argument checks, tap generation, the per-device
+// scratch owned by a context, strip planning and kernel launches.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "toed_common.cuh"
+#include "toed_internal.h"
+
+namespace toed {
+DetectEntry detect_entry_r1(bool);
+DetectEntry detect_entry_r2(bool);
+DetectEntry detect_entry_r3(bool);
+DetectEntry detect_entry_r4(bool);
+DetectEntry detect_entry_r5(bool);
+DetectEntry detect_entry_r6(bool);
+DetectEntry detect_entry_r7(bool);
+DetectEntry detect_entry_r8(bool);
+DetectEntry detect_entry_r9(bool);
+DetectEntry detect_entry_r10(bool);
+DetectEntry detect_entry_r11(bool);
+DetectEntry detect_entry_r12(bool);
+
+DetectEntry detect_entry(int r, bool hyb)
+{
+    switch (r) {
+    case 1: return detect_entry_r1(hyb);
+    case 2: return detect_entry_r2(hyb);
+    case 3: return detect_entry_r3(hyb);
+    case 4: return detect_entry_r4(hyb);
+    case 5: return detect_entry_r5(hyb);
+    case 6: return detect_entry_r6(hyb);
+    case 7: return detect_entry_r7(hyb);
+    case 8: return detect_entry_r8(hyb);
+    case 9: return detect_entry_r9(hyb);
+    case 10: return detect_entry_r10(hyb);
+    case 11: return detect_entry_r11(hyb);
+    case 12: return detect_entry_r12(hyb);
+    default: return DetectEntry{nullptr, 0};
+    }
+}
+
+// Taps from the reference's own commented generator (cpu_toed.cpp:141-162),
+// evaluated in double and rounded once to float.
+void make_taps(double sigma, int r, TapBlock* tb)
+{
+    std::memset(tb, 0, sizeof(*tb));
+    const double nrm = std::sqrt(2.0 * 3.14159265358979323846);
+    const double s = sigma;
+    for (int sh = 0; sh < 2; ++sh) {
+        const double d = sh ? 0.5 : 0.0;
+        for (int k = 0; k < 2 * r + 3; ++k) {
+            const double x = (double)(k - (r + 1)) + d;
+            const double e = std::exp(-(x * x) / (2.0 * s * s));
+            tb->v[4 * sh + 0][k] = (float)(e / (nrm * s));
+            tb->v[4 * sh + 1][k] = (float)((-x * e) / (nrm * s * s * s));
+            tb->v[4 * sh + 2][k] = (float)(((x * x - s * s) * e) / (nrm * s * s * s * s * s));
+            tb->v[4 * sh + 3][k] = (float)(((x * (3.0 * s * s - x * x)) * e) / (nrm * s * s * s * s * s * s * s));
+        }
+    }
+}
+
+}  // namespace toed
+
+using namespace toed;
+
+static thread_local std::string g_last_cuda_error;
+
+#define TOED_CU(call)                                                                 \
+    do {                                                                              \
+        cudaError_t e_ = (call);                                                      \
+        if (e_ != cudaSuccess) {                                                      \
+            g_last_cuda_error = std::string(#call) + ": " + cudaGetErrorString(e_);   \
+            return TOED_ERR_CUDA;                                                     \
+        }                                                                             \
+    } while (0)
+
+struct toed_ctx {
+    int device = 0;
+    int num_sms = 0;
+    int* words = nullptr;  // [0] queue [1] cursor [2] flags [3] spare
+    double4_32a* staging = nullptr;
+    int* staging_idx = nullptr;
+    long long staging_cap = 0;
+    int2* seg = nullptr;
+    long long seg_cap = 0;
+    int* tile_sum = nullptr;
+    long long tile_cap = 0;
+    long long* img_base = nullptr;
+    int img_cap = 0;
+    int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
+    cudaEvent_t prof_start = nullptr, prof_stop = nullptr;
+    std::mutex mu;
+};
+
+extern "C" {
+
+void toed_params_default(toed_params* p, float sigma)
+{
+    if (!p) return;
+    p->sigma = sigma;
+    p->radius = 0;
+    p->threshold = 2.0f;
+    p->border = 10;
+    p->out_dtype = TOED_F32;
+    p->precision = TOED_HYBRID;
+}
+
+const char* toed_status_string(toed_status s)
+{
+    switch (s) {
+    case TOED_OK: return "ok";
+    case TOED_ERR_INVALID_ARG: return "invalid argument";
+    case TOED_ERR_CAPACITY: return "capacity exceeded";
+    case TOED_ERR_CUDA: return "CUDA error";
+    case TOED_ERR_TIMEOUT: return "device wait timed out";
+    case TOED_ERR_UNSUPPORTED: return "unsupported configuration";
+    case TOED_ERR_CAPTURE: return "scratch must grow during stream capture (call toed_reserve first)";
+    }
+    return "unknown status";
+}
+
+const char* toed_last_cuda_error(void) { return g_last_cuda_error.c_str(); }
+
+toed_status toed_create(toed_ctx** out, int device)
+{
+    if (!out) return TOED_ERR_INVALID_ARG;
+    *out = nullptr;
+    int ndev = 0;
+    TOED_CU(cudaGetDeviceCount(&ndev));
+    if (device < 0 || device >= ndev) return TOED_ERR_INVALID_ARG;
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    TOED_CU(cudaSetDevice(device));
+    toed_ctx* c = new toed_ctx();
+    c->device = device;
+    cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+    if (e == cudaSuccess) e = cudaMalloc(&c->words, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->words, 0, 4 * sizeof(int));
+    cudaSetDevice(prev);
+    if (e != cudaSuccess) {
+        g_last_cuda_error = cudaGetErrorString(e);
+        delete c;
+        return TOED_ERR_CUDA;
+    }
+    *out = c;
+    return TOED_OK;
+}
+
+toed_status toed_destroy(toed_ctx* c)
+{
+    if (!c) return TOED_ERR_INVALID_ARG;
+    int prev = 0;
+    cudaGetDevice(&prev);
+    cudaSetDevice(c->device);
+    cudaFree(c->words);
+    cudaFree(c->staging);
+    cudaFree(c->staging_idx);
+    cudaFree(c->seg);
+    cudaFree(c->tile_sum);
+    cudaFree(c->img_base);
+    cudaSetDevice(prev);
+    delete c;
+    return TOED_OK;
+}
+
+}  // extern "C"
+
+// Grow a device buffer; refuses while the stream is being captured.
+template <typename T>
+static toed_status grow(T** buf, long long* cap, long long need, cudaStream_t stream)
+{
+    if (need <= *cap) return TOED_OK;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (stream) cudaStreamIsCapturing(stream, &cs);
+    if (cs != cudaStreamCaptureStatusNone) return TOED_ERR_CAPTURE;
+    long long n = std::max(need, *cap + *cap / 2);
+    if (*buf) TOED_CU(cudaFree(*buf));
+    *buf = nullptr;
+    *cap = 0;
+    TOED_CU(cudaMalloc((void**)buf, sizeof(T) * (size_t)n));
+    *cap = n;
+    return TOED_OK;
+}
+
+static toed_status ensure_scratch(toed_ctx* c, long long staging, long long segs, long long tiles,
+                                  int imgs, cudaStream_t stream)
+{
+    toed_status st;
+    long long sc = c->staging_cap;
+    if ((st = grow(&c->staging, &sc, staging, stream)) != TOED_OK) return st;
+    long long sc2 = c->staging_cap;
+    if ((st = grow(&c->staging_idx, &sc2, staging, stream)) != TOED_OK) return st;
+    c->staging_cap = std::min(sc, sc2);
+    if ((st = grow(&c->seg, &c->seg_cap, segs, stream)) != TOED_OK) return st;
+    if ((st = grow(&c->tile_sum, &c->tile_cap, tiles, stream)) != TOED_OK) return st;
+    long long ic = c->img_cap;
+    if ((st = grow(&c->img_base, &ic, (long long)imgs, stream)) != TOED_OK) return st;
+    c->img_cap = (int)ic;
+    return TOED_OK;
+}
+
+extern "C" toed_status toed_reserve(toed_ctx* c, long long max_pixels, long long max_edgels, int max_images)
+{
+    if (!c || max_pixels < 0 || max_edgels < 0 || max_images < 0) return TOED_ERR_INVALID_ARG;
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    TOED_CU(cudaSetDevice(c->device));
+    // segments: 2 rows per pixel row x ceil(W/30) strip columns, bounded by pixels/15 + tiles of padding
+    const int imgs = std::min(std::max(max_images, 1), kBatchMax);
+    const long long segs = max_pixels / 15 + 2LL * 4096 + (long long)imgs * kSegTile;
+    const long long tiles = segs / kSegTile + imgs + 1;
+    std::lock_guard<std::mutex> lk(c->mu);
+    toed_status st = ensure_scratch(c, std::max(max_edgels, 1LL), segs, tiles, imgs, nullptr);
+    cudaSetDevice(prev);
+    return st;
+}
+
+static toed_status check_image(const toed_image& im)
+{
+    if (!im.pixels || !im.edgels || !im.count) return TOED_ERR_INVALID_ARG;
+    if (im.height <= 0 || im.width <= 0 || im.pitch < im.width || im.capacity < 0) return TOED_ERR_INVALID_ARG;
+    if (im.dtype != TOED_U8 && im.dtype != TOED_F32) return TOED_ERR_UNSUPPORTED;
+    if ((long long)(2LL * im.height) * (2LL * im.width) >= (1LL << 31)) return TOED_ERR_UNSUPPORTED;
+    if ((reinterpret_cast<uintptr_t>(im.edgels) & 15u) != 0) return TOED_ERR_INVALID_ARG;
+    if (im.dtype == TOED_F32 && (reinterpret_cast<uintptr_t>(im.pixels) & 3u) != 0) return TOED_ERR_INVALID_ARG;
+    return TOED_OK;
+}
+
+static int radius_of(const toed_params* p)
+{
+    if (p->radius > 0) return p->radius;
+    return (int)std::ceil(4.0 * (double)p->sigma);
+}
+
+// Strip height: the tallest multiple of the step (minus the 2-row ring) that
+// still gives every resident CTA several units to balance the queue.
+static int plan_strip_rows(const toed_image* images, int n, long long resident)
+{
+    static const int steps[] = {16, 8, 4, 2, 1};
+    for (int st : steps) {
+        const int S = st * kStepRows - 2;
+        long long units = 0;
+        for (int i = 0; i < n; ++i)
+            units += (long long)((images[i].width + kInner - 1) / kInner) * ((images[i].height + S - 1) / S);
+        if (units >= 4 * resident) return S;
+    }
+    return kStepRows - 2;
+}
+
+static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
+                                int r, bool first_chunk, cudaStream_t stream)
+{
+    const bool hyb = prm->precision != TOED_FP32;
+    DetectEntry ent = detect_entry(r, hyb);
+    if (!ent.func) return TOED_ERR_UNSUPPORTED;
+    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0];
+    if (bps == 0) {
+        TOED_CU(cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem));
+        TOED_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ent.func, kThreads, ent.smem));
+        if (bps <= 0) return TOED_ERR_UNSUPPORTED;
+    }
+    const long long resident = (long long)bps * c->num_sms;
+
+    BatchParams* p = new BatchParams();
+    std::unique_ptr<BatchParams> guard(p);
+    make_taps((double)prm->sigma, r, &p->taps);
+    p->thr = prm->threshold;
+    p->border = prm->border;
+    p->S = plan_strip_rows(images, n, resident);
+    p->n_img = n;
+    p->out_f64 = (prm->out_dtype == TOED_F64) ? 1 : 0;
+    p->radius = r;
+    long long units = 0, tiles = 0, staging = 0;
+    for (int i = 0; i < n; ++i) {
+        const toed_image& im = images[i];
+        DetImage& d = p->img[i];
+        d.src = im.pixels;
+        d.pitch = im.pitch;
+        d.out = im.edgels;
+        d.count = im.count;
+        d.index = im.grid_index;
+        d.H = im.height;
+        d.W = im.width;
+        d.dtype = im.dtype;
+        d.cap = im.capacity;
+        d.nsc = (im.width + kInner - 1) / kInner;
+        d.nsr = (im.height + p->S - 1) / p->S;
+        d.unit_base = (int)units;
+        d.tile_base = (int)tiles;
+        d.seg_base = tiles * kSegTile;
+        const long long nseg = 2LL * im.height * d.nsc;
+        units += (long long)d.nsc * d.nsr;
+        tiles += (nseg + kSegTile - 1) / kSegTile;
+        staging += im.capacity;
+    }
+    if (units >= (1LL << 31) || tiles >= (1LL << 31)) return TOED_ERR_UNSUPPORTED;
+    p->n_units = (int)units;
+    p->n_tiles = (int)tiles;
+    toed_status st = ensure_scratch(c, std::max(staging, 1LL), tiles * kSegTile, tiles, n, stream);
+    if (st != TOED_OK) return st;
+    p->sc.words = c->words;
+    p->sc.staging = c->staging;
+    p->sc.staging_idx = c->staging_idx;
+    p->sc.staging_cap = c->staging_cap;
+    p->sc.seg = c->seg;
+    p->sc.tile_sum = c->tile_sum;
+    p->sc.img_base = c->img_base;
+
+    TOED_CU(cudaMemsetAsync(c->words, 0, (first_chunk ? 3 : 2) * sizeof(int), stream));
+    const int grid = (int)std::min<long long>(units, resident);
+    void* args[] = {p};
+    if (c->prof_start) TOED_CU(cudaEventRecord(c->prof_start, stream));
+    TOED_CU(cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream));
+    if (c->prof_stop) TOED_CU(cudaEventRecord(c->prof_stop, stream));
+    TOED_CU(launch_finalize(*p, stream));
+    return TOED_OK;
+}
+
+extern "C" toed_status toed_detect_batch(toed_ctx* c, const toed_image* images, int n,
+                                         const toed_params* prm, cudaStream_t stream)
+{
+    if (!c || !images || n <= 0 || !prm) return TOED_ERR_INVALID_ARG;
+    if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma) || !std::isfinite(prm->threshold)) return TOED_ERR_INVALID_ARG;
+    if (prm->border < 1) return TOED_ERR_INVALID_ARG;
+    if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
+    if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
+    const int r = radius_of(prm);
+    if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
+    for (int i = 0; i < n; ++i) {
+        toed_status st = check_image(images[i]);
+        if (st != TOED_OK) return st;
+    }
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    if (prev != c->device) TOED_CU(cudaSetDevice(c->device));
+    toed_status st = TOED_OK;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
+            st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream);
+    }
+    if (prev != c->device) cudaSetDevice(prev);
+    return st;
+}
+
+extern "C" toed_status toed_detect(toed_ctx* c, const toed_image* image, const toed_params* prm,
+                                   cudaStream_t stream)
+{
+    return toed_detect_batch(c, image, 1, prm, stream);
+}
+
+extern "C" toed_status toed_device_flags(toed_ctx* c, cudaStream_t stream, int* flags)
+{
+    if (!c || !flags) return TOED_ERR_INVALID_ARG;
+    int w[4] = {0, 0, 0, 0};
+    TOED_CU(cudaMemcpyAsync(w, c->words, sizeof(w), cudaMemcpyDeviceToHost, stream));
+    TOED_CU(cudaStreamSynchronize(stream));
+    *flags = w[2];
+    return TOED_OK;
+}
+
+extern "C" toed_status toed_profile_events(toed_ctx* c, cudaEvent_t start, cudaEvent_t stop)
+{
+    if (!c || ((start == nullptr) != (stop == nullptr))) return TOED_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->prof_start = start;
+    c->prof_stop = stop;
+    return TOED_OK;
+}

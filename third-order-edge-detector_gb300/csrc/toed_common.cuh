@@ -1,0 +1,87 @@
+// toed_common.cuh -- launch descriptors shared by the detection kernels and
+// the host side of the C ABI.
+//
+// Data layout in HBM (all caller-owned except the scratch block):
+//   image k      : H x pitch pixels (uint8 or float32), row-major
+//   edgels k     : capacity x 4 (float32 or float64) [x, y, orientation, strength]
+//   scratch      : work-queue / cursor / flags words, staging records
+//                  (double4 + int index per edgel), the row-segment table
+//                  (int2 {staging offset, count} per (2x-grid row, strip column)),
+//                  and the ordering pass' tile sums.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/toed_gb300.h"
+
+namespace toed {
+
+constexpr int kMaxTaps = 2 * TOED_MAX_RADIUS + 3;  // taps of the widest (shifted/full) filter
+constexpr int kBatchMax = 64;                      // images per launch (larger batches are chunked)
+constexpr int kThreads = 256;                      // threads per detection CTA
+constexpr int kExt = 32;                           // strip width incl. a 1-pixel ring each side
+constexpr int kInner = kExt - 2;                   // 30 output columns per strip
+constexpr int kStepRows = 16;                      // original rows per sliding step (B)
+constexpr int kColRows = 8;                        // rows per column-pass thread (register blocking)
+constexpr int kSegTile = 1024;                     // segments per ordering-pass tile
+
+// 1-D taps, index k <-> offset x = k - (r+1) (+0.5 for the shifted set).
+// Filters: 0 G, 1 Gx, 2 Gxx, 3 Gxxx, 4..7 the same shifted by +0.5.
+// Passed by value as a kernel parameter, so unrolled loops read each tap as
+// a constant-bank operand of the FMA.
+struct TapBlock {
+    float v[8][kMaxTaps];
+};
+
+struct DetImage {
+    const void* src;
+    long long pitch;     // elements
+    void* out;           // edgels
+    int* count;          // user count word
+    int* index;          // optional grid index output
+    long long seg_base;  // first segment of this image (tile aligned)
+    int H, W;
+    int dtype;
+    int cap;
+    int nsc, nsr;        // strip columns / strip rows
+    int unit_base;       // first work unit
+    int tile_base;       // first ordering tile
+};
+
+struct Scratch {
+    int* words;          // [0] unit queue, [1] staging cursor, [2] flags, [3] spare
+    double4_32a* staging;  // staged edgels (x, y, orientation, strength)
+    int* staging_idx;
+    long long staging_cap;
+    int2* seg;           // per segment {staging offset, count}
+    int* tile_sum;       // per ordering tile
+    long long* img_base; // per image: exclusive prefix of its first segment
+};
+
+struct BatchParams {
+    TapBlock taps;
+    float thr;
+    int border;
+    int S;               // strip inner rows (multiple of kStepRows minus 2)
+    int n_img;
+    int n_units;
+    int n_tiles;
+    int out_f64;
+    int radius;
+    Scratch sc;
+    DetImage img[kBatchMax];
+};
+
+// Index of the image whose [base, next base) range holds `u` (bases ascending).
+template <typename GetBase>
+__device__ __forceinline__ int find_image(int n_img, int u, GetBase base)
+{
+    int lo = 0, hi = n_img - 1;
+    while (lo < hi) {
+        int mid = (lo + hi + 1) >> 1;
+        if (base(mid) <= u) lo = mid; else hi = mid - 1;
+    }
+    return lo;
+}
+
+}  // namespace toed

@@ -1,0 +1,471 @@
+// toed_detect.cuh -- fused single-pass TOED detection kernel (sm_103a).
+//
+// One persistent CTA (256 threads) repeatedly takes a work unit from an
+// atomic queue.  A unit is a vertical strip of one image: 30 output columns
+// (32 with a one-pixel ring) by S output rows.  The CTA slides down the strip
+// in steps of B = 16 rows, keeping everything on chip:
+//
+//   1. load B new input rows (+ halo) into shared memory, converting to FP32;
+//   2. row pass: 12 horizontal 1-D filter responses per (row, column) --
+//      G/Gx/Gxx/Gxxx, each truncated to 2r+1 taps (T), full 2r+3 taps (F) and
+//      half-pixel shifted (S) -- into a sliding window of B+2r+3 rows;
+//   3. column pass: Ix and Iy at the four half-pixel sub-grids (the 2x grid
+//      of the reference, cpu_toed.cpp:204-355) for the B new rows, and
+//      |grad I| -- only the two first derivatives are evaluated densely;
+//   4. subpixel NMS along the gradient with the reference's 8-sector
+//      interpolation, max test and parabola fit (cpu_toed.cpp:399-495),
+//      decided in FP32; survivors are compacted with warp ballots in
+//      row-major order;
+//   5. per edgel only: the seven higher derivatives from the row-pass window,
+//      the third-order orientation (cpu_toed.cpp:227-232) and the peak fit
+//      in FP64 (HYBRID) or FP32; the record goes to a staging area and the
+//      row's {offset, count} to the row-segment table that the ordering pass
+//      (toed_finalize.cu) turns into the reference's row-major edgel list.
+//
+// Compared with the reference kernel (direct 17x17 and 19x19 sums of nine
+// derivatives at every point, gpu_convolve.cu:114-131) this evaluates the
+// separable form, keeps the nine-derivative stack off HBM entirely and
+// computes seven of the nine derivatives only where an edgel survives.
+#pragma once
+#include "toed_common.cuh"
+
+namespace toed {
+
+__host__ __device__ constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+template <int R>
+struct Cfg {
+    static constexpr int B = kStepRows;
+    static constexpr int NT = 2 * R + 3;            // taps of a full / shifted filter
+    static constexpr int NIN = kExt + 2 * R + 2;    // input columns held per row
+    static constexpr int HS = B + 2 * R + 3;        // row-pass window slots
+    static constexpr int MS = 2 * B + 2;            // 2x-grid rows held for NMS
+    static constexpr int NMS_ROWS = 2 * B;          // 2x-grid rows decided per step
+    static constexpr int MAXC = NMS_ROWS * 2 * kInner;
+    static constexpr size_t off_in = 0;
+    static constexpr size_t off_P = align_up(off_in + sizeof(float) * HS * NIN, 16);
+    static constexpr size_t off_mag = off_P + sizeof(float2) * 6 * HS * kExt;
+    static constexpr size_t off_fxy = off_mag + sizeof(float) * MS * 64;
+    static constexpr size_t off_tab = off_fxy + sizeof(float2) * MS * 64;
+    static constexpr size_t off_cand = off_tab + sizeof(float4) * 3 * NT;
+    static constexpr size_t off_misc = off_cand + sizeof(unsigned) * MAXC;
+    static constexpr size_t smem = off_misc + sizeof(int) * 96;
+};
+
+__device__ __forceinline__ float sqrt_approx(float x)
+{
+    float y;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+    return y;
+}
+
+// Image pixel as FP32 with zero padding outside the image (cpu_toed.cpp:207-208).
+__device__ __forceinline__ float fetch_px(const void* src, long long pitch, int H, int W, int dtype,
+                                          int y, int x)
+{
+    if ((unsigned)y >= (unsigned)H || (unsigned)x >= (unsigned)W) return 0.f;
+    const long long o = (long long)y * pitch + x;
+    if (dtype == TOED_U8) return (float)__ldg((const unsigned char*)src + o);
+    return __ldg((const float*)src + o);
+}
+
+// ---------------------------------------------------------------------------
+// Row pass: for input rows [in0, in0+nrows) of sIn write window slots
+// [slot0, slot0+nrows).  Item = (row, pair of ext columns 2k, 2k+1).
+// Planes: 0 PT=(T_G,T_Gx) 1 PF=(F_G,F_Gx) 2 PS=(S_G,S_Gx)
+//         3 QT=(T_Gxx,T_Gxxx) 4 QF 5 QS, each [HS][32] float2.
+// Convolution direction as the reference: out(x) = sum_q in(x-q) X(q).
+// ---------------------------------------------------------------------------
+template <int R>
+__device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int in0, int nrows, int slot0,
+                                         float2* __restrict__ sP, const TapBlock& tp)
+{
+    using C = Cfg<R>;
+    constexpr int NV = 2 * R + 4;
+    for (int item = threadIdx.x; item < nrows * 16; item += kThreads) {
+        const int i = item >> 4, k = item & 15;
+        const float2* src = reinterpret_cast<const float2*>(sIn + (in0 + i) * C::NIN + 2 * k);
+        float v[NV];
+#pragma unroll
+        for (int t = 0; t < NV / 2; ++t) {
+            const float2 q = src[t];
+            v[2 * t] = q.x;
+            v[2 * t + 1] = q.y;
+        }
+        float o_[2][12];
+#pragma unroll
+        for (int o = 0; o < 2; ++o) {
+            float tG = 0.f, tGx = 0.f, tGxx = 0.f, tGxxx = 0.f;
+#pragma unroll
+            for (int q = -R; q <= R; ++q) {
+                const float x = v[o + R + 1 - q];
+                tG = fmaf(x, tp.v[0][q + R + 1], tG);
+                tGx = fmaf(x, tp.v[1][q + R + 1], tGx);
+                tGxx = fmaf(x, tp.v[2][q + R + 1], tGxx);
+                tGxxx = fmaf(x, tp.v[3][q + R + 1], tGxxx);
+            }
+            // full 2r+3-tap responses add the two outermost taps q = +-(r+1)
+            const float xl = v[o], xr = v[o + 2 * R + 2];
+            const float fG = fmaf(xr, tp.v[0][0], fmaf(xl, tp.v[0][2 * R + 2], tG));
+            const float fGx = fmaf(xr, tp.v[1][0], fmaf(xl, tp.v[1][2 * R + 2], tGx));
+            const float fGxx = fmaf(xr, tp.v[2][0], fmaf(xl, tp.v[2][2 * R + 2], tGxx));
+            const float fGxxx = fmaf(xr, tp.v[3][0], fmaf(xl, tp.v[3][2 * R + 2], tGxxx));
+            float sG = 0.f, sGx = 0.f, sGxx = 0.f, sGxxx = 0.f;
+#pragma unroll
+            for (int q = -(R + 1); q <= R + 1; ++q) {
+                const float x = v[o + R + 1 - q];
+                sG = fmaf(x, tp.v[4][q + R + 1], sG);
+                sGx = fmaf(x, tp.v[5][q + R + 1], sGx);
+                sGxx = fmaf(x, tp.v[6][q + R + 1], sGxx);
+                sGxxx = fmaf(x, tp.v[7][q + R + 1], sGxxx);
+            }
+            o_[o][0] = tG;  o_[o][1] = tGx;  o_[o][2] = fG;  o_[o][3] = fGx;
+            o_[o][4] = sG;  o_[o][5] = sGx;  o_[o][6] = tGxx; o_[o][7] = tGxxx;
+            o_[o][8] = fGxx; o_[o][9] = fGxxx; o_[o][10] = sGxx; o_[o][11] = sGxxx;
+        }
+        const int slot = slot0 + i;
+#pragma unroll
+        for (int a = 0; a < 6; ++a) {
+            float4* dst = reinterpret_cast<float4*>(sP + (a * C::HS + slot) * kExt + 2 * k);
+            *dst = make_float4(o_[0][2 * a], o_[0][2 * a + 1], o_[1][2 * a], o_[1][2 * a + 1]);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Column pass for one (column, sub-grid, 8-row group): Ix and Iy.
+// V = 0: unshifted y taps truncated to 2r+1 (sub-grid (0,0), cpu_toed.cpp:205-221)
+// V = 1: unshifted y taps, full 2r+3 (sub-grid (0,1/2), :246-262)
+// V = 2: shifted y taps (sub-grids (1/2, .), :287-344)
+// ---------------------------------------------------------------------------
+template <int R, int V>
+__device__ __forceinline__ void col_pass(const float2* __restrict__ P, int g, int lane,
+                                         const TapBlock& tp, float (&fx)[kColRows],
+                                         float (&fy)[kColRows])
+{
+    constexpr int YF = (V == 2) ? 4 : 0;
+#pragma unroll
+    for (int o = 0; o < kColRows; ++o) { fx[o] = 0.f; fy[o] = 0.f; }
+#pragma unroll
+    for (int t = 0; t < kColRows + 2 * R + 2; ++t) {
+        const float2 h = P[(g * kColRows + 1 + t) * kExt + lane];
+#pragma unroll
+        for (int o = 0; o < kColRows; ++o) {
+            const int p = o + R + 1 - t;
+            const bool in = (V == 0) ? (p >= -R && p <= R) : (p >= -(R + 1) && p <= R + 1);
+            if (in) {
+                fx[o] = fmaf(h.y, tp.v[YF + 0][p + R + 1], fx[o]);
+                fy[o] = fmaf(h.x, tp.v[YF + 1][p + R + 1], fy[o]);
+            }
+        }
+    }
+}
+
+// NMS evaluation at 2x-grid slot (m, c) of the step window.  Shared by the
+// decision stage and the per-edgel epilogue so both see identical numbers.
+struct NmsEval {
+    float mv, gx, gy, nx, ny, slope, Map, Mdp, Mam, Mdm, sstar;
+    bool cand;
+};
+
+__device__ __forceinline__ NmsEval nms_eval(const float* __restrict__ sMag,
+                                            const float2* __restrict__ sFxy, int m, int c, float thr)
+{
+    NmsEval r;
+    r.cand = false;
+    r.mv = sMag[m * 64 + c];
+    if (!(r.mv > thr)) return r;  // cpu_toed.cpp:403 (also rejects NaN)
+    const float2 g = sFxy[m * 64 + c];
+    r.gx = g.x;
+    r.gy = g.y;
+    if (fabsf(g.x) < 10e-6f && fabsf(g.y) < 10e-6f) return r;  // :407
+    r.nx = __fdividef(g.x, r.mv);
+    r.ny = __fdividef(g.y, r.mv);
+    // Eight sectors of cpu_toed.cpp:415-462 in closed form: x-major when
+    // |Ix| >= |Iy|; the axis neighbour steps along the major axis towards
+    // the gradient, the diagonal one along both; fm mirrors fp.
+    const bool xmaj = fabsf(g.x) >= fabsf(g.y);
+    const int sx = (g.x >= 0.f) ? 1 : -1, sy = (g.y >= 0.f) ? 1 : -1;
+    r.slope = xmaj ? __fdividef(fabsf(r.ny), fabsf(r.nx)) : __fdividef(fabsf(r.nx), fabsf(r.ny));
+    const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+    r.Map = sMag[(m + ar) * 64 + c + ac];
+    r.Mdp = sMag[(m + sy) * 64 + c + sx];
+    r.Mam = sMag[(m - ar) * 64 + c - ac];
+    r.Mdm = sMag[(m - sy) * 64 + c - sx];
+    const float fp = r.Map * (1.f - r.slope) + r.Mdp * r.slope;
+    const float fm = r.Mam * (1.f - r.slope) + r.Mdm * r.slope;
+    const float mv = r.mv;
+    const bool maxt = (mv > fm && mv >= fp) || (mv >= fm && mv > fp);  // :466-468
+    // s* = -B/(2A) with A = (fm+fp-2f)/(2s^2), B = (fp-fm)/(2s) (:471-476)
+    const float s = sqrtf(1.f + r.slope * r.slope);
+    r.sstar = __fdividef(-(fp - fm) * s, 2.f * (fm + fp - 2.f * mv));
+    r.cand = maxt && (fabsf(r.sstar) <= 1.41421356f);  // :478
+    return r;
+}
+
+template <int R, bool HYB>
+__global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_constant__ BatchParams p)
+{
+    using C = Cfg<R>;
+    constexpr int B = C::B;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* sIn = reinterpret_cast<float*>(smem + C::off_in);
+    float2* sP = reinterpret_cast<float2*>(smem + C::off_P);
+    float* sMag = reinterpret_cast<float*>(smem + C::off_mag);
+    float2* sFxy = reinterpret_cast<float2*>(smem + C::off_fxy);
+    float4* sTab = reinterpret_cast<float4*>(smem + C::off_tab);
+    unsigned* sCand = reinterpret_cast<unsigned*>(smem + C::off_cand);
+    int* sMisc = reinterpret_cast<int*>(smem + C::off_misc);
+    int* sRowCnt = sMisc;        // [32]
+    int* sRowOff = sMisc + 32;   // [32]
+    int* sScal = sMisc + 64;     // [0] unit, [1] staging base, [2] total K
+
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+    const TapBlock& tp = p.taps;
+
+    // y-direction tap table for the per-edgel stage: [variant][k] = (G, Gy, Gyy, Gyyy)
+    for (int i = tid; i < 3 * C::NT; i += kThreads) {
+        const int v = i / C::NT, k = i % C::NT;
+        const int f = (v == 2) ? 4 : 0;
+        float4 t = make_float4(tp.v[f][k], tp.v[f + 1][k], tp.v[f + 2][k], tp.v[f + 3][k]);
+        if (v == 0 && (k == 0 || k == C::NT - 1)) t = make_float4(0.f, 0.f, 0.f, 0.f);
+        sTab[i] = t;
+    }
+
+    for (;;) {
+        __syncthreads();
+        if (tid == 0) sScal[0] = atomicAdd(&p.sc.words[0], 1);
+        __syncthreads();
+        const int u = sScal[0];
+        if (u >= p.n_units) break;
+        const int k = find_image(p.n_img, u, [&](int i) { return p.img[i].unit_base; });
+        const DetImage& im = p.img[k];
+        const void* src = im.src;
+        const long long pitch = im.pitch;
+        const int H = im.H, W = im.W, dtype = im.dtype;
+        const int local = u - im.unit_base;
+        const int sr = local / im.nsc, sc = local - sr * im.nsc;
+        const int ys = sr * p.S, x0 = sc * kInner;
+        const int S_act = min(p.S, H - ys);
+        const int nsteps = (2 * S_act + 3 + 2 * B - 1) / (2 * B);
+        const int W2 = 2 * W;
+        const int row_lo = max(p.border, 2 * ys), row_hi = min(2 * H - p.border, 2 * ys + 2 * S_act);
+        const int col_lo = p.border, col_hi = W2 - p.border;
+        const long long seg0 = im.seg_base;
+
+        for (int i = tid; i < 2 * 64; i += kThreads) {
+            sMag[i] = 0.f;
+            sFxy[i] = make_float2(0.f, 0.f);
+        }
+
+        for (int s = 0; s < nsteps; ++s) {
+            // ---- 1. input rows -> sIn (FP32, zero padded) -------------------
+            {
+                const int nrows = (s == 0) ? C::HS : B;
+                // slot h <-> ext row e = s*B - R - 2 + h <-> image row ys - 1 + e
+                const int img_row0 = ys - 1 + s * B - R - 2 + ((s == 0) ? 0 : 2 * R + 3);
+                const int col0 = x0 - R - 2;
+                for (int i = tid; i < nrows * C::NIN; i += kThreads) {
+                    const int rr = i / C::NIN, cc = i - rr * C::NIN;
+                    sIn[i] = fetch_px(src, pitch, H, W, dtype, img_row0 + rr, col0 + cc);
+                }
+            }
+            __syncthreads();
+            // ---- 2. row pass ------------------------------------------------
+            if (s == 0)
+                row_pass<R>(sIn, 0, C::HS, 0, sP, tp);
+            else
+                row_pass<R>(sIn, 0, B, 2 * R + 3, sP, tp);
+            __syncthreads();
+            // ---- 3. column pass: Ix, Iy, |grad I| for ext rows s*B .. s*B+B-1
+            {
+                const int sg = wid & 3, g = wid >> 2;
+                const int a = sg >> 1, b = sg & 1;
+                float fx[kColRows], fy[kColRows];
+                if (sg == 0)
+                    col_pass<R, 0>(sP + 0 * C::HS * kExt, g, lane, tp, fx, fy);
+                else if (sg == 2)
+                    col_pass<R, 2>(sP + 1 * C::HS * kExt, g, lane, tp, fx, fy);
+                else if (sg == 1)
+                    col_pass<R, 1>(sP + 2 * C::HS * kExt, g, lane, tp, fx, fy);
+                else
+                    col_pass<R, 2>(sP + 2 * C::HS * kExt, g, lane, tp, fx, fy);
+#pragma unroll
+                for (int o = 0; o < kColRows; ++o) {
+                    const int m = 2 * (g * kColRows + o) + a + 2;
+                    const int c = 2 * lane + b;
+                    sMag[m * 64 + c] = sqrt_approx(fmaf(fx[o], fx[o], fy[o] * fy[o]));
+                    sFxy[m * 64 + c] = make_float2(fx[o], fy[o]);
+                }
+            }
+            __syncthreads();
+            // ---- 4. NMS decisions on 2x-grid rows m = 1..2B (rho = 2sB-2+m) ---
+            // global 2x-grid row of slot m: Gr = 2*ys - 2 + (2sB - 2 + m)
+            const int gr_base = 2 * ys - 4 + 2 * s * B;
+            const int gc_base = 2 * (x0 - 1);
+            unsigned bal0[4], bal1[4];
+#pragma unroll
+            for (int t = 0; t < 4; ++t) {
+                const int m = 1 + wid + 8 * t;
+                const int Gr = gr_base + m;
+                const int c0 = 2 + 2 * lane;
+                const bool rowok = (Gr >= row_lo) && (Gr < row_hi) && (lane < kInner);
+                bool k0 = false, k1 = false;
+                if (rowok) {
+                    const int Gc = gc_base + c0;
+                    if (Gc >= col_lo && Gc < col_hi) k0 = nms_eval(sMag, sFxy, m, c0, p.thr).cand;
+                    if (Gc + 1 >= col_lo && Gc + 1 < col_hi) k1 = nms_eval(sMag, sFxy, m, c0 + 1, p.thr).cand;
+                }
+                bal0[t] = __ballot_sync(0xffffffffu, k0);
+                bal1[t] = __ballot_sync(0xffffffffu, k1);
+                if (lane == 0) sRowCnt[m - 1] = __popc(bal0[t]) + __popc(bal1[t]);
+            }
+            __syncthreads();
+            if (wid == 0) {
+                const int cnt = sRowCnt[lane];
+                int incl = cnt;
+#pragma unroll
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, d);
+                    if (lane >= d) incl += y;
+                }
+                sRowOff[lane] = incl - cnt;
+                const int total = __shfl_sync(0xffffffffu, incl, 31);
+                int base = 0;
+                if (lane == 0 && total > 0) base = atomicAdd(&p.sc.words[1], total);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (lane == 0) {
+                    sScal[1] = base;
+                    sScal[2] = total;
+                    if ((long long)base + total > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
+                }
+                const int Gr = gr_base + lane + 1;
+                if (Gr >= 2 * ys && Gr < 2 * ys + 2 * S_act)
+                    p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
+            }
+            __syncthreads();
+            {
+                const unsigned lt = (1u << lane) - 1u;
+#pragma unroll
+                for (int t = 0; t < 4; ++t) {
+                    const int m = 1 + wid + 8 * t;
+                    const bool k0 = (bal0[t] >> lane) & 1u, k1 = (bal1[t] >> lane) & 1u;
+                    const int pos = sRowOff[m - 1] + __popc(bal0[t] & lt) + __popc(bal1[t] & lt);
+                    const unsigned c0 = 2 + 2 * lane;
+                    if (k0) sCand[pos] = ((unsigned)m << 8) | c0;
+                    if (k1) sCand[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
+                }
+            }
+            __syncthreads();
+            // ---- 5. per-edgel derivatives, TO orientation, fit, staging ----
+            {
+                const int total = sScal[2], base = sScal[1];
+                for (int j = tid; j < total; j += kThreads) {
+                    const unsigned rec = sCand[j];
+                    const int m = rec >> 8, c = rec & 255;
+                    const int a = m & 1, xe = c >> 1, b = c & 1;
+                    const int xv = b ? 2 : (a ? 1 : 0);
+                    const int yv = a ? 2 : (b ? 1 : 0);
+                    const float2* Pp = sP + xv * C::HS * kExt + xe;
+                    const float2* Qp = sP + (3 + xv) * C::HS * kExt + xe;
+                    const float4* tab = sTab + yv * C::NT;
+                    float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
+                    const int h0 = m >> 1;
+#pragma unroll
+                    for (int kk = 0; kk < C::NT; ++kk) {
+                        const float2 hp = Pp[(h0 + kk) * kExt];
+                        const float2 hq = Qp[(h0 + kk) * kExt];
+                        const float4 t = tab[C::NT - 1 - kk];
+                        fxy = fmaf(hp.y, t.y, fxy);
+                        fyy = fmaf(hp.x, t.z, fyy);
+                        fxyy = fmaf(hp.y, t.z, fxyy);
+                        fyyy = fmaf(hp.x, t.w, fyyy);
+                        fxx = fmaf(hq.x, t.x, fxx);
+                        fxxy = fmaf(hq.x, t.y, fxxy);
+                        fxxx = fmaf(hq.y, t.x, fxxx);
+                    }
+                    const NmsEval e = nms_eval(sMag, sFxy, m, c, p.thr);
+                    const int Gr = gr_base + m, Gc = gc_base + c;
+                    double x, y;
+                    float ori, str;
+                    if (HYB) {
+                        // peak fit in FP64 (cancellation in fm+fp-2f and fp-fm)
+                        const double s1 = e.slope;
+                        const double fp = (double)e.Map * (1.0 - s1) + (double)e.Mdp * s1;
+                        const double fm = (double)e.Mam * (1.0 - s1) + (double)e.Mdm * s1;
+                        const double num = fp - fm, den = fm + fp - 2.0 * (double)e.mv;
+                        const double ss = (double)sqrtf(1.f + e.slope * e.slope);
+                        const double rden = 1.0 / den;
+                        const double sst = -0.5 * num * ss * rden;
+                        const double maxf = (double)e.mv - 0.125 * num * num * rden;
+                        x = ((double)Gc + sst * (double)e.nx - 1.0) * 0.5;
+                        y = ((double)Gr + sst * (double)e.ny - 1.0) * 0.5;
+                        const float mf = (float)maxf;
+                        str = sqrtf((mf * e.nx) * (mf * e.nx) + (mf * e.ny) * (mf * e.ny));
+                        // third-order orientation in FP64 (cpu_toed.cpp:227-232)
+                        const double dfx = e.gx, dfy = e.gy, dxx = fxx, dxy = fxy, dyy = fyy;
+                        const double tix = dfx * (2.0 * dxx * dxx + 2.0 * dxy * dxy) +
+                                           dfy * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
+                                           2.0 * dfx * dfy * (double)fxxy + dfy * dfy * (double)fxyy +
+                                           dfx * dfx * (double)fxxx;
+                        const double tiy = dfx * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
+                                           dfy * (2.0 * dyy * dyy + 2.0 * dxy * dxy) +
+                                           2.0 * dfx * dfy * (double)fxyy + dfx * dfx * (double)fxxy +
+                                           dfy * dfy * (double)fyyy;
+                        ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000)
+                                                         : atan2f((float)tix, (float)(-tiy));
+                    } else {
+                        const float sl = e.slope;
+                        const float fp = e.Map * (1.f - sl) + e.Mdp * sl;
+                        const float fm = e.Mam * (1.f - sl) + e.Mdm * sl;
+                        const float num = fp - fm, den = fm + fp - 2.f * e.mv;
+                        const float ss = sqrtf(1.f + sl * sl);
+                        const float sst = -0.5f * num * ss / den;
+                        const float maxf = e.mv - 0.125f * num * num / den;
+                        x = ((double)((float)Gc + sst * e.nx) - 1.0) * 0.5;
+                        y = ((double)((float)Gr + sst * e.ny) - 1.0) * 0.5;
+                        str = sqrtf((maxf * e.nx) * (maxf * e.nx) + (maxf * e.ny) * (maxf * e.ny));
+                        const float tix = e.gx * (2.f * fxx * fxx + 2.f * fxy * fxy) +
+                                          e.gy * (2.f * fxx * fxy + 2.f * fyy * fxy) +
+                                          2.f * e.gx * e.gy * fxxy + e.gy * e.gy * fxyy + e.gx * e.gx * fxxx;
+                        const float tiy = e.gx * (2.f * fxx * fxy + 2.f * fyy * fxy) +
+                                          e.gy * (2.f * fyy * fyy + 2.f * fxy * fxy) +
+                                          2.f * e.gx * e.gy * fxyy + e.gx * e.gx * fxxy + e.gy * e.gy * fyyy;
+                        ori = (tix == 0.f && tiy == 0.f) ? __int_as_float(0x7fc00000) : atan2f(tix, -tiy);
+                    }
+                    const long long dst = (long long)base + j;
+                    if (dst < p.sc.staging_cap) {
+                        p.sc.staging[dst] = make_double4_32a(x, y, (double)ori, (double)str);
+                        p.sc.staging_idx[dst] = Gr * W2 + Gc;
+                    }
+                }
+            }
+            __syncthreads();
+            // ---- 6. slide the windows -------------------------------------
+            if (s + 1 < nsteps) {
+                // row-pass window: slots [B, HS) -> [0, 2R+3), in phases of B rows so
+                // that no source slot is overwritten before it is read
+                for (int ph = 0; ph < 2 * R + 3; ph += B) {
+                    const int nr = min(B, 2 * R + 3 - ph);
+                    const int n4 = 6 * nr * (kExt / 2);
+                    for (int i = tid; i < n4; i += kThreads) {
+                        const int a = i / (nr * 16), rem = i - a * nr * 16;
+                        const int rr = rem >> 4, cc = (rem & 15) * 2;
+                        const float4 v = *reinterpret_cast<const float4*>(sP + (a * C::HS + B + ph + rr) * kExt + cc);
+                        *reinterpret_cast<float4*>(sP + (a * C::HS + ph + rr) * kExt + cc) = v;
+                    }
+                    __syncthreads();
+                }
+                for (int i = tid; i < 2 * 64; i += kThreads) {
+                    sMag[i] = sMag[2 * B * 64 + i];
+                    sFxy[i] = sFxy[2 * B * 64 + i];
+                }
+            }
+        }
+    }
+}
+
+template <int R, bool HYB>
+void launch_detect(const BatchParams& p, int grid, cudaStream_t stream);
+
+}  // namespace toed

@@ -1,0 +1,3 @@
+// Detection kernels for half-width r = 7.
+#include "toed_detect_inst.cuh"
+TOED_DETECT_INSTANCE(7)

@@ -1,0 +1,127 @@
+// toed_finalize.cu -- ordering pass: turns the detection kernel's staged
+// edgels and row-segment table into each image's edgel list in the
+// reference's order (row-major over the 2x grid, cpu_toed.cpp:510-538).
+//
+// Segments are (2x-grid row, strip column) pairs laid out row-major per image
+// and padded to whole tiles of kSegTile.  Three short kernels:
+//   fin_tile_sums : edgels per tile
+//   fin_tile_scan : exclusive scan over tiles; per-image base and count,
+//                   capacity flag
+//   fin_scatter   : per segment, destination = global prefix - image base;
+//                   copy the staged records, converting to the output dtype.
+#include "toed_common.cuh"
+#include "toed_internal.h"
+
+namespace toed {
+
+template <int NT>
+__device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        constexpr int NW = NT / 32;
+        int w = (lane < NW) ? s_warp[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, d);
+            if (lane >= d) wi += y;
+        }
+        if (lane < NW) s_warp[lane] = wi - w;
+        if (lane == NW - 1) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const int r = incl - v + s_warp[wid];
+    *total = s_warp[32];
+    __syncthreads();
+    return r;
+}
+
+__global__ void __launch_bounds__(256) fin_tile_sums(const __grid_constant__ BatchParams p)
+{
+    __shared__ int s_warp[33];
+    const int t = blockIdx.x;
+    const int k = find_image(p.n_img, t, [&](int i) { return p.img[i].tile_base; });
+    const DetImage& im = p.img[k];
+    const long long nseg = 2LL * im.H * im.nsc;
+    const long long first = (long long)(t - im.tile_base) * kSegTile;
+    int sum = 0;
+    for (int i = threadIdx.x; i < kSegTile; i += blockDim.x) {
+        const long long q = first + i;
+        if (q < nseg) sum += p.sc.seg[im.seg_base + q].y;
+    }
+    int total;
+    block_excl_scan<256>(sum, s_warp, &total);
+    if (threadIdx.x == 0) p.sc.tile_sum[t] = total;
+}
+
+__global__ void __launch_bounds__(1024) fin_tile_scan(const __grid_constant__ BatchParams p)
+{
+    __shared__ int s_warp[33];
+    int carry = 0;
+    for (int base = 0; base < p.n_tiles; base += 1024) {
+        const int i = base + threadIdx.x;
+        const int v = (i < p.n_tiles) ? p.sc.tile_sum[i] : 0;
+        int total;
+        const int ex = block_excl_scan<1024>(v, s_warp, &total);
+        if (i < p.n_tiles) p.sc.tile_sum[i] = carry + ex;
+        carry += total;
+    }
+    __syncthreads();
+    for (int k = threadIdx.x; k < p.n_img; k += blockDim.x) {
+        const long long b0 = p.sc.tile_sum[p.img[k].tile_base];
+        const long long b1 = (k + 1 < p.n_img) ? p.sc.tile_sum[p.img[k + 1].tile_base] : carry;
+        const int cnt = (int)(b1 - b0);
+        p.sc.img_base[k] = b0;
+        *p.img[k].count = cnt;
+        if (cnt > p.img[k].cap) atomicOr(&p.sc.words[2], TOED_FLAG_OVER_CAPACITY);
+    }
+}
+
+__global__ void __launch_bounds__(kSegTile) fin_scatter(const __grid_constant__ BatchParams p)
+{
+    __shared__ int s_warp[33];
+    const int t = blockIdx.x;
+    const int k = find_image(p.n_img, t, [&](int i) { return p.img[i].tile_base; });
+    const DetImage& im = p.img[k];
+    const long long nseg = 2LL * im.H * im.nsc;
+    const long long q = (long long)(t - im.tile_base) * kSegTile + threadIdx.x;
+    const int2 sg = (q < nseg) ? p.sc.seg[im.seg_base + q] : make_int2(0, 0);
+    int total;
+    const int ex = block_excl_scan<kSegTile>(sg.y, s_warp, &total);
+    const long long dest = (long long)p.sc.tile_sum[t] + ex - p.sc.img_base[k];
+    const long long cap = im.cap;
+    for (int j = 0; j < sg.y; ++j) {
+        const long long d = dest + j, src = (long long)sg.x + j;
+        if (d >= cap || src >= p.sc.staging_cap) break;
+        const double4_32a r = p.sc.staging[src];
+        if (p.out_f64) {  // two 16-byte stores: the caller's buffer need only be 16-byte aligned
+            double2* o = reinterpret_cast<double2*>(im.out) + 2 * d;
+            o[0] = make_double2(r.x, r.y);
+            o[1] = make_double2(r.z, r.w);
+        } else
+            reinterpret_cast<float4*>(im.out)[d] =
+                make_float4((float)r.x, (float)r.y, (float)r.z, (float)r.w);
+        if (im.index) im.index[d] = p.sc.staging_idx[src];
+    }
+}
+
+cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream)
+{
+    void* args[] = {const_cast<BatchParams*>(&p)};
+    cudaError_t e = cudaLaunchKernel((const void*)fin_tile_sums, dim3(p.n_tiles), dim3(256), args, 0, stream);
+    if (e != cudaSuccess) return e;
+    e = cudaLaunchKernel((const void*)fin_tile_scan, dim3(1), dim3(1024), args, 0, stream);
+    if (e != cudaSuccess) return e;
+    return cudaLaunchKernel((const void*)fin_scatter, dim3(p.n_tiles), dim3(kSegTile), args, 0, stream);
+}
+
+}  // namespace toed

@@ -188,16 +188,15 @@ def ridge_map(H: int = 2048, W: int = 2048, seed: int = 5000, n_curves: int = 40
         L = sum(np.linalg.norm(pts[i + 1] - pts[i]) for i in range(3))
         ns = max(8, int(L * 2))
         c = _bezier(pts[0], pts[1], pts[2], pts[3], np.linspace(0, 1, ns))
-        # distance-to-curve ridge: max over samples of a Gaussian bump
-        for cx, cy in c:
-            x0, x1 = max(0, int(cx) - rad), min(W, int(cx) + rad + 2)
-            y0, y1 = max(0, int(cy) - rad), min(H, int(cy) + rad + 2)
-            if x0 >= x1 or y0 >= y1:
-                continue
-            ys, xs = np.mgrid[y0:y1, x0:x1]
-            d2 = (xs - cx) ** 2 + (ys - cy) ** 2
-            np.maximum(E[y0:y1, x0:x1], peak * np.exp(-d2 / (2 * width * width)),
-                       out=E[y0:y1, x0:x1])
+        # ridge = max over curve samples of a Gaussian bump, splatted on the
+        # (2 rad + 2)^2 pixel window around each sample
+        offs = np.arange(-rad, rad + 2)
+        ox, oy = np.meshgrid(offs, offs)
+        xs = np.floor(c[:, 0])[:, None].astype(np.int64) + ox.ravel()[None, :]
+        ys = np.floor(c[:, 1])[:, None].astype(np.int64) + oy.ravel()[None, :]
+        d2 = (xs - c[:, 0:1]) ** 2 + (ys - c[:, 1:2]) ** 2
+        ok = (xs >= 0) & (xs < W) & (ys >= 0) & (ys < H)
+        np.maximum.at(E, (ys[ok], xs[ok]), peak * np.exp(-d2[ok] / (2 * width * width)))
     E += rng.uniform(noise[0], noise[1], size=E.shape)
     return np.clip(E, 0.0, 1.0).astype(dtype)
 
@@ -212,12 +211,15 @@ def ellipse_distance(px, py, e: Ellipse) -> np.ndarray:
     u = np.abs(dx * c + dy * s)
     v = np.abs(-dx * s + dy * c)
     a, b = e.a, e.b
-    t = np.arctan2(a * v, b * u)
-    for _ in range(12):
-        ct, st = np.cos(t), np.sin(t)
-        ex, ey = a * ct, b * st
-        f = (a * a - b * b) * st * ct - u * a * st + v * b * ct
-        fp = (a * a - b * b) * (ct * ct - st * st) - u * a * ct - v * b * st
-        t = np.clip(t - f / np.where(np.abs(fp) < 1e-30, 1e-30, fp), 0.0, math.pi / 2)
-    ex, ey = a * np.cos(t), b * np.sin(t)
-    return np.hypot(u - ex, v - ey)
+    best = None
+    # Newton from three starts (radial, both axes); keep the closest boundary point
+    for t0 in (np.arctan2(a * v, b * u), np.zeros_like(u), np.full_like(u, math.pi / 2)):
+        t = t0.copy()
+        for _ in range(16):
+            ct, st = np.cos(t), np.sin(t)
+            f = (a * a - b * b) * st * ct - u * a * st + v * b * ct
+            fp = (a * a - b * b) * (ct * ct - st * st) - u * a * ct - v * b * st
+            t = np.clip(t - f / np.where(np.abs(fp) < 1e-30, 1e-30, fp), 0.0, math.pi / 2)
+        d = np.hypot(u - a * np.cos(t), v - b * np.sin(t))
+        best = d if best is None else np.minimum(best, d)
+    return best
