@@ -119,14 +119,15 @@ toed_status toed_detect_batch(toed_ctx* ctx, const toed_image* images, int n_ima
 toed_status toed_device_flags(toed_ctx* ctx, cudaStream_t stream, int* flags);
 
 /* Measurement hooks (used by bench.py).
- * toed_profile_events: when both events are non-null, every following
- * detection on `ctx` records `start` just before and `stop` just after its
- * fused detection kernel (on the call's stream), so the kernel's own device
- * time can be read with cudaEventElapsedTime; pass NULLs to stop.
+ * toed_profile_begin: from now on every detection on `ctx` records a pair of
+ * CUDA events just before and just after its fused detection kernel, on the
+ * call's stream.  toed_profile_end: waits for the last pair, returns the sum
+ * of the kernel times (ms) and the number of kernel launches, and stops.
  * toed_peak_probe: times a register-resident FMA loop on all SMs and returns
  * the sustained FP32 (kind 0) or FP64 (kind 1) rate in TFLOP/s -- the
  * denominator of the FP32 roofline, measured at the clocks of the run. */
-toed_status toed_profile_events(toed_ctx* ctx, cudaEvent_t start, cudaEvent_t stop);
+toed_status toed_profile_begin(toed_ctx* ctx);
+toed_status toed_profile_end(toed_ctx* ctx, double* kernel_ms, int* launches);
 toed_status toed_peak_probe(int kind, int iters, cudaStream_t stream, double* tflops);
 
 /* Compatibility: the reference's dense two-kernel form.

@@ -77,10 +77,10 @@ def compare_edgels(ref_edges, ref_index, got_edges, got_index):
     ref_index = np.asarray(ref_index, np.int64)
     got_index = np.asarray(got_index, np.int64)
     common, ia, ib = np.intersect1d(ref_index, got_index, return_indices=True)
-    denom = max(len(ref_index), len(got_index), 1)
+    denom = max(len(ref_index), len(got_index))
     out = {
         "n_ref": len(ref_index), "n_got": len(got_index), "n_common": len(common),
-        "agreement": len(common) / denom if denom else 1.0,
+        "agreement": len(common) / denom if denom else 1.0,  # two empty sets agree
         "pos_max": 0.0, "pos_p99": 0.0, "ori_max": 0.0, "ori_p99": 0.0, "str_rel_max": 0.0,
     }
     if len(common):

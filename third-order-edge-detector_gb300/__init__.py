@@ -37,7 +37,7 @@ MAX_RADIUS = 12
 C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
-    "toed_convolve_planes", "toed_nms_planes", "toed_profile_events", "toed_peak_probe",
+    "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
 ]
 
 
@@ -100,7 +100,8 @@ def lib():
         L.toed_convolve_planes.argtypes = [vp, ip, ip, ip, ip, ctypes.c_float, ip, ip, vp, vp, vp, vp,
                                            vp]
         L.toed_nms_planes.argtypes = [ip, ip, ip, vp, vp, vp, ctypes.c_float, ip, vp, vp, vp]
-        L.toed_profile_events.argtypes = [vp, vp, vp]
+        L.toed_profile_begin.argtypes = [vp]
+        L.toed_profile_end.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ip)]
         L.toed_peak_probe.argtypes = [ip, ip, vp, ctypes.POINTER(ctypes.c_double)]
         for name in C_SYMBOLS:
             if name not in ("toed_status_string", "toed_last_cuda_error", "toed_params_default"):
@@ -181,12 +182,15 @@ class Detector:
         _check(lib().toed_reserve(self._ctx, int(max_pixels), int(max_edgels), int(max_images)),
                "toed_reserve")
 
-    def profile_events(self, start=None, stop=None):
-        """Record ``start``/``stop`` (torch.cuda.Event) around the fused
-        detection kernel of every following call; ``None`` disables."""
-        a = ctypes.c_void_p(start.cuda_event) if start is not None else None
-        b = ctypes.c_void_p(stop.cuda_event) if stop is not None else None
-        _check(lib().toed_profile_events(self._ctx, a, b), "toed_profile_events")
+    def profile_begin(self):
+        """Time the fused detection kernel of every following call."""
+        _check(lib().toed_profile_begin(self._ctx), "toed_profile_begin")
+
+    def profile_end(self):
+        """(total kernel ms, launches) since profile_begin()."""
+        ms, n = ctypes.c_double(0.0), ctypes.c_int(0)
+        _check(lib().toed_profile_end(self._ctx, ctypes.byref(ms), ctypes.byref(n)), "toed_profile_end")
+        return ms.value, n.value
 
     def flags(self, stream=None) -> int:
         f = ctypes.c_int(0)

@@ -95,7 +95,8 @@ struct toed_ctx {
     long long* img_base = nullptr;
     int img_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
-    cudaEvent_t prof_start = nullptr, prof_stop = nullptr;
+    bool profiling = false;
+    std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
     std::mutex mu;
 };
 
@@ -316,9 +317,15 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     TOED_CU(cudaMemsetAsync(c->words, 0, (first_chunk ? 3 : 2) * sizeof(int), stream));
     const int grid = (int)std::min<long long>(units, resident);
     void* args[] = {p};
-    if (c->prof_start) TOED_CU(cudaEventRecord(c->prof_start, stream));
+    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+    if (c->profiling) {
+        TOED_CU(cudaEventCreate(&ev0));
+        TOED_CU(cudaEventCreate(&ev1));
+        c->prof.emplace_back(ev0, ev1);
+        TOED_CU(cudaEventRecord(ev0, stream));
+    }
     TOED_CU(cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream));
-    if (c->prof_stop) TOED_CU(cudaEventRecord(c->prof_stop, stream));
+    if (ev1) TOED_CU(cudaEventRecord(ev1, stream));
     TOED_CU(launch_finalize(*p, stream));
     return TOED_OK;
 }
@@ -366,11 +373,35 @@ extern "C" toed_status toed_device_flags(toed_ctx* c, cudaStream_t stream, int* 
     return TOED_OK;
 }
 
-extern "C" toed_status toed_profile_events(toed_ctx* c, cudaEvent_t start, cudaEvent_t stop)
+extern "C" toed_status toed_profile_begin(toed_ctx* c)
 {
-    if (!c || ((start == nullptr) != (stop == nullptr))) return TOED_ERR_INVALID_ARG;
+    if (!c) return TOED_ERR_INVALID_ARG;
     std::lock_guard<std::mutex> lk(c->mu);
-    c->prof_start = start;
-    c->prof_stop = stop;
+    c->profiling = true;
+    return TOED_OK;
+}
+
+extern "C" toed_status toed_profile_end(toed_ctx* c, double* kernel_ms, int* launches)
+{
+    if (!c || !kernel_ms || !launches) return TOED_ERR_INVALID_ARG;
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->profiling = false;
+    double tot = 0.0;
+    cudaError_t err = cudaSuccess;
+    for (auto& pr : c->prof) {
+        float ms = 0.f;
+        if (err == cudaSuccess) err = cudaEventSynchronize(pr.second);
+        if (err == cudaSuccess) err = cudaEventElapsedTime(&ms, pr.first, pr.second);
+        tot += ms;
+        cudaEventDestroy(pr.first);
+        cudaEventDestroy(pr.second);
+    }
+    *launches = (int)c->prof.size();
+    c->prof.clear();
+    *kernel_ms = tot;
+    if (err != cudaSuccess) {
+        g_last_cuda_error = cudaGetErrorString(err);
+        return TOED_ERR_CUDA;
+    }
     return TOED_OK;
 }
