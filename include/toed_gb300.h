@@ -118,6 +118,35 @@ toed_status toed_detect_batch(toed_ctx* ctx, const toed_image* images, int n_ima
  * detection on this context (0 = all images fit their capacities). */
 toed_status toed_device_flags(toed_ctx* ctx, cudaStream_t stream, int* flags);
 
+/* Subpixel third-order correction of dense edge maps (the reference's
+ * SubpixelTOCorrectionCPU<T>, subpix_TO_correction/subpix_to_correction.cpp,
+ * at interp_n = 0).  All pointers are device pointers. */
+typedef struct toed_edgemap {
+    const void* E;      /* height x pitch edge map (probabilities), TOED_F32 or TOED_F64 */
+    const void* theta;  /* optional orientation map in radians (same dtype/pitch); NULL ->
+                           estimated from E (estimate_orientation, :307-375) */
+    int height;         /* >= 2 */
+    int width;          /* >= 2 */
+    int pitch;          /* elements between row starts */
+    int dtype;
+    void* edgels;       /* capacity x 4 of out_dtype: x, y, orientation, strength (0-based px) */
+    int capacity;
+    int* count;         /* edgels after removing isolated ones (exact even past capacity) */
+    void* TO_E;         /* optional dense height x width (out_dtype): strength at round(x, y) */
+    void* TO_O;         /* optional dense height x width (out_dtype): orientation at round(x, y) */
+} toed_edgemap;
+
+typedef struct toed_subpix_params {
+    float thresh;      /* NMS threshold on E (reference default 0.2; main_subpix_to_correction.cpp:147) */
+    float sigma;       /* Gaussian scale; radius ceil(4 sigma) <= TOED_MAX_RADIUS */
+    float nbr_radius;  /* drop edgels with no other edgel within this distance; <= 0 keeps all (default 2) */
+    int out_dtype;     /* TOED_F32 or TOED_F64 */
+    int precision;     /* TOED_HYBRID: FP64 peak fit and orientation correction per edgel */
+} toed_subpix_params;
+
+toed_status toed_subpix_to_correct_batch(toed_ctx* ctx, const toed_edgemap* maps, int n_maps,
+                                         const toed_subpix_params* params, cudaStream_t stream);
+
 /* Measurement hooks (used by bench.py).
  * toed_profile_begin: from now on every detection on `ctx` records a pair of
  * CUDA events just before and just after its fused detection kernel, on the
@@ -134,10 +163,14 @@ toed_status toed_peak_probe(int kind, int iters, cudaStream_t stream, double* tf
  * toed_convolve_planes writes Ix, Iy, |grad I| and the TO orientation on the
  * 2x grid ((2h) x (2w) row-major, dtype planes_dtype = TOED_F32 or TOED_F64,
  * the latter computed in FP64 throughout); toed_nms_planes writes the subpixel
- * position maps (zero where no edgel), as gpu_convolve / gpu_nms do. */
+ * position maps (zero where no edgel), as gpu_convolve / gpu_nms do.
+ * `taps` (optional, host) overrides the generated filters: 8 rows of 2r+3
+ * doubles, G, Gx, Gxx, Gxxx then the +0.5-shifted set, entry k at offset
+ * k-(r+1) -- the arrays the reference passes to gpu_convolve. */
 toed_status toed_convolve_planes(const void* pixels, int dtype, int h, int w, int pitch,
-                                 float sigma, int radius, int planes_dtype, void* Ix, void* Iy,
-                                 void* grad_mag, void* orient, cudaStream_t stream);
+                                 float sigma, int radius, const double* taps, int planes_dtype,
+                                 void* Ix, void* Iy, void* grad_mag, void* orient,
+                                 cudaStream_t stream);
 toed_status toed_nms_planes(int planes_dtype, int interp_h, int interp_w, const void* Ix,
                             const void* Iy, const void* grad_mag, float threshold, int border,
                             void* pos_x_map, void* pos_y_map, cudaStream_t stream);

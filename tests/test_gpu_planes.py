@@ -17,7 +17,7 @@ def _planes(toed, img, sigma, dt):
     P = [torch.zeros((2 * H, 2 * W), dtype=tdt, device="cuda") for _ in range(4)]
     src_dt = {np.uint8: toed.TOED_U8, np.float32: toed.TOED_F32, np.float64: toed.TOED_F64}[img.dtype.type]
     s = torch.cuda.current_stream().cuda_stream
-    st = toed.lib().toed_convolve_planes(ctypes.c_void_p(x.data_ptr()), src_dt, H, W, W, float(sigma), 0, dt,
+    st = toed.lib().toed_convolve_planes(ctypes.c_void_p(x.data_ptr()), src_dt, H, W, W, float(sigma), 0, None, dt,
                                          *[ctypes.c_void_p(p.data_ptr()) for p in P], ctypes.c_void_p(s))
     assert st == 0
     pos = [torch.zeros((2 * H, 2 * W), dtype=tdt, device="cuda") for _ in range(2)]

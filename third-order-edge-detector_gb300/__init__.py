@@ -97,8 +97,8 @@ def lib():
         L.toed_detect_batch.argtypes = [vp, ctypes.POINTER(toed_image), ip,
                                         ctypes.POINTER(toed_params), vp]
         L.toed_device_flags.argtypes = [vp, vp, ctypes.POINTER(ip)]
-        L.toed_convolve_planes.argtypes = [vp, ip, ip, ip, ip, ctypes.c_float, ip, ip, vp, vp, vp, vp,
-                                           vp]
+        L.toed_convolve_planes.argtypes = [vp, ip, ip, ip, ip, ctypes.c_float, ip, vp, ip, vp, vp, vp,
+                                           vp, vp]
         L.toed_nms_planes.argtypes = [ip, ip, ip, vp, vp, vp, ctypes.c_float, ip, vp, vp, vp]
         L.toed_profile_begin.argtypes = [vp]
         L.toed_profile_end.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ip)]

@@ -94,6 +94,14 @@ struct toed_ctx {
     long long tile_cap = 0;
     long long* img_base = nullptr;
     int img_cap = 0;
+    float2* dir = nullptr;
+    int* eid = nullptr;
+    int* win = nullptr;
+    long long px_cap = 0, px_cap2 = 0, px_cap3 = 0;
+    int* img_count = nullptr;
+    long long img_count_cap = 0;
+    unsigned char* keep = nullptr;
+    long long keep_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
@@ -166,6 +174,11 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->seg);
     cudaFree(c->tile_sum);
     cudaFree(c->img_base);
+    cudaFree(c->dir);
+    cudaFree(c->eid);
+    cudaFree(c->win);
+    cudaFree(c->img_count);
+    cudaFree(c->keep);
     cudaSetDevice(prev);
     delete c;
     return TOED_OK;
@@ -297,6 +310,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
         const long long nseg = 2LL * im.height * d.nsc;
+        d.nseg = nseg;
         units += (long long)d.nsc * d.nsr;
         tiles += (nseg + kSegTile - 1) / kSegTile;
         staging += im.capacity;
@@ -404,4 +418,73 @@ extern "C" toed_status toed_profile_end(toed_ctx* c, double* kernel_ms, int* lau
         return TOED_ERR_CUDA;
     }
     return TOED_OK;
+}
+
+extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edgemap* maps, int n,
+                                                    const toed_subpix_params* prm, cudaStream_t stream)
+{
+    if (!c || !maps || n <= 0 || !prm) return TOED_ERR_INVALID_ARG;
+    if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma) || !std::isfinite(prm->thresh) ||
+        !std::isfinite(prm->nbr_radius))
+        return TOED_ERR_INVALID_ARG;
+    if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
+    if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
+    const int r = (int)std::ceil((double)prm->sigma * 4.0);  // build_gaussian_kernels radius
+    if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
+    for (int i = 0; i < n; ++i) {
+        const toed_edgemap& m = maps[i];
+        if (!m.E || !m.edgels || !m.count || m.height < 2 || m.width < 2 || m.pitch < m.width || m.capacity < 0)
+            return TOED_ERR_INVALID_ARG;
+        if (m.dtype != TOED_F32 && m.dtype != TOED_F64) return TOED_ERR_UNSUPPORTED;
+        if ((long long)m.height * m.width >= (1LL << 31)) return TOED_ERR_UNSUPPORTED;
+        if ((reinterpret_cast<uintptr_t>(m.edgels) & 15u) != 0) return TOED_ERR_INVALID_ARG;
+    }
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    if (prev != c->device) TOED_CU(cudaSetDevice(c->device));
+    toed_status st = TOED_OK;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax) {
+            const int cn = std::min(kBatchMax, n - i0);
+            const toed_edgemap* mp = maps + i0;
+            long long px = 0, stag = 0, segs = 0, segtiles = 0;
+            for (int i = 0; i < cn; ++i) {
+                const long long hw = (long long)mp[i].height * mp[i].width;
+                px += hw;
+                // every NMS edgel is staged before isolated ones are removed:
+                // at most one per pixel, in practice far fewer than half
+                stag += std::max<long long>(mp[i].capacity, hw / 2 + 1024);
+                const long long nseg = (long long)mp[i].height * ((mp[i].width + 31) / 32);
+                segtiles += (nseg + kSegTile - 1) / kSegTile;
+            }
+            segs = segtiles * kSegTile;
+            if ((st = ensure_scratch(c, stag, segs, segtiles, cn, stream)) != TOED_OK) break;
+            if ((st = grow(&c->dir, &c->px_cap, px, stream)) != TOED_OK) break;
+            if ((st = grow(&c->eid, &c->px_cap2, px, stream)) != TOED_OK) break;
+            if ((st = grow(&c->win, &c->px_cap3, px, stream)) != TOED_OK) break;
+            if ((st = grow(&c->img_count, &c->img_count_cap, (long long)cn, stream)) != TOED_OK) break;
+            if ((st = grow(&c->keep, &c->keep_cap, c->staging_cap, stream)) != TOED_OK) break;
+            SubScratch s;
+            s.sc.words = c->words;
+            s.sc.staging = c->staging;
+            s.sc.staging_idx = c->staging_idx;
+            s.sc.staging_cap = std::min(c->staging_cap, c->keep_cap);
+            s.sc.seg = c->seg;
+            s.sc.tile_sum = c->tile_sum;
+            s.sc.img_base = c->img_base;
+            s.dir = c->dir;
+            s.eid = c->eid;
+            s.win = c->win;
+            s.img_count = c->img_count;
+            s.keep = c->keep;
+            cudaError_t e = subpix_launch(mp, cn, prm, r, s, stream);
+            if (e != cudaSuccess) {
+                g_last_cuda_error = std::string("subpix_launch: ") + cudaGetErrorString(e);
+                st = TOED_ERR_CUDA;
+            }
+        }
+    }
+    if (prev != c->device) cudaSetDevice(prev);
+    return st;
 }

@@ -40,6 +40,7 @@ struct DetImage {
     int* count;          // user count word
     int* index;          // optional grid index output
     long long seg_base;  // first segment of this image (tile aligned)
+    long long nseg;      // segments of this image (rows x strip/tile columns)
     int H, W;
     int dtype;
     int cap;

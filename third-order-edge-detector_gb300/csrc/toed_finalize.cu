@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) fin_tile_sums(const __grid_constant__ Bat
     const int t = blockIdx.x;
     const int k = find_image(p.n_img, t, [&](int i) { return p.img[i].tile_base; });
     const DetImage& im = p.img[k];
-    const long long nseg = 2LL * im.H * im.nsc;
+    const long long nseg = im.nseg;
     const long long first = (long long)(t - im.tile_base) * kSegTile;
     int sum = 0;
     for (int i = threadIdx.x; i < kSegTile; i += blockDim.x) {
@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kSegTile) fin_scatter(const __grid_constant__ 
     const int t = blockIdx.x;
     const int k = find_image(p.n_img, t, [&](int i) { return p.img[i].tile_base; });
     const DetImage& im = p.img[k];
-    const long long nseg = 2LL * im.H * im.nsc;
+    const long long nseg = im.nseg;
     const long long q = (long long)(t - im.tile_base) * kSegTile + threadIdx.x;
     const int2 sg = (q < nseg) ? p.sc.seg[im.seg_base + q] : make_int2(0, 0);
     int total;

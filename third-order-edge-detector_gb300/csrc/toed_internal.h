@@ -4,9 +4,9 @@
 #include <cstddef>
 #include <cuda_runtime.h>
 
-namespace toed {
+#include "toed_common.cuh"
 
-struct BatchParams;
+namespace toed {
 
 // One compiled detection kernel: entry point and its dynamic shared memory.
 struct DetectEntry {
@@ -18,5 +18,19 @@ struct DetectEntry {
 DetectEntry detect_entry(int radius, bool hyb);
 
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
+
+// Scratch of the TO-correction pipeline (owned by the caller's context).
+struct SubScratch {
+    Scratch sc;
+    float2* dir;          // per pixel
+    int* eid;             // per pixel
+    int* win;             // per pixel (dense maps)
+    int* img_count;       // per map
+    unsigned char* keep;  // per staged edgel
+};
+
+// Enqueue the TO-correction kernels for up to kBatchMax maps (toed_subpix.cu).
+cudaError_t subpix_launch(const toed_edgemap* maps, int n, const toed_subpix_params* prm, int r,
+                          const SubScratch& s, cudaStream_t stream);
 
 }  // namespace toed

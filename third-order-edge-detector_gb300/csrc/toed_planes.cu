@@ -157,8 +157,8 @@ __global__ void __launch_bounds__(256) nms_kernel(int H2, int W2, const T* Ix, c
 }
 
 template <typename T>
-cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, float sigma, int r, void* Ix,
-                       void* Iy, void* gm, void* orient, cudaStream_t stream)
+cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, float sigma, int r,
+                       const double* taps, void* Ix, void* Iy, void* gm, void* orient, cudaStream_t stream)
 {
     TapBlock tb;
     make_taps((double)sigma, r, &tb);
@@ -175,6 +175,9 @@ cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, f
                                     ((x * (3.0 * s * s - x * x)) * e) / (nrm * s * s * s * s * s * s * s)};
             for (int f = 0; f < 4; ++f) tt.v[4 * sh + f][k] = sizeof(T) == 4 ? (T)tb.v[4 * sh + f][k] : (T)vals[f];
         }
+    if (taps)
+        for (int f = 0; f < 8; ++f)
+            for (int k = 0; k < 2 * r + 3; ++k) tt.v[f][k] = (T)taps[f * (2 * r + 3) + k];
     const int NR = TH + 2 * r + 2, NIN = TW + 2 * r + 2;
     const size_t smem = sizeof(T) * ((size_t)NR * NIN + 12 * (size_t)NR * TW);
     cudaError_t e = cudaFuncSetAttribute((const void*)planes_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -192,19 +195,20 @@ cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, f
 using namespace toed;
 
 extern "C" toed_status toed_convolve_planes(const void* pixels, int dtype, int h, int w, int pitch, float sigma,
-                                            int radius, int planes_dtype, void* Ix, void* Iy, void* grad_mag,
-                                            void* orient, cudaStream_t stream)
+                                            int radius, const double* taps, int planes_dtype, void* Ix, void* Iy,
+                                            void* grad_mag, void* orient, cudaStream_t stream)
 {
     if (!pixels || !Ix || !Iy || !grad_mag || !orient || h <= 0 || w <= 0 || pitch < w) return TOED_ERR_INVALID_ARG;
-    if (!(sigma > 0.f)) return TOED_ERR_INVALID_ARG;
+    if (!(sigma > 0.f) && !taps) return TOED_ERR_INVALID_ARG;
+    if (taps && radius <= 0) return TOED_ERR_INVALID_ARG;
     if (dtype != TOED_U8 && dtype != TOED_F32 && dtype != TOED_F64) return TOED_ERR_UNSUPPORTED;
     const int r = radius > 0 ? radius : (int)std::ceil(4.0 * (double)sigma);
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
     cudaError_t e;
     if (planes_dtype == TOED_F32)
-        e = run_planes<float>(pixels, dtype, h, w, pitch, sigma, r, Ix, Iy, grad_mag, orient, stream);
+        e = run_planes<float>(pixels, dtype, h, w, pitch, sigma, r, taps, Ix, Iy, grad_mag, orient, stream);
     else if (planes_dtype == TOED_F64)
-        e = run_planes<double>(pixels, dtype, h, w, pitch, sigma, r, Ix, Iy, grad_mag, orient, stream);
+        e = run_planes<double>(pixels, dtype, h, w, pitch, sigma, r, taps, Ix, Iy, grad_mag, orient, stream);
     else
         return TOED_ERR_INVALID_ARG;
     return e == cudaSuccess ? TOED_OK : TOED_ERR_CUDA;

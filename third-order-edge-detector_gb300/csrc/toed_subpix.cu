@@ -1,0 +1,750 @@
+// toed_subpix.cu -- subpixel third-order correction of dense edge maps on
+// GB300: the reference's SubpixelTOCorrectionCPU<T>::estimate_orientation()
+// + run() (subpix_TO_correction/subpix_to_correction.cpp:307-736, interp_n=0)
+// as five short kernels over a batch of maps:
+//
+//   tc_orient_nms   one CTA per 32x32 tile: triangle smoothing (r = 4,
+//                   symmetric padding), gradient2 with one-sided borders and
+//                   the Hessian orientation (:307-375) -- or the caller's
+//                   orientation -- then dir = (cos, sin) (:296-305) and NMS
+//                   along dir on E with the parabola fit (:413-519); edgels are
+//                   compacted in row-major order into staging with a
+//                   (row, tile column) segment table and a per-pixel id map.
+//   tc_correct      one CTA per tile that holds edgels: the eight circular
+//                   separable Gaussian-derivative convolutions (:377-411,
+//                   :641-648) fused over the tile + halo in shared memory
+//                   (6 row filters, 8 column filters), then per edgel the Keys
+//                   bicubic samples of ten planes (:521-556) and the corrected
+//                   orientation (:663-694).
+//   tc_isolate      per segment: an edgel survives if another lies within
+//                   the neighbour radius in the reference's 3x3 cell grid
+//                   (:563-621), found through the id map.
+//   tc_compact      per segment: stable in-place compaction of survivors.
+//   then the ordering pass of toed_finalize.cu, and tc_dense (two passes)
+//   for the dense TO_E / TO_O maps at round(x, y), later edgels winning
+//   (:708-715).
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+#include "toed_common.cuh"
+#include "toed_internal.h"
+
+namespace toed {
+
+constexpr int kT = 32;   // tile side (pixels)
+constexpr int kTriR = 4; // triangle filter radius (:316)
+
+struct SubMap {
+    const void* E;
+    const void* theta;
+    long long pitch;
+    long long px_base;   // offset of this map in the per-pixel scratch planes
+    void* TO_E;
+    void* TO_O;
+    int h, w, dtype;
+    int ntx, nty;
+    int tile_base;       // first spatial tile of this map
+    long long seg_base;  // first (row, tile column) segment, kSegTile aligned
+    int seg_tile_base;   // first segment tile
+};
+
+struct SubParams {
+    float g[3][kMaxTaps];  // G, dG, d2G at integer offsets -r..r (index k <-> k - r)
+    int r;
+    float thresh;
+    double nbr;
+    int hyb;
+    int out_f64;
+    int n_maps;
+    int n_tiles;
+    Scratch sc;
+    float2* dir;         // per pixel (cos, sin) of the NMS direction
+    int* eid;            // per pixel staging index of its edgel or -1
+    int* img_count;      // per map number of NMS edgels (before removal)
+    int* win;            // per pixel winning list index for the dense maps
+    unsigned char* keep; // per staged edgel: survives the isolation test
+    int n_seg_tiles;
+    SubMap m[kBatchMax];
+};
+
+__device__ __forceinline__ int wrap_sym(int i, int n)
+{  // :47-55
+    if (n <= 1) return 0;
+    while (i < 0 || i >= n) i = (i < 0) ? -i - 1 : 2 * n - i - 1;
+    return i;
+}
+
+__device__ __forceinline__ int wrap_circ(int i, int n)
+{  // :40-45
+    int r = i % n;
+    return r < 0 ? r + n : r;
+}
+
+__device__ __forceinline__ float load_map(const void* p, int dtype, long long o)
+{
+    return dtype == TOED_F64 ? (float)__ldg((const double*)p + o) : __ldg((const float*)p + o);
+}
+
+__device__ __forceinline__ double cubic_w(double s)
+{  // Keys kernel, a = -0.5 (:57-67)
+    const double a = -0.5;
+    const double x = fabs(s);
+    if (x <= 1.0) return ((a + 2) * x - (a + 3)) * x * x + 1;
+    if (x < 2.0) return ((a * x - 5 * a) * x + 8 * a) * x - 4 * a;
+    return 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// Orientation + NMS
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ SubParams p)
+{
+    constexpr int HE = 6, NE = kT + 2 * HE;  // E region: rows/cols i0-6 .. i0+37
+    __shared__ float sE[NE][NE + 1];
+    __shared__ float sTmp[NE][kT + 4];        // cols j0-2 .. j0+33
+    __shared__ float sSm[kT + 4][kT + 4];     // rows/cols -2 .. +33
+    __shared__ float sOx[kT + 2][kT + 3], sOy[kT + 2][kT + 3];  // -1 .. +32
+    __shared__ float2 sDir[kT][kT];
+    __shared__ int sRowCnt[kT], sRowOff[kT];
+
+    const int t = blockIdx.x;
+    const int k = find_image(p.n_maps, t, [&](int i) { return p.m[i].tile_base; });
+    const SubMap& M = p.m[k];
+    const int h = M.h, w = M.w, dtype = M.dtype;
+    const int lt = t - M.tile_base;
+    const int ty = lt / M.ntx, tx = lt - ty * M.ntx;
+    const int i0 = ty * kT, j0 = tx * kT;
+    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
+
+    for (int q = tid; q < NE * NE; q += blockDim.x) {
+        const int a = q / NE, b = q - a * NE;
+        const int ii = wrap_sym(i0 - HE + a, h), jj = wrap_sym(j0 - HE + b, w);
+        sE[a][b] = load_map(M.E, dtype, (long long)ii * M.pitch + jj);
+    }
+    __syncthreads();
+
+    if (M.theta == nullptr) {
+        const float tri[9] = {1.f / 25, 2.f / 25, 3.f / 25, 4.f / 25, 5.f / 25, 4.f / 25, 3.f / 25, 2.f / 25, 1.f / 25};
+        for (int q = tid; q < NE * (kT + 4); q += blockDim.x) {
+            const int a = q / (kT + 4), c = q - a * (kT + 4);
+            float acc = 0.f;
+#pragma unroll
+            for (int qq = -kTriR; qq <= kTriR; ++qq) acc += sE[a][c + 4 - qq] * tri[qq + kTriR];
+            sTmp[a][c] = acc;
+        }
+        __syncthreads();
+        for (int q = tid; q < (kT + 4) * (kT + 4); q += blockDim.x) {
+            const int d = q / (kT + 4), c = q - d * (kT + 4);
+            float acc = 0.f;
+#pragma unroll
+            for (int pp = -kTriR; pp <= kTriR; ++pp) acc += sTmp[d + 4 - pp][c] * tri[pp + kTriR];
+            sSm[d][c] = acc;
+        }
+        __syncthreads();
+        // gradient2 (:346-355): central differences, one-sided at the borders
+        for (int q = tid; q < (kT + 2) * (kT + 2); q += blockDim.x) {
+            const int e = q / (kT + 2), f = q - e * (kT + 2);
+            const int i = i0 - 1 + e, j = j0 - 1 + f;
+            float ox = 0.f, oy = 0.f;
+            if (i >= 0 && i < h && j >= 0 && j < w) {
+                const int d = e + 1, c = f + 1;
+                ox = (j == 0) ? sSm[d][c + 1] - sSm[d][c]
+                              : (j == w - 1 ? sSm[d][c] - sSm[d][c - 1] : 0.5f * (sSm[d][c + 1] - sSm[d][c - 1]));
+                oy = (i == 0) ? sSm[d + 1][c] - sSm[d][c]
+                              : (i == h - 1 ? sSm[d][c] - sSm[d - 1][c] : 0.5f * (sSm[d + 1][c] - sSm[d - 1][c]));
+            }
+            sOx[e][f] = ox;
+            sOy[e][f] = oy;
+        }
+        __syncthreads();
+    }
+    const float PI_F = 3.14159265358979323846f;
+    for (int q = tid; q < kT * kT; q += blockDim.x) {
+        const int a = q >> 5, b = q & 31;
+        const int i = i0 + a, j = j0 + b;
+        float th = 0.f;
+        if (i < h && j < w) {
+            if (M.theta) {
+                th = load_map(M.theta, dtype, (long long)i * M.pitch + j);
+            } else {
+                const int e = a + 1, f = b + 1;
+                const float oxx = (j == 0) ? sOx[e][f + 1] - sOx[e][f]
+                                           : (j == w - 1 ? sOx[e][f] - sOx[e][f - 1] : 0.5f * (sOx[e][f + 1] - sOx[e][f - 1]));
+                const float oxy = (j == 0) ? sOy[e][f + 1] - sOy[e][f]
+                                           : (j == w - 1 ? sOy[e][f] - sOy[e][f - 1] : 0.5f * (sOy[e][f + 1] - sOy[e][f - 1]));
+                const float oyy = (i == 0) ? sOy[e + 1][f] - sOy[e][f]
+                                           : (i == h - 1 ? sOy[e][f] - sOy[e - 1][f] : 0.5f * (sOy[e + 1][f] - sOy[e - 1][f]));
+                const float sgn = (oxy < 0.f) ? 1.f : ((oxy > 0.f) ? -1.f : 0.f);
+                th = atanf(oyy * sgn / (oxx + 1e-5f));  // :370-371
+            }
+            // wrap_mod_pi (:216-222), then compute_dir_from_theta (:296-305)
+            float a2 = fmodf(th, PI_F);
+            if (a2 < 0.f) a2 += PI_F;
+            float sn, cs;
+            sincosf(a2, &sn, &cs);
+            sDir[a][b] = make_float2(cs, sn);
+            p.dir[M.px_base + (long long)i * w + j] = make_float2(cs, sn);
+        }
+    }
+    __syncthreads();
+
+    // NMS along dir on E (:424-514), margin 3: i, j in [4, dim - 5)
+    unsigned bal[4];
+    double rx[4], ry[4], rm[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int a = wid + 8 * u, b = lane;
+        const int i = i0 + a, j = j0 + b;
+        bool acc = false;
+        rx[u] = ry[u] = rm[u] = 0.0;
+        if (i >= 4 && i < h - 5 && j >= 4 && j < w - 5) {
+            const float f = sE[a + HE][b + HE];
+            const float2 g = sDir[a][b];
+            if (f > p.thresh && !(fabsf(g.x) < 1e-5f && fabsf(g.y) < 1e-5f)) {
+                // eight sectors of :453-493 in closed form (x-major when |gx| >= |gy|)
+                const bool xmaj = fabsf(g.x) >= fabsf(g.y);
+                const int sx = g.x >= 0.f ? 1 : -1, sy = g.y >= 0.f ? 1 : -1;
+                const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+                const float Map = sE[a + HE + ar][b + HE + ac], Mdp = sE[a + HE + sy][b + HE + sx];
+                const float Mam = sE[a + HE - ar][b + HE - ac], Mdm = sE[a + HE - sy][b + HE - sx];
+                if (p.hyb) {
+                    const double gx = g.x, gy = g.y, fd = f;
+                    const double md = sqrt(gx * gx + gy * gy);
+                    const double nx = gx / md, ny = gy / md;
+                    const double sl = xmaj ? fabs(ny) / fabs(nx) : fabs(nx) / fabs(ny);
+                    const double fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
+                    if ((fd > fm && fd >= fp) || (fd >= fm && fd > fp)) {
+                        const double s = sqrt(1 + sl * sl);
+                        const double A = (fm + fp - 2 * fd) / (2 * s * s), B = (fp - fm) / (2 * s);
+                        if (!(fabs(A) < 1e-16)) {
+                            const double ss = -B / (2 * A);
+                            const double mf = A * ss * ss + B * ss + fd;
+                            if (fabs(ss) <= 1.4142135623730951) {
+                                acc = true;
+                                rx[u] = (double)j + ss * nx;
+                                ry[u] = (double)i + ss * ny;
+                                rm[u] = fabs(mf);
+                            }
+                        }
+                    }
+                } else {
+                    const float md = sqrtf(g.x * g.x + g.y * g.y);
+                    const float nx = g.x / md, ny = g.y / md;
+                    const float sl = xmaj ? fabsf(ny) / fabsf(nx) : fabsf(nx) / fabsf(ny);
+                    const float fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
+                    if ((f > fm && f >= fp) || (f >= fm && f > fp)) {
+                        const float s = sqrtf(1 + sl * sl);
+                        const float A = (fm + fp - 2 * f) / (2 * s * s), B = (fp - fm) / (2 * s);
+                        if (!(fabsf(A) < 1e-16f)) {
+                            const float ss = -B / (2 * A);
+                            const float mf = A * ss * ss + B * ss + f;
+                            if (fabsf(ss) <= 1.41421356f) {
+                                acc = true;
+                                rx[u] = (double)((float)j + ss * nx);
+                                ry[u] = (double)((float)i + ss * ny);
+                                rm[u] = (double)fabsf(mf);
+                            }
+                        }
+                    }
+                }
+            }
+        }
+        bal[u] = __ballot_sync(0xffffffffu, acc);
+        if (lane == 0) sRowCnt[a] = __popc(bal[u]);
+    }
+    __syncthreads();
+    if (wid == 0) {
+        const int cnt = sRowCnt[lane];
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        const int total = __shfl_sync(0xffffffffu, incl, 31);
+        int base = 0;
+        if (lane == 0 && total > 0) {
+            base = atomicAdd(&p.sc.words[1], total);
+            atomicAdd(&p.img_count[k], total);
+            if ((long long)base + total > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
+        }
+        base = __shfl_sync(0xffffffffu, base, 0);
+        sRowOff[lane] = base + incl - cnt;
+        // segment (row, tile column) -> {staging offset, count}
+        const int i = i0 + lane;
+        if (i < h) p.sc.seg[M.seg_base + (long long)i * M.ntx + tx] = make_int2(base + incl - cnt, cnt);
+    }
+    __syncthreads();
+    const unsigned ltm = (1u << lane) - 1u;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int a = wid + 8 * u, b = lane;
+        const int i = i0 + a, j = j0 + b;
+        if (i >= h || j >= w) continue;
+        int id = -1;
+        if ((bal[u] >> lane) & 1u) {
+            id = sRowOff[a] + __popc(bal[u] & ltm);
+            if (id < p.sc.staging_cap) {
+                p.sc.staging[id] = make_double4_32a(rx[u], ry[u], 0.0, rm[u]);
+                p.sc.staging_idx[id] = i * w + j;
+            } else {
+                id = -1;
+            }
+        }
+        p.eid[M.px_base + (long long)i * w + j] = id;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Fused convolutions + per-edgel orientation correction
+// ---------------------------------------------------------------------------
+template <int R>
+struct CorrCfg {
+    static constexpr int HB = 3;                  // bicubic reach around a tile pixel
+    static constexpr int NO = kT + 2 * HB;        // 38: conv output region side
+    static constexpr int NI = NO + 2 * R;         // input region side
+    static constexpr size_t off_E = 0;                                   // [NI][NI]
+    static constexpr size_t off_Hx = off_E + sizeof(float) * NI * NI;    // [NI][NI]
+    static constexpr size_t off_Hy = off_Hx + sizeof(float) * NI * NI;   // [NI][NI]
+    static constexpr size_t off_row = off_Hy + sizeof(float) * NI * NI;  // 6 x [NI][NO]
+    static constexpr size_t off_col = off_row + sizeof(float) * 6 * NI * NO;  // 8 x [NO][NO]
+    static constexpr size_t off_misc = off_col + sizeof(float) * 8 * NO * NO;
+    static constexpr size_t smem = off_misc + sizeof(int) * 2 * (kT + 1);
+};
+
+template <int R>
+__global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubParams p)
+{
+    using C = CorrCfg<R>;
+    constexpr int NI = C::NI, NO = C::NO, HB = C::HB;
+    extern __shared__ __align__(16) unsigned char smem[];
+    float* sE = reinterpret_cast<float*>(smem + C::off_E);
+    float* sHx = reinterpret_cast<float*>(smem + C::off_Hx);
+    float* sHy = reinterpret_cast<float*>(smem + C::off_Hy);
+    float* sRow = reinterpret_cast<float*>(smem + C::off_row);
+    float* sCol = reinterpret_cast<float*>(smem + C::off_col);
+    int* sOff = reinterpret_cast<int*>(smem + C::off_misc);  // [kT+1] exclusive prefix of row counts
+    int* sSegOff = sOff + kT + 1;                             // [kT] staging offsets
+
+    const int t = blockIdx.x;
+    const int k = find_image(p.n_maps, t, [&](int i) { return p.m[i].tile_base; });
+    const SubMap& M = p.m[k];
+    const int h = M.h, w = M.w;
+    const int lt = t - M.tile_base;
+    const int ty = lt / M.ntx, tx = lt - ty * M.ntx;
+    const int i0 = ty * kT, j0 = tx * kT;
+    const int tid = threadIdx.x;
+
+    if (tid < 32) {
+        const int i = i0 + tid;
+        int2 sg = make_int2(0, 0);
+        if (i < h) sg = p.sc.seg[M.seg_base + (long long)i * M.ntx + tx];
+        int incl = sg.y;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (tid >= d) incl += y;
+        }
+        sOff[tid + 1] = incl;
+        if (tid == 0) sOff[0] = 0;
+        sSegOff[tid] = sg.x;
+    }
+    __syncthreads();
+    const int n_edg = sOff[kT];
+    if (n_edg == 0) return;  // tiles without edgels need no convolution
+
+    // inputs with circular wrap: E, Hx = E dirx, Hy = E diry (:634-638)
+    const int ri = i0 - HB - R, rj = j0 - HB - R;
+    for (int q = tid; q < NI * NI; q += blockDim.x) {
+        const int a = q / NI, b = q - a * NI;
+        const int ii = wrap_circ(ri + a, h), jj = wrap_circ(rj + b, w);
+        const float e = load_map(M.E, M.dtype, (long long)ii * M.pitch + jj);
+        const float2 d = p.dir[M.px_base + (long long)ii * w + jj];
+        sE[q] = e;
+        sHx[q] = e * d.x;
+        sHy[q] = e * d.y;
+    }
+    __syncthreads();
+    // row pass (along j): E -> G, dG, d2G ; Hx -> dG ; Hy -> G, dG
+    // out(x) = sum_q src(x - q) k(q)  (:392-396)
+    for (int q = tid; q < NI * NO; q += blockDim.x) {
+        const int a = q / NO, c = q - a * NO;
+        const float* e = sE + a * NI + c + R;
+        const float* hx = sHx + a * NI + c + R;
+        const float* hy = sHy + a * NI + c + R;
+        float eG = 0.f, edG = 0.f, ed2G = 0.f, xdG = 0.f, yG = 0.f, ydG = 0.f;
+#pragma unroll
+        for (int qq = -R; qq <= R; ++qq) {
+            const float g0 = p.g[0][qq + R], g1 = p.g[1][qq + R], g2 = p.g[2][qq + R];
+            const float ve = e[-qq], vx = hx[-qq], vy = hy[-qq];
+            eG = fmaf(ve, g0, eG);
+            edG = fmaf(ve, g1, edG);
+            ed2G = fmaf(ve, g2, ed2G);
+            xdG = fmaf(vx, g1, xdG);
+            yG = fmaf(vy, g0, yG);
+            ydG = fmaf(vy, g1, ydG);
+        }
+        sRow[(0 * NI + a) * NO + c] = eG;
+        sRow[(1 * NI + a) * NO + c] = edG;
+        sRow[(2 * NI + a) * NO + c] = ed2G;
+        sRow[(3 * NI + a) * NO + c] = xdG;
+        sRow[(4 * NI + a) * NO + c] = yG;
+        sRow[(5 * NI + a) * NO + c] = ydG;
+    }
+    __syncthreads();
+    // column pass (along i): planes 0 Px 1 Py 2 Pxx 3 Pxy 4 Pyy 5 Hxx 6 Hyy 7 Hxy (:641-648)
+    for (int q = tid; q < NO * NO; q += blockDim.x) {
+        const int a = q / NO, c = q - a * NO;
+        float px = 0.f, py = 0.f, pxx = 0.f, pxy = 0.f, pyy = 0.f, hxx = 0.f, hyy = 0.f, hxy = 0.f;
+#pragma unroll
+        for (int pp = -R; pp <= R; ++pp) {
+            const int row = a + R - pp;
+            const float g0 = p.g[0][pp + R], g1 = p.g[1][pp + R], g2 = p.g[2][pp + R];
+            const float eG = sRow[(0 * NI + row) * NO + c], edG = sRow[(1 * NI + row) * NO + c];
+            const float ed2G = sRow[(2 * NI + row) * NO + c], xdG = sRow[(3 * NI + row) * NO + c];
+            const float yG = sRow[(4 * NI + row) * NO + c], ydG = sRow[(5 * NI + row) * NO + c];
+            px = fmaf(edG, g0, px);    // (dG, G)  E
+            py = fmaf(eG, g1, py);     // (G, dG)  E
+            pxx = fmaf(ed2G, g0, pxx); // (d2G, G) E
+            pxy = fmaf(edG, g1, pxy);  // (dG, dG) E
+            pyy = fmaf(eG, g2, pyy);   // (G, d2G) E
+            hxx = fmaf(xdG, g0, hxx);  // (dG, G)  Hx
+            hyy = fmaf(yG, g1, hyy);   // (G, dG)  Hy
+            hxy = fmaf(ydG, g0, hxy);  // (dG, G)  Hy
+        }
+        sCol[0 * NO * NO + q] = px;
+        sCol[1 * NO * NO + q] = py;
+        sCol[2 * NO * NO + q] = pxx;
+        sCol[3 * NO * NO + q] = pxy;
+        sCol[4 * NO * NO + q] = pyy;
+        sCol[5 * NO * NO + q] = hxx;
+        sCol[6 * NO * NO + q] = hyy;
+        sCol[7 * NO * NO + q] = hxy;
+    }
+    __syncthreads();
+    // per edgel: Keys bicubic of ten planes at (sx, sy), clamp to the image (:521-556)
+    for (int e = tid; e < n_edg; e += blockDim.x) {
+        int row = 0;
+        while (sOff[row + 1] <= e) ++row;
+        const long long sidx = (long long)sSegOff[row] + (e - sOff[row]);
+        if (sidx >= p.sc.staging_cap) continue;
+        double4_32a rec = p.sc.staging[sidx];
+        const double sx = rec.x, sy = rec.y;
+        const int x0 = (int)floor(sx), y0 = (int)floor(sy);
+        const double fx = sx - x0, fy = sy - y0;
+        double wx[4], wy[4];
+        wx[0] = cubic_w(fx + 1); wx[1] = cubic_w(fx); wx[2] = cubic_w(fx - 1); wx[3] = cubic_w(fx - 2);
+        wy[0] = cubic_w(fy + 1); wy[1] = cubic_w(fy); wy[2] = cubic_w(fy - 1); wy[3] = cubic_w(fy - 2);
+        // plane order for interpolation: Px Py Pxx Pyy Pxy Hx Hxx Hxy Hyy Hy
+        double v[10];
+#pragma unroll
+        for (int pl = 0; pl < 10; ++pl) v[pl] = 0.0;
+        for (int pp = 0; pp < 4; ++pp) {
+            int ii = y0 - 1 + pp;
+            ii = ii < 0 ? 0 : (ii >= h ? h - 1 : ii);
+            const int ra = ii - (i0 - HB);           // row in the conv region
+            const int rin = ii - ri;                 // row in the input region
+            double rowv[10];
+#pragma unroll
+            for (int pl = 0; pl < 10; ++pl) rowv[pl] = 0.0;
+            for (int qq = 0; qq < 4; ++qq) {
+                int jj = x0 - 1 + qq;
+                jj = jj < 0 ? 0 : (jj >= w ? w - 1 : jj);
+                const int ca = jj - (j0 - HB);
+                const int cin = jj - rj;
+                const int o = ra * NO + ca;
+                const double wq = wx[qq];
+                rowv[0] += (double)sCol[0 * NO * NO + o] * wq;
+                rowv[1] += (double)sCol[1 * NO * NO + o] * wq;
+                rowv[2] += (double)sCol[2 * NO * NO + o] * wq;
+                rowv[3] += (double)sCol[4 * NO * NO + o] * wq;
+                rowv[4] += (double)sCol[3 * NO * NO + o] * wq;
+                rowv[5] += (double)sHx[rin * NI + cin] * wq;
+                rowv[6] += (double)sCol[5 * NO * NO + o] * wq;
+                rowv[7] += (double)sCol[7 * NO * NO + o] * wq;
+                rowv[8] += (double)sCol[6 * NO * NO + o] * wq;
+                rowv[9] += (double)sHy[rin * NI + cin] * wq;
+            }
+#pragma unroll
+            for (int pl = 0; pl < 10; ++pl) v[pl] += rowv[pl] * wy[pp];
+        }
+        const double Px = v[0], Py = v[1], Pxx = v[2], Pyy = v[3], Pxy = v[4];
+        const double Hx = v[5], Hxx = v[6], Hxy = v[7], Hyy = v[8], Hy = v[9];
+        double Fx = Px * Hxx + Pxx * Hx + Py * Hxy + Pxy * Hy;  // :683-684
+        double Fy = Px * Hxy + Pxy * Hx + Py * Hyy + Pyy * Hy;
+        const double Fm = sqrt(Fx * Fx + Fy * Fy);
+        float ori;
+        if (Fm < 1e-12) {
+            const int pi = p.sc.staging_idx[sidx];
+            const float2 d = p.dir[M.px_base + pi];
+            ori = atan2f(d.x, -d.y);
+        } else {
+            Fx /= Fm;
+            Fy /= Fm;
+            ori = atan2f((float)Fx, (float)(-Fy));
+        }
+        rec.z = (double)ori;
+        p.sc.staging[sidx] = rec;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Isolated-edgel removal (:563-621) and stable compaction
+// ---------------------------------------------------------------------------
+// segment tile t -> (map, first local segment)
+__device__ __forceinline__ int seg_map(const SubParams& p, int t)
+{
+    return find_image(p.n_maps, t, [&](int i) { return p.m[i].seg_tile_base; });
+}
+
+__global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubParams p)
+{
+    const int t = blockIdx.x;
+    const int k = seg_map(p, t);
+    const SubMap& M = p.m[k];
+    const long long nseg = (long long)M.h * M.ntx;
+    const bool all = !(p.nbr > 0.0) || p.img_count[k] < 2;  // :567-568
+    const double r2 = p.nbr * p.nbr, inv = 1.0 / p.nbr;
+    const int reach = (int)ceil(p.nbr + 1.5);  // an edgel lies within sqrt(2) of its pixel
+    for (int q = threadIdx.x; q < kSegTile; q += blockDim.x) {
+        const long long local = (long long)(t - M.seg_tile_base) * kSegTile + q;
+        if (local >= nseg) break;
+        const int2 sg = p.sc.seg[M.seg_base + local];
+        for (int e = 0; e < sg.y; ++e) {
+            const long long r = (long long)sg.x + e;
+            if (r >= p.sc.staging_cap) break;
+            if (all) {
+                p.keep[r] = 1;
+                continue;
+            }
+            const double4_32a me = p.sc.staging[r];
+            const long long cx = (long long)floor(me.x * inv), cy = (long long)floor(me.y * inv);
+            const int pi = (int)floor(me.y), pj = (int)floor(me.x);
+            bool found = false;
+            for (int ii = max(0, pi - reach); ii <= min(M.h - 1, pi + reach) && !found; ++ii) {
+                for (int jj = max(0, pj - reach); jj <= min(M.w - 1, pj + reach); ++jj) {
+                    const int o = p.eid[M.px_base + (long long)ii * M.w + jj];
+                    if (o < 0 || o == r) continue;
+                    const double4_32a ot = p.sc.staging[o];
+                    const long long ox = (long long)floor(ot.x * inv), oy = (long long)floor(ot.y * inv);
+                    if (ox < cx - 1 || ox > cx + 1 || oy < cy - 1 || oy > cy + 1) continue;  // 3x3 cells
+                    const double ddx = me.x - ot.x, ddy = me.y - ot.y;
+                    if (ddx * ddx + ddy * ddy <= r2) {
+                        found = true;
+                        break;
+                    }
+                }
+            }
+            p.keep[r] = found ? 1 : 0;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) tc_compact(const __grid_constant__ SubParams p)
+{
+    const int t = blockIdx.x;
+    const int k = seg_map(p, t);
+    const SubMap& M = p.m[k];
+    const long long nseg = (long long)M.h * M.ntx;
+    for (int q = threadIdx.x; q < kSegTile; q += blockDim.x) {
+        const long long local = (long long)(t - M.seg_tile_base) * kSegTile + q;
+        if (local >= nseg) break;
+        int2 sg = p.sc.seg[M.seg_base + local];
+        long long wpos = sg.x;
+        for (int e = 0; e < sg.y; ++e) {
+            const long long r = (long long)sg.x + e;
+            if (r >= p.sc.staging_cap) break;
+            if (p.keep[r]) {
+                if (wpos != r) {
+                    p.sc.staging[wpos] = p.sc.staging[r];
+                    p.sc.staging_idx[wpos] = p.sc.staging_idx[r];
+                }
+                ++wpos;
+            }
+        }
+        sg.y = (int)(wpos - sg.x);
+        p.sc.seg[M.seg_base + local] = sg;
+    }
+}
+
+// Dense TO_E / TO_O (:708-715): pass 0 elects, per pixel, the last edgel in
+// list order that rounds onto it; pass 1 writes its strength and orientation.
+template <int PASS>
+__global__ void __launch_bounds__(kSegTile) tc_dense(const __grid_constant__ SubParams p)
+{
+    __shared__ int s_warp[33];
+    const int t = blockIdx.x;
+    const int k = seg_map(p, t);
+    const SubMap& M = p.m[k];
+    const long long nseg = (long long)M.h * M.ntx;
+    const long long local = (long long)(t - M.seg_tile_base) * kSegTile + threadIdx.x;
+    const int2 sg = (local < nseg) ? p.sc.seg[M.seg_base + local] : make_int2(0, 0);
+    // block-wide exclusive scan of the segment counts (same order as the ordering pass)
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = sg.y;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        const int v = s_warp[lane];
+        int wi = v;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, d);
+            if (lane >= d) wi += y;
+        }
+        s_warp[lane] = wi - v;
+    }
+    __syncthreads();
+    if (M.TO_E == nullptr && M.TO_O == nullptr) return;
+    const long long dest = (long long)p.sc.tile_sum[t] + (incl - sg.y + s_warp[wid]) - p.sc.img_base[k];
+    for (int e = 0; e < sg.y; ++e) {
+        const long long r = (long long)sg.x + e;
+        if (r >= p.sc.staging_cap) break;
+        const double4_32a rec = p.sc.staging[r];
+        int X = (int)round(rec.x), Y = (int)round(rec.y);
+        X = max(0, min(X, M.w - 1));
+        Y = max(0, min(Y, M.h - 1));
+        const long long o = (long long)Y * M.w + X;
+        const int li = (int)(dest + e);
+        if (PASS == 0) {
+            atomicMax(&p.win[M.px_base + o], li);
+        } else if (p.win[M.px_base + o] == li) {
+            if (p.out_f64) {
+                if (M.TO_E) reinterpret_cast<double*>(M.TO_E)[o] = rec.w;
+                if (M.TO_O) reinterpret_cast<double*>(M.TO_O)[o] = rec.z;
+            } else {
+                if (M.TO_E) reinterpret_cast<float*>(M.TO_E)[o] = (float)rec.w;
+                if (M.TO_O) reinterpret_cast<float*>(M.TO_O)[o] = (float)rec.z;
+            }
+        }
+    }
+}
+
+template <int R>
+static const void* correct_kernel() { return (const void*)tc_correct<R>; }
+
+static const void* correct_entry(int r, size_t* smem)
+{
+    switch (r) {
+#define TOED_TC_CASE(R) \
+    case R: *smem = CorrCfg<R>::smem; return correct_kernel<R>();
+        TOED_TC_CASE(1) TOED_TC_CASE(2) TOED_TC_CASE(3) TOED_TC_CASE(4) TOED_TC_CASE(5) TOED_TC_CASE(6)
+        TOED_TC_CASE(7) TOED_TC_CASE(8) TOED_TC_CASE(9) TOED_TC_CASE(10) TOED_TC_CASE(11) TOED_TC_CASE(12)
+#undef TOED_TC_CASE
+    default: return nullptr;
+    }
+}
+
+// Host side of toed_subpix_to_correct_batch for one chunk of maps.
+cudaError_t subpix_launch(const toed_edgemap* maps, int n, const toed_subpix_params* prm, int r,
+                          const SubScratch& s, cudaStream_t stream)
+{
+    SubParams* p = new SubParams();
+    std::memset(p, 0, sizeof(SubParams));
+    const double sig = prm->sigma, s2 = sig * sig, s3 = s2 * sig, s5 = s2 * s3;
+    const double nrm = std::sqrt(2.0 * 3.14159265358979323846);
+    for (int kk = -r; kk <= r; ++kk) {  // build_gaussian_kernels :207-213
+        const double x = kk, e = std::exp(-(x * x) / (2.0 * s2));
+        p->g[0][kk + r] = (float)(e / (nrm * sig));
+        p->g[1][kk + r] = (float)(-x * e / (nrm * s3));
+        p->g[2][kk + r] = (float)((x * x - s2) * e / (nrm * s5));
+    }
+    p->r = r;
+    p->thresh = prm->thresh;
+    p->nbr = prm->nbr_radius;
+    p->hyb = prm->precision != TOED_FP32;
+    p->out_f64 = prm->out_dtype == TOED_F64;
+    p->n_maps = n;
+    long long px = 0, segtiles = 0;
+    int tiles = 0;
+    for (int i = 0; i < n; ++i) {
+        const toed_edgemap& m = maps[i];
+        SubMap& d = p->m[i];
+        d.E = m.E;
+        d.theta = m.theta;
+        d.pitch = m.pitch;
+        d.px_base = px;
+        d.TO_E = m.TO_E;
+        d.TO_O = m.TO_O;
+        d.h = m.height;
+        d.w = m.width;
+        d.dtype = m.dtype;
+        d.ntx = (m.width + kT - 1) / kT;
+        d.nty = (m.height + kT - 1) / kT;
+        d.tile_base = tiles;
+        d.seg_tile_base = (int)segtiles;
+        d.seg_base = segtiles * kSegTile;
+        const long long nseg = (long long)m.height * d.ntx;
+        tiles += d.ntx * d.nty;
+        segtiles += (nseg + kSegTile - 1) / kSegTile;
+        px += (long long)m.height * m.width;
+    }
+    p->n_tiles = tiles;
+    p->n_seg_tiles = (int)segtiles;
+    p->sc = s.sc;
+    p->dir = s.dir;
+    p->eid = s.eid;
+    p->win = s.win;
+    p->img_count = s.img_count;
+    p->keep = s.keep;
+    std::unique_ptr<SubParams> guard(p);
+
+    cudaError_t e = cudaMemsetAsync(s.sc.words, 0, 3 * sizeof(int), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.img_count, 0, sizeof(int) * n, stream);
+    void* args[] = {p};
+    if (e == cudaSuccess) e = cudaLaunchKernel((const void*)tc_orient_nms, dim3(tiles), dim3(256), args, 0, stream);
+    size_t smem = 0;
+    const void* cf = correct_entry(r, &smem);
+    if (!cf) return cudaErrorInvalidValue;
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(cf, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (e == cudaSuccess) e = cudaLaunchKernel(cf, dim3(tiles), dim3(512), args, smem, stream);
+    if (e == cudaSuccess) e = cudaLaunchKernel((const void*)tc_isolate, dim3(p->n_seg_tiles), dim3(256), args, 0, stream);
+    if (e == cudaSuccess) e = cudaLaunchKernel((const void*)tc_compact, dim3(p->n_seg_tiles), dim3(256), args, 0, stream);
+    // ordering pass shared with the detector
+    BatchParams* b = new BatchParams();
+    std::memset(b, 0, sizeof(BatchParams));
+    std::unique_ptr<BatchParams> bguard(b);
+    b->n_img = n;
+    b->n_tiles = p->n_seg_tiles;
+    b->out_f64 = p->out_f64;
+    b->sc = s.sc;
+    for (int i = 0; i < n; ++i) {
+        DetImage& d = b->img[i];
+        d.out = maps[i].edgels;
+        d.count = maps[i].count;
+        d.index = nullptr;
+        d.seg_base = p->m[i].seg_base;
+        d.nseg = (long long)maps[i].height * p->m[i].ntx;
+        d.tile_base = p->m[i].seg_tile_base;
+        d.cap = maps[i].capacity;
+        d.H = maps[i].height;
+        d.W = maps[i].width;
+    }
+    if (e == cudaSuccess) e = launch_finalize(*b, stream);
+    bool dense = false;
+    for (int i = 0; i < n; ++i) dense = dense || maps[i].TO_E || maps[i].TO_O;
+    if (dense && e == cudaSuccess) {
+        e = cudaMemsetAsync(s.win, 0xff, sizeof(int) * (size_t)px, stream);
+        const size_t es = p->out_f64 ? sizeof(double) : sizeof(float);
+        for (int i = 0; i < n && e == cudaSuccess; ++i) {
+            const size_t bytes = es * (size_t)maps[i].height * maps[i].width;
+            if (maps[i].TO_E) e = cudaMemsetAsync(maps[i].TO_E, 0, bytes, stream);
+            if (e == cudaSuccess && maps[i].TO_O) e = cudaMemsetAsync(maps[i].TO_O, 0, bytes, stream);
+        }
+        if (e == cudaSuccess)
+            e = cudaLaunchKernel((const void*)tc_dense<0>, dim3(p->n_seg_tiles), dim3(kSegTile), args, 0, stream);
+        if (e == cudaSuccess)
+            e = cudaLaunchKernel((const void*)tc_dense<1>, dim3(p->n_seg_tiles), dim3(kSegTile), args, 0, stream);
+    }
+    return e;
+}
+
+}  // namespace toed
