@@ -38,6 +38,7 @@ C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
     "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
+    "toed_subpix_to_correct_batch",
 ]
 
 
@@ -59,6 +60,22 @@ class toed_params(ctypes.Structure):
     _fields_ = [
         ("sigma", ctypes.c_float), ("radius", ctypes.c_int), ("threshold", ctypes.c_float),
         ("border", ctypes.c_int), ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class toed_edgemap(ctypes.Structure):
+    _fields_ = [
+        ("E", ctypes.c_void_p), ("theta", ctypes.c_void_p), ("height", ctypes.c_int),
+        ("width", ctypes.c_int), ("pitch", ctypes.c_int), ("dtype", ctypes.c_int),
+        ("edgels", ctypes.c_void_p), ("capacity", ctypes.c_int), ("count", ctypes.c_void_p),
+        ("TO_E", ctypes.c_void_p), ("TO_O", ctypes.c_void_p),
+    ]
+
+
+class toed_subpix_params(ctypes.Structure):
+    _fields_ = [
+        ("thresh", ctypes.c_float), ("sigma", ctypes.c_float), ("nbr_radius", ctypes.c_float),
+        ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
     ]
 
 
@@ -103,6 +120,8 @@ def lib():
         L.toed_profile_begin.argtypes = [vp]
         L.toed_profile_end.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ip)]
         L.toed_peak_probe.argtypes = [ip, ip, vp, ctypes.POINTER(ctypes.c_double)]
+        L.toed_subpix_to_correct_batch.argtypes = [vp, ctypes.POINTER(toed_edgemap), ip,
+                                                   ctypes.POINTER(toed_subpix_params), vp]
         for name in C_SYMBOLS:
             if name not in ("toed_status_string", "toed_last_cuda_error", "toed_params_default"):
                 getattr(L, name).restype = ip
@@ -264,6 +283,51 @@ class Detector:
 
     def detect(self, image, **kw):
         return self.detect_batch([image], **kw)[0]
+
+    def subpix_to_correct_batch(self, maps, thresh=0.2, sigma=2.0, nbr_radius=2.0, thetas=None,
+                                out_dtype=TOED_F32, precision=TOED_HYBRID, capacity=None, dense=True,
+                                stream=None):
+        """Subpixel TO correction of dense edge maps (2-D CUDA float32 /
+        float64 tensors), the reference's SubpixelTOCorrectionCPU<T>.
+        Returns dicts with ``edgels`` (N x 4: x, y, orientation, strength)
+        and, with ``dense``, ``TO_E`` / ``TO_O``."""
+        t = self.torch
+        dt = t.float64 if out_dtype == TOED_F64 else t.float32
+        dev = f"cuda:{self.device}"
+        arr, outs = [], []
+        for k, E in enumerate(maps):
+            if E.dim() != 2 or E.dtype not in (t.float32, t.float64) or E.stride(1) != 1:
+                raise ValueError("edge maps must be 2-D row-contiguous float32/float64 CUDA tensors")
+            th = None if thetas is None else thetas[k]
+            if th is not None and (th.dtype != E.dtype or th.stride() != E.stride() or th.shape != E.shape):
+                raise ValueError("orientation map must match the edge map's dtype, shape and strides")
+            h, w = E.shape
+            cap = int(capacity) if capacity is not None else h * w
+            o = {"edgels": t.empty((max(cap, 1), 4), dtype=dt, device=dev),
+                 "count": t.zeros(1, dtype=t.int32, device=dev), "capacity": cap}
+            if dense:
+                o["TO_E"] = t.empty((h, w), dtype=dt, device=dev)
+                o["TO_O"] = t.empty((h, w), dtype=dt, device=dev)
+            outs.append(o)
+            arr.append(toed_edgemap(E.data_ptr(), th.data_ptr() if th is not None else None, h, w,
+                                    E.stride(0), TOED_F64 if E.dtype == t.float64 else TOED_F32,
+                                    o["edgels"].data_ptr(), cap, o["count"].data_ptr(),
+                                    o["TO_E"].data_ptr() if dense else None,
+                                    o["TO_O"].data_ptr() if dense else None))
+        a = (toed_edgemap * len(arr))(*arr)
+        prm = toed_subpix_params(float(thresh), float(sigma), float(nbr_radius), int(out_dtype), int(precision))
+        s = stream if stream is not None else t.cuda.current_stream(self.device)
+        _check(lib().toed_subpix_to_correct_batch(self._ctx, a, len(arr), ctypes.byref(prm),
+                                                  ctypes.c_void_p(s.cuda_stream)), "toed_subpix_to_correct_batch")
+        s.synchronize()
+        res = []
+        for o in outs:
+            n = int(o["count"].item())
+            r = {"count": n, "edgels": o["edgels"][:min(n, o["capacity"])]}
+            if dense:
+                r["TO_E"], r["TO_O"] = o["TO_E"], o["TO_O"]
+            res.append(r)
+        return res
 
 
 _DEFAULT = {}
