@@ -147,6 +147,27 @@ typedef struct toed_subpix_params {
 toed_status toed_subpix_to_correct_batch(toed_ctx* ctx, const toed_edgemap* maps, int n_maps,
                                          const toed_subpix_params* params, cudaStream_t stream);
 
+/* Allocation-free detection (no counterpart in the reference).
+ * For callers that cannot call cudaMalloc where they detect edges -- code
+ * whose device memory is owned by a pool or arena, real-time loops that
+ * forbid allocation after start-up, plug-in hosts that hand out only
+ * pre-sized buffers -- and therefore cannot use a toed_ctx, whose scratch
+ * grows on demand.  One image per call on the current device; the caller
+ * passes the image and the output buffers as for toed_detect.  The scratch
+ * is a fixed array compiled into the library (about 11 MB, reserved on every
+ * GPU that loads the library until the process exits).  The first call on a
+ * device looks up that array's device address, so make the first call
+ * before any stream capture.  Images above TOED_NOALLOC_MAX_DIM rows or
+ * columns or TOED_NOALLOC_MAX_PIXELS pixels, or a capacity above
+ * TOED_NOALLOC_MAX_EDGELS, return TOED_ERR_CAPACITY.  All calls share the
+ * array: calls that overlap on the GPU (other streams or host threads on the
+ * same device) race and must be serialised by the caller.  If the image has
+ * more edgels than `capacity`, count is exact and the list is incomplete. */
+#define TOED_NOALLOC_MAX_DIM 4096
+#define TOED_NOALLOC_MAX_PIXELS (2048LL * 2048LL)
+#define TOED_NOALLOC_MAX_EDGELS 262144
+toed_status toed_detect_noalloc(const toed_image* image, const toed_params* params, cudaStream_t stream);
+
 /* Measurement hooks (used by bench.py).
  * toed_profile_begin: from now on every detection on `ctx` records a pair of
  * CUDA events just before and just after its fused detection kernel, on the

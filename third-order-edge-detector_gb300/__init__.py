@@ -38,7 +38,7 @@ C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
     "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
-    "toed_subpix_to_correct_batch",
+    "toed_subpix_to_correct_batch", "toed_detect_noalloc",
 ]
 
 
@@ -122,6 +122,7 @@ def lib():
         L.toed_peak_probe.argtypes = [ip, ip, vp, ctypes.POINTER(ctypes.c_double)]
         L.toed_subpix_to_correct_batch.argtypes = [vp, ctypes.POINTER(toed_edgemap), ip,
                                                    ctypes.POINTER(toed_subpix_params), vp]
+        L.toed_detect_noalloc.argtypes = [ctypes.POINTER(toed_image), ctypes.POINTER(toed_params), vp]
         for name in C_SYMBOLS:
             if name not in ("toed_status_string", "toed_last_cuda_error", "toed_params_default"):
                 getattr(L, name).restype = ip

@@ -1,0 +1,170 @@
+// toed_noalloc.cu -- toed_detect_noalloc: single-image detection that makes
+// no device (or host heap) allocation of its own.
+//
+// Who needs it: callers that cannot call cudaMalloc at the point where they
+// detect edges -- code running under a memory pool or allocator that owns
+// all device memory (an inference server's arena, a real-time loop that
+// forbids allocation after start-up, a plug-in host that hands out only
+// pre-sized buffers) -- and so cannot create a toed_ctx, whose scratch grows
+// with cudaMalloc on demand.
+//
+// How: the scratch the fused kernel and the ordering pass need (work-queue
+// and flag words, staged edgel records, the row-segment table, tile sums)
+// lives in one file-scope __device__ array of fixed size, g_noalloc_scratch.
+// The module that holds it is loaded with the library, so every GPU that
+// loads the library keeps these bytes reserved until the process exits.
+// Host code may not use the array's name as a device address (on the host it
+// names a host-side stand-in), so the device address is looked up once per
+// device with cudaGetSymbolAddress, with that device current, by the first
+// call on that device; that first call should therefore happen before any
+// stream capture that includes this entry point.
+//
+// Limits: an image of at most TOED_NOALLOC_MAX_DIM rows and columns and
+// TOED_NOALLOC_MAX_PIXELS pixels, and an edgel capacity of at most
+// TOED_NOALLOC_MAX_EDGELS; larger requests return TOED_ERR_CAPACITY before
+// anything is launched.  All calls share the one array and it keeps the
+// previous call's contents: each call clears the queue / cursor / flag words
+// it needs at zero (an asynchronous memset on the caller's stream), and calls
+// whose work overlaps on the GPU (different streams, or different host
+// threads on the same device) race on the array and corrupt each other's
+// results -- serialise them.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+
+#include "toed_common.cuh"
+#include "toed_internal.h"
+
+namespace toed {
+void make_taps(double sigma, int r, TapBlock* tb);
+
+namespace {
+
+constexpr long long kNaMaxPixels = TOED_NOALLOC_MAX_PIXELS;
+constexpr int kNaMaxDim = TOED_NOALLOC_MAX_DIM;
+constexpr long long kNaMaxEdgels = TOED_NOALLOC_MAX_EDGELS;
+// segments 2H x ceil(W/30) <= pixels/15 + 2H, padded to whole ordering tiles
+constexpr long long kNaMaxTiles = (kNaMaxPixels / 15 + 2LL * kNaMaxDim) / kSegTile + 2;
+constexpr long long kNaMaxSegs = kNaMaxTiles * kSegTile;
+
+constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
+constexpr size_t kOffWords = 0;
+constexpr size_t kOffStaging = align256(kOffWords + 4 * sizeof(int));
+constexpr size_t kOffIdx = align256(kOffStaging + sizeof(double4_32a) * kNaMaxEdgels);
+constexpr size_t kOffSeg = align256(kOffIdx + sizeof(int) * kNaMaxEdgels);
+constexpr size_t kOffTiles = align256(kOffSeg + sizeof(int2) * kNaMaxSegs);
+constexpr size_t kOffBase = align256(kOffTiles + sizeof(int) * kNaMaxTiles);
+constexpr size_t kScratchBytes = align256(kOffBase + sizeof(long long));
+
+// The fixed scratch (see the file comment): about 11 MB per device.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_mu;
+unsigned char* g_dev_scratch[kMaxDevices] = {};
+
+// Device address of g_noalloc_scratch on `dev` (current), looked up once.
+cudaError_t scratch_address(int dev, unsigned char** out)
+{
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_dev_scratch[dev]) {
+        void* ptr = nullptr;
+        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        if (e != cudaSuccess) return e;
+        g_dev_scratch[dev] = static_cast<unsigned char*>(ptr);
+    }
+    *out = g_dev_scratch[dev];
+    return cudaSuccess;
+}
+
+}  // namespace
+}  // namespace toed
+
+using namespace toed;
+
+extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_params* prm, cudaStream_t stream)
+{
+    if (!im || !prm || !im->pixels || !im->edgels || !im->count) return TOED_ERR_INVALID_ARG;
+    if (im->height <= 0 || im->width <= 0 || im->pitch < im->width || im->capacity < 0) return TOED_ERR_INVALID_ARG;
+    if (im->dtype != TOED_U8 && im->dtype != TOED_F32) return TOED_ERR_UNSUPPORTED;
+    if ((reinterpret_cast<uintptr_t>(im->edgels) & 15u) != 0) return TOED_ERR_INVALID_ARG;
+    if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma) || !std::isfinite(prm->threshold) || prm->border < 1)
+        return TOED_ERR_INVALID_ARG;
+    if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
+    if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
+    // the fixed scratch bounds the image and the edgel capacity
+    if (im->height > kNaMaxDim || im->width > kNaMaxDim || (long long)im->height * im->width > kNaMaxPixels ||
+        im->capacity > kNaMaxEdgels)
+        return TOED_ERR_CAPACITY;
+    const int r = prm->radius > 0 ? prm->radius : (int)std::ceil(4.0 * (double)prm->sigma);
+    if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
+    const DetectEntry ent = detect_entry(r, prm->precision != TOED_FP32);
+    if (!ent.func) return TOED_ERR_UNSUPPORTED;
+
+    int dev = 0, sms = 0, bps = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TOED_ERR_CUDA;
+    unsigned char* base = nullptr;
+    if (scratch_address(dev, &base) != cudaSuccess) return TOED_ERR_CUDA;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return TOED_ERR_CUDA;
+    if (cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem) != cudaSuccess)
+        return TOED_ERR_CUDA;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ent.func, kThreads, ent.smem) != cudaSuccess || bps <= 0)
+        return TOED_ERR_CUDA;
+
+    BatchParams p;  // on the stack: no heap allocation either
+    std::memset(&p, 0, sizeof(p));
+    make_taps((double)prm->sigma, r, &p.taps);
+    p.thr = prm->threshold;
+    p.border = prm->border;
+    p.n_img = 1;
+    p.out_f64 = prm->out_dtype == TOED_F64;
+    p.radius = r;
+    // strip height: the tallest of 254 / 126 / 62 / 30 / 14 rows that still
+    // gives every resident CTA a few strips
+    const int nsc = (im->width + kInner - 1) / kInner;
+    const long long resident = (long long)bps * sms;
+    int S = kStepRows - 2;
+    for (int st = 16; st >= 1; st /= 2) {
+        const int s = st * kStepRows - 2;
+        if ((long long)nsc * ((im->height + s - 1) / s) >= 4 * resident) {
+            S = s;
+            break;
+        }
+    }
+    p.S = S;
+    DetImage& d = p.img[0];
+    d.src = im->pixels;
+    d.pitch = im->pitch;
+    d.out = im->edgels;
+    d.count = im->count;
+    d.index = im->grid_index;
+    d.H = im->height;
+    d.W = im->width;
+    d.dtype = im->dtype;
+    d.cap = im->capacity;
+    d.nsc = nsc;
+    d.nsr = (im->height + S - 1) / S;
+    d.unit_base = 0;
+    d.tile_base = 0;
+    d.seg_base = 0;
+    d.nseg = 2LL * im->height * nsc;
+    p.n_units = d.nsc * d.nsr;
+    p.n_tiles = (int)((d.nseg + kSegTile - 1) / kSegTile);
+    p.sc.words = reinterpret_cast<int*>(base + kOffWords);
+    p.sc.staging = reinterpret_cast<double4_32a*>(base + kOffStaging);
+    p.sc.staging_idx = reinterpret_cast<int*>(base + kOffIdx);
+    p.sc.staging_cap = im->capacity > 0 ? im->capacity : 1;
+    p.sc.seg = reinterpret_cast<int2*>(base + kOffSeg);
+    p.sc.tile_sum = reinterpret_cast<int*>(base + kOffTiles);
+    p.sc.img_base = reinterpret_cast<long long*>(base + kOffBase);
+
+    // queue, staging cursor and flags start at zero on every call
+    if (cudaMemsetAsync(p.sc.words, 0, 3 * sizeof(int), stream) != cudaSuccess) return TOED_ERR_CUDA;
+    const int grid = (int)std::min<long long>(p.n_units, resident);
+    void* args[] = {&p};
+    if (cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream) != cudaSuccess)
+        return TOED_ERR_CUDA;
+    if (launch_finalize(p, stream) != cudaSuccess) return TOED_ERR_CUDA;
+    return TOED_OK;
+}
