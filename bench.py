@@ -88,7 +88,7 @@ class ClockSampler:
         try:
             self.f = tempfile.TemporaryFile(mode="w+")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                          "--format=csv,noheader,nounits", "-lms", "50"],
                                          stdout=self.f, stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -210,6 +210,131 @@ def run_reference(args, ws, rank):
     print(json.dumps(line), flush=True)
 
 
+def _gen_shapes(args):
+    H, W, seed, dtype, ell = args
+    import importlib.util
+    p = os.path.join(ROOT, "third-order-edge-detector_gb300", "synth.py")
+    spec = importlib.util.spec_from_file_location("toed_bench_synth", p)
+    m = importlib.util.module_from_spec(spec)
+    sys.modules[spec.name] = m
+    spec.loader.exec_module(m)
+    if dtype == "ridge":
+        return m.ridge_map(H, W, seed=seed)
+    return m.shapes_image(H, W, seed=seed, dtype=np.uint8 if dtype == "u8" else np.float32,
+                          ellipses_only=ell).image
+
+
+def make_side_workloads():
+    """Inputs of the other configurations (spawn pool, before CUDA):
+    752x480 uint8; 1920x1080 and 3840x2160 float32; 16 x 512^2 float32
+    ellipses; 8 x 2048^2 ridge maps."""
+    jobs = [(480, 752, 1, "u8", False), (1080, 1920, 2, "f32", False), (2160, 3840, 2, "f32", False)]
+    jobs += [(512, 512, 4000 + k, "f32", True) for k in range(16)]
+    jobs += [(2048, 2048, 5000 + k, "ridge", False) for k in range(8)]
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
+        out = pool.map(_gen_shapes, jobs)
+    return {"c1": out[0], "c2_1080": out[1], "c2_2160": out[2], "c4": out[3:19], "c5": out[19:27]}
+
+
+def _time_ms(fn, reps, stream):
+    import torch
+    for _ in range(3):
+        fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(reps):
+        fn()
+    e1.record(stream)
+    e1.synchronize()
+    return e0.elapsed_time(e1) / reps
+
+
+def side_measurements(toed, det, images, side, stream):
+    """Timings and precision of the other configurations (reported next to
+    the headline line; none of them feeds ``value``)."""
+    import torch
+    import oracle
+    oracle.build()
+    out = {}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    # -- config 1 and the plain single-image form --------------------------
+    c1 = torch.as_tensor(side["c1"]).to(dev)
+    o1 = det.alloc_outputs([c1.shape], None)
+    for sg in (1.0, 2.0):
+        p1 = toed.make_params(sg)
+        ms = _time_ms(lambda: det.detect_into([c1], o1, p1, stream), 20, stream)
+        out[f"single_752x480_u8_sigma{sg:g}_mpx_s"] = round(c1.numel() / (ms * 1e-3) / 1e6, 1)
+    d_imgs = [torch.as_tensor(im).to(dev) for im in images]
+    outs = det.alloc_outputs([im.shape for im in images], None)
+    prm = toed.make_params(SIGMA, 0, THRESH)
+    seq = _time_ms(lambda: [det.detect_into([d], [o], prm, stream) for d, o in zip(d_imgs, outs)], 3, stream)
+    npx = sum(im.size for im in images)
+    out["batch_as_64_sequential_launches_mpx_s"] = round(npx / (seq * 1e-3) / 1e6, 1)
+    # the reference's dense two-kernel form rebuilt (toed_convolve_planes + toed_nms_planes), FP32, per image
+    import ctypes
+    L = toed.lib()
+
+    planes = [torch.empty((6, 2 * d.shape[0], 2 * d.shape[1]), dtype=torch.float32, device=dev) for d in d_imgs]
+
+    def dense_form():
+        for d, P in zip(d_imgs, planes):
+            H, W = d.shape
+            L.toed_convolve_planes(ctypes.c_void_p(d.data_ptr()), toed.TOED_F32, H, W, W, float(SIGMA), 0, None,
+                                   toed.TOED_F32, *[ctypes.c_void_p(P[k].data_ptr()) for k in range(4)],
+                                   ctypes.c_void_p(stream.cuda_stream))
+            L.toed_nms_planes(toed.TOED_F32, 2 * H, 2 * W, *[ctypes.c_void_p(P[k].data_ptr()) for k in range(3)],
+                              float(THRESH), 10, ctypes.c_void_p(P[4].data_ptr()), ctypes.c_void_p(P[5].data_ptr()),
+                              ctypes.c_void_p(stream.cuda_stream))
+    dms = _time_ms(dense_form, 2, stream)
+    out["dense_two_kernel_form_mpx_s"] = round(npx / (dms * 1e-3) / 1e6, 1)
+    del planes
+    # -- config 4: forward vs forward + backward (16 x 512^2, sigma learnable)
+    c4 = [torch.as_tensor(im).to(dev) for im in side["c4"]]
+    o4 = det.alloc_outputs([im.shape for im in c4], None)
+    fwd = _time_ms(lambda: det.detect_into(c4, o4, prm, stream), 10, stream)
+    res = det.detect_batch(c4, sigma=SIGMA)
+    gout = [torch.randn_like(r["edgels"]) for r in res]
+    idx = [r["index"] for r in res]
+    bwd = _time_ms(lambda: det.backward_batch(c4, idx, gout, sigma=SIGMA), 10, stream)
+    out["fwd_bwd_16x512"] = {"fwd_ms": round(fwd, 4), "bwd_ms": round(bwd, 4),
+                             "fwd_plus_bwd_over_fwd": round((fwd + bwd) / fwd, 3),
+                             "fwd_mpx_s": round(16 * 512 * 512 / (fwd * 1e-3) / 1e6, 1),
+                             "fwd_bwd_mpx_s": round(16 * 512 * 512 / ((fwd + bwd) * 1e-3) / 1e6, 1),
+                             "edgels": int(sum(r["count"] for r in res))}
+    # -- config 5: subpixel TO correction, 8 x 2048^2 ridge maps -----------
+    c5 = [torch.as_tensor(E).to(dev) for E in side["c5"]]
+    tms = _time_ms(lambda: det.subpix_to_correct_batch(c5, thresh=0.1, sigma=2.0, nbr_radius=2.0, dense=True), 5, stream)
+    out["subpix_8x2048"] = {"ms": round(tms, 3), "mpx_s": round(8 * 2048 * 2048 / (tms * 1e-3) / 1e6, 1)}
+    E0 = side["c5"][0].astype(np.float64)
+    t0 = time.perf_counter()
+    oracle.subpix_to_correct(E0, 0.1, 2.0, 2.0, nthreads=os.cpu_count())
+    cpu_s = time.perf_counter() - t0
+    out["subpix_8x2048"]["cpu_port_mpx_s_one_map"] = round(E0.size / cpu_s / 1e6, 2)
+    # -- config 2: precision vs the FP64 oracle ---------------------------
+    prec = {}
+    for name in ("c2_1080", "c2_2160"):
+        im = side[name]
+        for sg in (1.0, 2.0):
+            ref = oracle.detect(im.astype(np.float64), sg, nthreads=os.cpu_count())
+            row = {}
+            for mode, pr in (("fp32_conv+fp64_epilogue", toed.TOED_HYBRID), ("all_fp32", toed.TOED_FP32)):
+                r = det.detect(torch.as_tensor(im).to(dev), sigma=sg, out_dtype=toed.TOED_F64, precision=pr)
+                gi = r["index"].cpu().numpy().astype(np.int64)
+                ge = r["edgels"].cpu().numpy()
+                common, ia, ib = np.intersect1d(ref["index"], gi, return_indices=True)
+                pe = np.hypot(*(ref["edges"][ia, :2] - ge[ib, :2]).T)
+                oe = np.abs(np.angle(np.exp(1j * (ref["edges"][ia, 2] - ge[ib, 2]))))
+                row[mode] = {"agreement": round(len(common) / max(len(gi), len(ref["index"])), 6),
+                             "pos_err_max_px": float(f"{pe.max():.3g}"), "pos_err_p99_px": float(f"{np.quantile(pe, .99):.3g}"),
+                             "ori_err_max_rad": float(f"{np.nanmax(oe):.3g}"),
+                             "ori_err_p99_rad": float(f"{np.nanquantile(oe, .99):.3g}")}
+            row["n_ref"] = int(len(ref["index"]))
+            prec[f"{name[3:]}_sigma{sg:g}"] = row
+    out["precision_vs_fp64_oracle"] = prec
+    return out
+
+
 def flops_per_px(r: int) -> int:
     """Dense FP32 work of the fused kernel per original pixel: row pass
     4(2r+1)+8+4(2r+3) FMA + column pass of Ix, Iy at four sub-grids
@@ -221,6 +346,7 @@ def flops_per_px(r: int) -> int:
 def run_ours(args, ws, rank, local):
     seed0 = SEED0 + N_IMAGES * rank
     images = make_batch(seed0)  # spawn pool, before the first CUDA call
+    side = make_side_workloads() if (rank == 0 and not args.no_side) else None
     import torch
     toed = _pkg()
     if not os.path.exists(toed.LIB_PATH):
@@ -343,6 +469,8 @@ def run_ours(args, ws, rank, local):
         "edgels_per_px": round(rho, 5),
         "clocks": clk,
     }
+    if side is not None:
+        line["other_configs"] = side_measurements(toed, det, images, side, stream)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
         v, px, n, dt = cpu_oracle_rate(images, args.cpu_seconds, threads)
@@ -356,11 +484,12 @@ def run_ours(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--steps", type=int, default=100)
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-side", action="store_true", help="skip the other configurations' measurements")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

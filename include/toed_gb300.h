@@ -66,6 +66,7 @@ typedef enum toed_precision {
 /* Device flags (toed_device_flags) */
 #define TOED_FLAG_OVER_CAPACITY 0x1 /* some image found more edgels than its capacity */
 #define TOED_FLAG_STAGING_FULL 0x2  /* the context staging buffer overflowed */
+#define TOED_FLAG_TIMEOUT 0x4       /* a bounded wait for an input copy gave up (results incomplete) */
 
 typedef struct toed_ctx toed_ctx;
 
@@ -117,6 +118,24 @@ toed_status toed_detect_batch(toed_ctx* ctx, const toed_image* images, int n_ima
 /* Synchronises `stream` and returns the OR of the device flags of the last
  * detection on this context (0 = all images fit their capacities). */
 toed_status toed_device_flags(toed_ctx* ctx, cudaStream_t stream, int* flags);
+
+/* Adjoint of toed_detect with the selection frozen (no reference counterpart:
+ * the reference has no gradients).  For every edgel the forward emitted
+ * (identified by the grid_index it wrote), given dL/d[x, y, orientation,
+ * strength], writes dL/dpixel for the whole image and accumulates dL/dsigma.
+ * The NMS decisions (which 2x-grid points are edgels, and each one's sector)
+ * are those of the forward and are not differentiated. */
+typedef struct toed_grad_image {
+    const void* pixels;       /* the forward's input (device) */
+    int height, width, pitch, dtype;
+    int n_edgels;             /* edgels of the forward (its count, at most its capacity) */
+    const int* grid_index;    /* the forward's grid_index output (device), ascending */
+    const void* grad_edgels;  /* n_edgels x 4 cotangents (device), params->out_dtype */
+    float* grad_pixels;       /* height x width float32 (device, row pitch = width): overwritten */
+} toed_grad_image;
+
+toed_status toed_backward_batch(toed_ctx* ctx, const toed_grad_image* items, int n_images,
+                                const toed_params* params, double* grad_sigma, cudaStream_t stream);
 
 /* Subpixel third-order correction of dense edge maps (the reference's
  * SubpixelTOCorrectionCPU<T>, subpix_TO_correction/subpix_to_correction.cpp,

@@ -189,3 +189,20 @@ def test_reference_class_mirror(toed, oracle, synth, tmp_path):
     assert np.abs(buf[:n, :2] - ref["edges"][:, :2]).max() < 1e-3
     assert os.path.exists(os.path.join(str(tmp_path), "data_final_output_gpu.txt"))
     assert d.time_conv > 0
+
+
+@pytest.mark.parametrize("dtype,W", [(np.float32, 97), (np.uint8, 101)])
+def test_tma_and_plain_loads_identical(detector, synth, dtype, W):
+    """Rows are staged by TMA when the image base and pitch are 16-byte
+    aligned and by plain loads otherwise; both must give the same edgels."""
+    t = _torch()
+    img = synth.shapes_image(130, W, seed=W, n_shapes=6, radius_range=(8, 40), scale_to_base=False,
+                             dtype=dtype).image
+    plain = t.as_tensor(img).cuda()                       # pitch W: not 16-byte aligned
+    padw = (W * img.itemsize + 15) // 16 * 16 // img.itemsize
+    buf = t.zeros((130, padw), dtype=plain.dtype, device="cuda")
+    buf[:, :W] = plain                                    # pitch padded: TMA path
+    a = detector.detect(plain, sigma=1.5)
+    b = detector.detect(buf[:, :W], sigma=1.5)
+    assert a["count"] > 20
+    assert t.equal(a["edgels"], b["edgels"]) and t.equal(a["index"], b["index"])

@@ -38,7 +38,7 @@ C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
     "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
-    "toed_subpix_to_correct_batch", "toed_detect_noalloc",
+    "toed_subpix_to_correct_batch", "toed_detect_noalloc", "toed_backward_batch",
 ]
 
 
@@ -60,6 +60,14 @@ class toed_params(ctypes.Structure):
     _fields_ = [
         ("sigma", ctypes.c_float), ("radius", ctypes.c_int), ("threshold", ctypes.c_float),
         ("border", ctypes.c_int), ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class toed_grad_image(ctypes.Structure):
+    _fields_ = [
+        ("pixels", ctypes.c_void_p), ("height", ctypes.c_int), ("width", ctypes.c_int),
+        ("pitch", ctypes.c_int), ("dtype", ctypes.c_int), ("n_edgels", ctypes.c_int),
+        ("grid_index", ctypes.c_void_p), ("grad_edgels", ctypes.c_void_p), ("grad_pixels", ctypes.c_void_p),
     ]
 
 
@@ -123,6 +131,8 @@ def lib():
         L.toed_subpix_to_correct_batch.argtypes = [vp, ctypes.POINTER(toed_edgemap), ip,
                                                    ctypes.POINTER(toed_subpix_params), vp]
         L.toed_detect_noalloc.argtypes = [ctypes.POINTER(toed_image), ctypes.POINTER(toed_params), vp]
+        L.toed_backward_batch.argtypes = [vp, ctypes.POINTER(toed_grad_image), ip, ctypes.POINTER(toed_params),
+                                          vp, vp]
         for name in C_SYMBOLS:
             if name not in ("toed_status_string", "toed_last_cuda_error", "toed_params_default"):
                 getattr(L, name).restype = ip
@@ -285,6 +295,37 @@ class Detector:
     def detect(self, image, **kw):
         return self.detect_batch([image], **kw)[0]
 
+    def backward_batch(self, images, indices, grad_edgels, sigma=2.0, radius=0, out_dtype=TOED_F32,
+                       stream=None):
+        """Adjoint of detect_batch with the selection frozen: given the
+        forward's images, its per-image grid indices and dL/d(edgels)
+        (N x 4 each), returns (dL/dimages as float32 tensors, dL/dsigma)."""
+        t = self.torch
+        dev = f"cuda:{self.device}"
+        items, grads = [], []
+        gdt = t.float64 if out_dtype == TOED_F64 else t.float32
+        keep = []
+        for im, idx, ge in zip(images, indices, grad_edgels):
+            if im.stride(1) != 1:
+                raise ValueError("image rows must be contiguous")
+            H, W = im.shape
+            gi = idx.to(device=dev, dtype=t.int32).contiguous()
+            go = ge.to(device=dev, dtype=gdt).contiguous()
+            gp = t.empty((H, W), dtype=t.float32, device=dev)
+            keep += [gi, go]
+            grads.append(gp)
+            items.append(toed_grad_image(im.data_ptr(), H, W, im.stride(0),
+                                         TOED_U8 if im.dtype == t.uint8 else TOED_F32, int(gi.numel()),
+                                         gi.data_ptr() if gi.numel() else None,
+                                         go.data_ptr() if go.numel() else None, gp.data_ptr()))
+        arr = (toed_grad_image * len(items))(*items)
+        gs = t.zeros(1, dtype=t.float64, device=dev)
+        p = make_params(sigma, radius, 2.0, 10, out_dtype)
+        s = stream if stream is not None else t.cuda.current_stream(self.device)
+        _check(lib().toed_backward_batch(self._ctx, arr, len(items), ctypes.byref(p), ctypes.c_void_p(gs.data_ptr()),
+                                         ctypes.c_void_p(s.cuda_stream)), "toed_backward_batch")
+        return grads, gs
+
     def subpix_to_correct_batch(self, maps, thresh=0.2, sigma=2.0, nbr_radius=2.0, thetas=None,
                                 out_dtype=TOED_F32, precision=TOED_HYBRID, capacity=None, dense=True,
                                 stream=None):
@@ -438,3 +479,45 @@ class ThirdOrderEdgeDetectionGPU:
                 for row in edges:
                     f.write("".join(f"{v:.10g}\t" for v in row) + "\n")
         return n
+
+
+def differentiable_detect(images, sigma, threshold=2.0, radius=0, detector=None):
+    """Edgels of a batch as a differentiable function of the pixels and sigma.
+
+    ``images``: (B, H, W) float32 CUDA tensor; ``sigma``: 0-d tensor (may
+    require grad).  Returns (edgels (N, 4) [x, y, orientation, strength],
+    counts (B,), grid_index (N,)) with the edgels of all images
+    concatenated.  The backward is the hand-written adjoint
+    (toed_backward_batch) with the selection held fixed."""
+    import torch
+
+    det = detector or _default_detector(images.device.index or 0)
+
+    class _Fn(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, imgs, sig):
+            s = float(sig.detach().cpu())
+            res = det.detect_batch(list(imgs), sigma=s, threshold=threshold, radius=radius, index=True)
+            counts = torch.tensor([r["count"] for r in res], dtype=torch.int64)
+            edg = torch.cat([r["edgels"] for r in res])
+            idx = torch.cat([r["index"] for r in res])
+            ctx.save_for_backward(imgs)
+            ctx.sigma = s
+            ctx.sig_meta = (sig.dtype, sig.device)
+            ctx.idx = [r["index"] for r in res]
+            ctx.counts = counts.tolist()
+            ctx.mark_non_differentiable(idx, counts)
+            return edg, idx, counts
+
+        @staticmethod
+        def backward(ctx, g_edg, g_idx, g_cnt):
+            (imgs,) = ctx.saved_tensors
+            splits = torch.split(g_edg.contiguous(), ctx.counts)
+            grads, gs = det.backward_batch(list(imgs), ctx.idx, list(splits), sigma=ctx.sigma, radius=radius)
+            gi = torch.stack(grads) if ctx.needs_input_grad[0] else None
+            gsig = gs.reshape(()).to(dtype=ctx.sig_meta[0], device=ctx.sig_meta[1]) if ctx.needs_input_grad[1] else None
+            return gi, gsig
+
+    sig = sigma if isinstance(sigma, torch.Tensor) else torch.tensor(float(sigma))
+    edg, idx, counts = _Fn.apply(images, sig)
+    return edg, counts, idx

@@ -10,6 +10,8 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "toed_common.cuh"
 #include "toed_internal.h"
 
@@ -66,6 +68,48 @@ void make_taps(double sigma, int r, TapBlock* tb)
     }
 }
 
+static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
+{
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+    });
+    return fn;
+}
+
+void encode_rows_map(CUtensorMap* m, DetImage& d, int r)
+{
+    d.tma = 0;
+    d.tma_align = 1;
+    d.tma_boxw = 0;
+    const int esz = (d.dtype == TOED_U8) ? 1 : 4;
+    const int align = 16 / esz;
+    const int nin = kExt + 2 * r + 2;
+    const int boxw = (nin + align - 1 + align - 1) / align * align;
+    auto fn = encode_fn();
+    if (!fn || (reinterpret_cast<uintptr_t>(d.src) & 15u) != 0 || ((long long)d.pitch * esz) % 16 != 0 ||
+        boxw * esz > 256)
+        return;
+    const cuuint64_t dims[2] = {(cuuint64_t)d.W, (cuuint64_t)d.H};
+    const cuuint64_t strides[1] = {(cuuint64_t)d.pitch * esz};
+    const cuuint32_t box[2] = {(cuuint32_t)boxw, (cuuint32_t)kStepRows};
+    const cuuint32_t estr[2] = {1, 1};
+    const CUresult res = fn(m, esz == 1 ? CU_TENSOR_MAP_DATA_TYPE_UINT8 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2,
+                            const_cast<void*>(d.src), dims, strides, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                            CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (res != CUDA_SUCCESS) return;
+    d.tma = 1;
+    d.tma_align = align;
+    d.tma_boxw = boxw;
+}
+
 }  // namespace toed
 
 using namespace toed;
@@ -102,6 +146,8 @@ struct toed_ctx {
     long long img_count_cap = 0;
     unsigned char* keep = nullptr;
     long long keep_cap = 0;
+    float* cot = nullptr;
+    long long cot_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
@@ -179,6 +225,7 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->win);
     cudaFree(c->img_count);
     cudaFree(c->keep);
+    cudaFree(c->cot);
     cudaSetDevice(prev);
     delete c;
     return TOED_OK;
@@ -309,6 +356,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.unit_base = (int)units;
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
+        encode_rows_map(&p->tmap[i], d, r);
         const long long nseg = 2LL * im.height * d.nsc;
         d.nseg = nseg;
         units += (long long)d.nsc * d.nsr;
@@ -481,6 +529,49 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
             cudaError_t e = subpix_launch(mp, cn, prm, r, s, stream);
             if (e != cudaSuccess) {
                 g_last_cuda_error = std::string("subpix_launch: ") + cudaGetErrorString(e);
+                st = TOED_ERR_CUDA;
+            }
+        }
+    }
+    if (prev != c->device) cudaSetDevice(prev);
+    return st;
+}
+
+extern "C" toed_status toed_backward_batch(toed_ctx* c, const toed_grad_image* items, int n, const toed_params* prm,
+                                           double* grad_sigma, cudaStream_t stream)
+{
+    if (!c || !items || n <= 0 || !prm || !grad_sigma) return TOED_ERR_INVALID_ARG;
+    if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma)) return TOED_ERR_INVALID_ARG;
+    if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
+    const int r = radius_of(prm);
+    if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
+    long long tot = 0;
+    for (int i = 0; i < n; ++i) {
+        const toed_grad_image& g = items[i];
+        if (!g.pixels || !g.grad_pixels || g.height <= 0 || g.width <= 0 || g.pitch < g.width || g.n_edgels < 0)
+            return TOED_ERR_INVALID_ARG;
+        if (g.n_edgels > 0 && (!g.grid_index || !g.grad_edgels)) return TOED_ERR_INVALID_ARG;
+        if (g.dtype != TOED_U8 && g.dtype != TOED_F32) return TOED_ERR_UNSUPPORTED;
+        tot += g.n_edgels;
+    }
+    if (tot >= (1LL << 31)) return TOED_ERR_UNSUPPORTED;
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    if (prev != c->device) TOED_CU(cudaSetDevice(c->device));
+    toed_status st = TOED_OK;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        st = grow(&c->cot, &c->cot_cap, std::max(1LL, tot * 18), stream);
+        if (st == TOED_OK) {
+            cudaError_t e = cudaMemsetAsync(grad_sigma, 0, sizeof(double), stream);
+            for (int i0 = 0; i0 < n && e == cudaSuccess; i0 += kBatchMax) {
+                const int cn = std::min(kBatchMax, n - i0);
+                long long off = 0;
+                for (int i = 0; i < i0; ++i) off += items[i].n_edgels;
+                e = backward_launch(items + i0, cn, prm, r, c->cot + off * 18, grad_sigma, stream);
+            }
+            if (e != cudaSuccess) {
+                g_last_cuda_error = std::string("backward: ") + cudaGetErrorString(e);
                 st = TOED_ERR_CUDA;
             }
         }

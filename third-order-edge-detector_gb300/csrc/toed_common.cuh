@@ -10,6 +10,7 @@
 //                  and the ordering pass' tile sums.
 #pragma once
 #include <cstdint>
+#include <cuda.h>  // CUtensorMap (the type only; encoding goes through the runtime's driver entry point)
 #include <cuda_runtime.h>
 
 #include "../../include/toed_gb300.h"
@@ -47,6 +48,9 @@ struct DetImage {
     int nsc, nsr;        // strip columns / strip rows
     int unit_base;       // first work unit
     int tile_base;       // first ordering tile
+    int tma;             // 1: rows arrive by TMA through BatchParams::tmap[k]; 0: plain loads
+    int tma_align;       // element alignment of a TMA box's x coordinate (16 bytes)
+    int tma_boxw;        // box width in elements (the halo row plus the alignment shift)
 };
 
 struct Scratch {
@@ -60,6 +64,7 @@ struct Scratch {
 };
 
 struct BatchParams {
+    CUtensorMap tmap[kBatchMax];  // per image: 2-D map, box (tma_boxw x kStepRows), OOB zero fill
     TapBlock taps;
     float thr;
     int border;

@@ -42,14 +42,25 @@ struct Cfg {
     static constexpr int MS = 2 * B + 2;            // 2x-grid rows held for NMS
     static constexpr int NMS_ROWS = 2 * B;          // 2x-grid rows decided per step
     static constexpr int MAXC = NMS_ROWS * 2 * kInner;
-    static constexpr size_t off_in = 0;
-    static constexpr size_t off_P = align_up(off_in + sizeof(float) * HS * NIN, 16);
+    static constexpr int RECW = 21;                 // words per deferred edgel record (odd: no bank conflicts)
+    // the input rows and the per-step point list are never live together
+    static constexpr size_t sz_in = sizeof(float) * HS * NIN;
+    static constexpr size_t sz_list = sizeof(unsigned) * MAXC;
+    static constexpr size_t sz_raw = kStepRows * 256;  // one TMA box: 16 rows x <= 256 bytes
+    static constexpr size_t off_raw = 0;
+    static constexpr size_t off_mbar = off_raw + sz_raw;
+    static constexpr size_t off_in = off_mbar + 16;
+    static constexpr size_t off_P = align_up(off_in + (sz_in > sz_list ? sz_in : sz_list), 16);
     static constexpr size_t off_mag = off_P + sizeof(float2) * 6 * HS * kExt;
     static constexpr size_t off_fxy = off_mag + sizeof(float) * MS * 64;
     static constexpr size_t off_tab = off_fxy + sizeof(float2) * MS * 64;
-    static constexpr size_t off_cand = off_tab + sizeof(float4) * 3 * NT;
-    static constexpr size_t off_misc = off_cand + sizeof(unsigned) * MAXC;
-    static constexpr size_t smem = off_misc + sizeof(int) * 96;
+    static constexpr size_t off_misc = off_tab + sizeof(float4) * 3 * NT;
+    static constexpr size_t off_rec = off_misc + sizeof(int) * 128;
+    // deferred-edgel ring: as many records as keep two CTAs per SM (<= 112 KB each)
+    static constexpr size_t budget = 112 * 1024;
+    static constexpr int NREC_FIT = off_rec < budget ? (int)((budget - off_rec) / (RECW * 4) / 32 * 32) : 0;
+    static constexpr int NREC = NREC_FIT > 256 ? 256 : (NREC_FIT < 64 ? 64 : NREC_FIT);
+    static constexpr size_t smem = off_rec + sizeof(float) * RECW * NREC;
 };
 
 __device__ __forceinline__ float sqrt_approx(float x)
@@ -67,6 +78,49 @@ __device__ __forceinline__ float fetch_px(const void* src, long long pitch, int 
     const long long o = (long long)y * pitch + x;
     if (dtype == TOED_U8) return (float)__ldg((const unsigned char*)src + o);
     return __ldg((const float*)src + o);
+}
+
+// ---------------------------------------------------------------------------
+// TMA staging of input rows (cp.async.bulk.tensor + mbarrier)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ uint32_t smem_addr(const void* p)
+{
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar)
+{
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+
+// Thread 0: one box of kStepRows rows at (x, y) of image map `tm` into `dst`.
+__device__ __forceinline__ void tma_load_rows(const CUtensorMap* tm, uint32_t dst, uint32_t bar, int x, int y,
+                                              uint32_t bytes)
+{
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes) : "memory");
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+            dst),
+        "l"(reinterpret_cast<uint64_t>(tm)), "r"(x), "r"(y), "r"(bar)
+        : "memory");
+}
+
+// Bounded wait for the mbarrier phase: gives up after ~2^20 polls (each poll
+// may suspend briefly) instead of hanging the SM.
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase)
+{
+    for (int i = 0; i < (1 << 20); ++i) {
+        uint32_t ok;
+        asm volatile(
+            "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+            : "=r"(ok)
+            : "r"(bar), "r"(phase)
+            : "memory");
+        if (ok) return true;
+    }
+    return false;
 }
 
 // ---------------------------------------------------------------------------
@@ -203,6 +257,88 @@ __device__ __forceinline__ NmsEval nms_eval(const float* __restrict__ sMag,
     return r;
 }
 
+// Per-edgel epilogue from a deferred record: peak fit (FP64 in HYB mode:
+// the cancellations in fm + fp - 2f and fp - fm) and the third-order
+// orientation (cpu_toed.cpp:227-232, FP64 in HYB mode), then the staged
+// output record (x, y, orientation, strength) at its reserved slot.
+template <bool HYB>
+__device__ __forceinline__ void finish_edgel(const float* __restrict__ rc, const Scratch& sc)
+{
+    const float gx = rc[0], gy = rc[1], mv = rc[2], nx = rc[3], ny = rc[4], sl = rc[5];
+    const float Map = rc[6], Mdp = rc[7], Mam = rc[8], Mdm = rc[9];
+    const float fxx = rc[10], fxy = rc[11], fyy = rc[12], fxxy = rc[13], fxyy = rc[14], fxxx = rc[15],
+                fyyy = rc[16];
+    const int Gr = __float_as_int(rc[17]), Gc = __float_as_int(rc[18]);
+    const int dst = __float_as_int(rc[19]), idx = __float_as_int(rc[20]);
+    double x, y;
+    float ori, str;
+    if (HYB) {
+        const double s1 = sl;
+        const double fp = (double)Map * (1.0 - s1) + (double)Mdp * s1;
+        const double fm = (double)Mam * (1.0 - s1) + (double)Mdm * s1;
+        const double num = fp - fm, den = fm + fp - 2.0 * (double)mv;
+        const double ss = (double)sqrtf(1.f + sl * sl);
+        const double rden = 1.0 / den;
+        const double sst = -0.5 * num * ss * rden;             // s* = -B / (2A)
+        const double maxf = (double)mv - 0.125 * num * num * rden;  // A s*^2 + B s* + C
+        x = ((double)Gc + sst * (double)nx - 1.0) * 0.5;       // (pos - 1) / 2, cpu_toed.cpp:516
+        y = ((double)Gr + sst * (double)ny - 1.0) * 0.5;
+        const float mf = (float)maxf;
+        str = sqrtf((mf * nx) * (mf * nx) + (mf * ny) * (mf * ny));
+        const double dfx = gx, dfy = gy, dxx = fxx, dxy = fxy, dyy = fyy;
+        const double tix = dfx * (2.0 * dxx * dxx + 2.0 * dxy * dxy) + dfy * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
+                           2.0 * dfx * dfy * (double)fxxy + dfy * dfy * (double)fxyy + dfx * dfx * (double)fxxx;
+        const double tiy = dfx * (2.0 * dxx * dxy + 2.0 * dyy * dxy) + dfy * (2.0 * dyy * dyy + 2.0 * dxy * dxy) +
+                           2.0 * dfx * dfy * (double)fxyy + dfx * dfx * (double)fxxy + dfy * dfy * (double)fyyy;
+        ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000) : atan2f((float)tix, (float)(-tiy));
+    } else {
+        const float fp = Map * (1.f - sl) + Mdp * sl;
+        const float fm = Mam * (1.f - sl) + Mdm * sl;
+        const float num = fp - fm, den = fm + fp - 2.f * mv;
+        const float ss = sqrtf(1.f + sl * sl);
+        const float sst = -0.5f * num * ss / den;
+        const float maxf = mv - 0.125f * num * num / den;
+        x = ((double)((float)Gc + sst * nx) - 1.0) * 0.5;
+        y = ((double)((float)Gr + sst * ny) - 1.0) * 0.5;
+        str = sqrtf((maxf * nx) * (maxf * nx) + (maxf * ny) * (maxf * ny));
+        const float tix = gx * (2.f * fxx * fxx + 2.f * fxy * fxy) + gy * (2.f * fxx * fxy + 2.f * fyy * fxy) +
+                          2.f * gx * gy * fxxy + gy * gy * fxyy + gx * gx * fxxx;
+        const float tiy = gx * (2.f * fxx * fxy + 2.f * fyy * fxy) + gy * (2.f * fyy * fyy + 2.f * fxy * fxy) +
+                          2.f * gx * gy * fxyy + gx * gx * fxxy + gy * gy * fyyy;
+        ori = (tix == 0.f && tiy == 0.f) ? __int_as_float(0x7fc00000) : atan2f(tix, -tiy);
+    }
+    if (dst < sc.staging_cap) {
+        sc.staging[dst] = make_double4_32a(x, y, (double)ori, (double)str);
+        sc.staging_idx[dst] = idx;
+    }
+}
+
+// Block-wide exclusive scan of one int per thread (256 threads); returns the
+// prefix and leaves the total in *tot.  Three barriers' worth of traffic on
+// sWarp[9].
+__device__ __forceinline__ int cta_excl_scan(int v, int* sWarp, int* tot)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) sWarp[wid] = incl;
+    __syncthreads();
+    int off = 0, t = 0;
+#pragma unroll
+    for (int w = 0; w < kThreads / 32; ++w) {
+        const int x = sWarp[w];
+        off += (w < wid) ? x : 0;
+        t += x;
+    }
+    *tot = t;
+    __syncthreads();
+    return off + incl - v;
+}
+
 template <int R, bool HYB>
 __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_constant__ BatchParams p)
 {
@@ -210,15 +346,21 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
     constexpr int B = C::B;
     extern __shared__ __align__(16) unsigned char smem[];
     float* sIn = reinterpret_cast<float*>(smem + C::off_in);
+    unsigned* sList = reinterpret_cast<unsigned*>(smem + C::off_in);  // aliases sIn (not live together)
     float2* sP = reinterpret_cast<float2*>(smem + C::off_P);
     float* sMag = reinterpret_cast<float*>(smem + C::off_mag);
     float2* sFxy = reinterpret_cast<float2*>(smem + C::off_fxy);
     float4* sTab = reinterpret_cast<float4*>(smem + C::off_tab);
-    unsigned* sCand = reinterpret_cast<unsigned*>(smem + C::off_cand);
     int* sMisc = reinterpret_cast<int*>(smem + C::off_misc);
-    int* sRowCnt = sMisc;        // [32]
+    float* sRec = reinterpret_cast<float*>(smem + C::off_rec);
+    int* sRowCnt = sMisc;        // [32] points above threshold per NMS row
     int* sRowOff = sMisc + 32;   // [32]
-    int* sScal = sMisc + 64;     // [0] unit, [1] staging base, [2] total K
+    int* sAccCnt = sMisc + 64;   // [32] accepted edgels per NMS row
+    int* sWarp = sMisc + 96;     // [8] scan scratch
+    int* sScal = sMisc + 112;    // [0] unit [1] staging base [2] list length [3] accepted
+    unsigned char* sRaw = smem + C::off_raw;  // TMA destination: one box of input rows
+    const uint32_t bar = smem_addr(smem + C::off_mbar);
+    uint32_t phase = 0;
 
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
     const TapBlock& tp = p.taps;
@@ -231,6 +373,8 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
         if (v == 0 && (k == 0 || k == C::NT - 1)) t = make_float4(0.f, 0.f, 0.f, 0.f);
         sTab[i] = t;
     }
+    int nrec = 0;  // deferred records in the ring (uniform across the CTA)
+    if (tid == 0) mbar_init(bar);
 
     for (;;) {
         __syncthreads();
@@ -252,6 +396,14 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
         const int row_lo = max(p.border, 2 * ys), row_hi = min(2 * H - p.border, 2 * ys + 2 * S_act);
         const int col_lo = p.border, col_hi = W2 - p.border;
         const long long seg0 = im.seg_base;
+        const int xin = x0 - R - 2;  // image column of sIn column 0
+        int x_al = xin, shift = 0;
+        if (im.tma) {
+            const int al = im.tma_align;
+            x_al = (xin >= 0) ? (xin / al) * al : -(((-xin) + al - 1) / al) * al;  // floor to the alignment
+            shift = xin - x_al;
+        }
+        const int rawpitch = im.tma_boxw * (dtype == TOED_U8 ? 1 : 4);  // bytes per staged row
 
         for (int i = tid; i < 2 * 64; i += kThreads) {
             sMag[i] = 0.f;
@@ -260,17 +412,57 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
 
         for (int s = 0; s < nsteps; ++s) {
             // ---- 1. input rows -> sIn (FP32, zero padded) -------------------
-            {
+            // slot h <-> ext row e = s*B - R - 2 + h <-> image row ys - 1 + e
+            if (im.tma) {
+                // rows arrive by TMA (out-of-image texels read as zero, the
+                // reference's zero padding); step s+1's box is requested as
+                // soon as step s has consumed the staging buffer
+                const int nch = (s == 0) ? (C::HS + B - 1) / B : 1;
+                for (int ch = 0; ch < nch; ++ch) {
+                    const int row0 = (s == 0) ? ys - R - 3 + ch * B : ys + s * B + R;
+                    // the first prologue box; later boxes are requested at the end of
+                    // the previous chunk, steady-state boxes at the end of the previous step
+                    if (s == 0 && ch == 0 && tid == 0)
+                        tma_load_rows(&p.tmap[k], smem_addr(sRaw), bar, x_al, row0, (uint32_t)(B * rawpitch));
+                    bool ok = mbar_wait(bar, phase);
+                    phase ^= 1u;
+                    if (__syncthreads_or(!ok)) {
+                        // give up on this CTA: flag it, drain the copy in flight, leave
+                        if (tid == 0) atomicOr(&p.sc.words[2], TOED_FLAG_TIMEOUT);
+                        mbar_wait(bar, phase ^ 1u);
+                        return;
+                    }
+                    const int nrows = min(B, C::HS - ((s == 0) ? ch * B : 0));
+                    const int dst0 = (s == 0) ? ch * B : 0;
+                    if (dtype == TOED_U8) {
+                        for (int i = tid; i < nrows * C::NIN; i += kThreads) {
+                            const int rr = i / C::NIN, cc = i - rr * C::NIN;
+                            sIn[(dst0 + rr) * C::NIN + cc] = (float)sRaw[rr * rawpitch + shift + cc];
+                        }
+                    } else {
+                        const float* rf = reinterpret_cast<const float*>(sRaw);
+                        for (int i = tid; i < nrows * C::NIN; i += kThreads) {
+                            const int rr = i / C::NIN, cc = i - rr * C::NIN;
+                            sIn[(dst0 + rr) * C::NIN + cc] = rf[rr * im.tma_boxw + shift + cc];
+                        }
+                    }
+                    __syncthreads();
+                    if (s == 0 && ch + 1 < nch && tid == 0)
+                        tma_load_rows(&p.tmap[k], smem_addr(sRaw), bar, x_al, row0 + B, (uint32_t)(B * rawpitch));
+                }
+                // the next step's rows (the last prologue chunk has been consumed)
+                if (s + 1 < nsteps && tid == 0)
+                    tma_load_rows(&p.tmap[k], smem_addr(sRaw), bar, x_al, ys + (s + 1) * B + R,
+                                  (uint32_t)(B * rawpitch));
+            } else {
                 const int nrows = (s == 0) ? C::HS : B;
-                // slot h <-> ext row e = s*B - R - 2 + h <-> image row ys - 1 + e
                 const int img_row0 = ys - 1 + s * B - R - 2 + ((s == 0) ? 0 : 2 * R + 3);
-                const int col0 = x0 - R - 2;
                 for (int i = tid; i < nrows * C::NIN; i += kThreads) {
                     const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                    sIn[i] = fetch_px(src, pitch, H, W, dtype, img_row0 + rr, col0 + cc);
+                    sIn[i] = fetch_px(src, pitch, H, W, dtype, img_row0 + rr, xin + cc);
                 }
+                __syncthreads();
             }
-            __syncthreads();
             // ---- 2. row pass ------------------------------------------------
             if (s == 0)
                 row_pass<R>(sIn, 0, C::HS, 0, sP, tp);
@@ -298,9 +490,10 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                     sFxy[m * 64 + c] = make_float2(fx[o], fy[o]);
                 }
             }
+            if (tid < 32) sAccCnt[tid] = 0;
             __syncthreads();
-            // ---- 4. NMS decisions on 2x-grid rows m = 1..2B (rho = 2sB-2+m) ---
-            // global 2x-grid row of slot m: Gr = 2*ys - 2 + (2sB - 2 + m)
+            // ---- 4a. points above the threshold, listed in row-major order ---
+            // NMS rows m = 1..2B (rho = 2sB-2+m), global 2x row Gr = gr_base + m
             const int gr_base = 2 * ys - 4 + 2 * s * B;
             const int gc_base = 2 * (x0 - 1);
             unsigned bal0[4], bal1[4];
@@ -309,12 +502,12 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                 const int m = 1 + wid + 8 * t;
                 const int Gr = gr_base + m;
                 const int c0 = 2 + 2 * lane;
-                const bool rowok = (Gr >= row_lo) && (Gr < row_hi) && (lane < kInner);
+                const int Gc = gc_base + c0;
                 bool k0 = false, k1 = false;
-                if (rowok) {
-                    const int Gc = gc_base + c0;
-                    if (Gc >= col_lo && Gc < col_hi) k0 = nms_eval(sMag, sFxy, m, c0, p.thr).cand;
-                    if (Gc + 1 >= col_lo && Gc + 1 < col_hi) k1 = nms_eval(sMag, sFxy, m, c0 + 1, p.thr).cand;
+                if (Gr >= row_lo && Gr < row_hi && lane < kInner) {
+                    const float2 mv = *reinterpret_cast<const float2*>(sMag + m * 64 + c0);
+                    k0 = (Gc >= col_lo && Gc < col_hi) && (mv.x > p.thr);  // cpu_toed.cpp:403
+                    k1 = (Gc + 1 >= col_lo && Gc + 1 < col_hi) && (mv.y > p.thr);
                 }
                 bal0[t] = __ballot_sync(0xffffffffu, k0);
                 bal1[t] = __ballot_sync(0xffffffffu, k1);
@@ -330,18 +523,7 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                     if (lane >= d) incl += y;
                 }
                 sRowOff[lane] = incl - cnt;
-                const int total = __shfl_sync(0xffffffffu, incl, 31);
-                int base = 0;
-                if (lane == 0 && total > 0) base = atomicAdd(&p.sc.words[1], total);
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (lane == 0) {
-                    sScal[1] = base;
-                    sScal[2] = total;
-                    if ((long long)base + total > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
-                }
-                const int Gr = gr_base + lane + 1;
-                if (Gr >= 2 * ys && Gr < 2 * ys + 2 * S_act)
-                    p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
+                if (lane == 31) sScal[2] = incl;
             }
             __syncthreads();
             {
@@ -352,109 +534,132 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                     const bool k0 = (bal0[t] >> lane) & 1u, k1 = (bal1[t] >> lane) & 1u;
                     const int pos = sRowOff[m - 1] + __popc(bal0[t] & lt) + __popc(bal1[t] & lt);
                     const unsigned c0 = 2 + 2 * lane;
-                    if (k0) sCand[pos] = ((unsigned)m << 8) | c0;
-                    if (k1) sCand[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
+                    if (k0) sList[pos] = ((unsigned)m << 8) | c0;
+                    if (k1) sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
                 }
             }
             __syncthreads();
-            // ---- 5. per-edgel derivatives, TO orientation, fit, staging ----
-            {
-                const int total = sScal[2], base = sScal[1];
-                for (int j = tid; j < total; j += kThreads) {
-                    const unsigned rec = sCand[j];
-                    const int m = rec >> 8, c = rec & 255;
-                    const int a = m & 1, xe = c >> 1, b = c & 1;
-                    const int xv = b ? 2 : (a ? 1 : 0);
-                    const int yv = a ? 2 : (b ? 1 : 0);
-                    const float2* Pp = sP + xv * C::HS * kExt + xe;
-                    const float2* Qp = sP + (3 + xv) * C::HS * kExt + xe;
-                    const float4* tab = sTab + yv * C::NT;
-                    float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
-                    const int h0 = m >> 1;
+            // ---- 4b. NMS on the list with full warps; survivors compacted in
+            // place, order kept (their rank never exceeds their list position)
+            const int LA = sScal[2];
+            int nacc = 0;
+            for (int r0 = 0; r0 < LA; r0 += kThreads) {
+                const int e = r0 + tid;
+                unsigned rec = 0;
+                bool acc = false;
+                if (e < LA) {
+                    rec = sList[e];
+                    acc = nms_eval(sMag, sFxy, rec >> 8, rec & 255, p.thr).cand;
+                }
+                int tot;
+                const int rank = cta_excl_scan(acc ? 1 : 0, sWarp, &tot);
+                if (acc) {
+                    sList[nacc + rank] = rec;
+                    atomicAdd(&sAccCnt[(rec >> 8) - 1], 1);
+                }
+                nacc += tot;
+            }
+            __syncthreads();
+            // ---- 4c. staging slots and the row-segment table ---------------
+            if (wid == 0) {
+                const int cnt = sAccCnt[lane];
+                int incl = cnt;
 #pragma unroll
-                    for (int kk = 0; kk < C::NT; ++kk) {
-                        const float2 hp = Pp[(h0 + kk) * kExt];
-                        const float2 hq = Qp[(h0 + kk) * kExt];
-                        const float4 t = tab[C::NT - 1 - kk];
-                        fxy = fmaf(hp.y, t.y, fxy);
-                        fyy = fmaf(hp.x, t.z, fyy);
-                        fxyy = fmaf(hp.y, t.z, fxyy);
-                        fyyy = fmaf(hp.x, t.w, fyyy);
-                        fxx = fmaf(hq.x, t.x, fxx);
-                        fxxy = fmaf(hq.x, t.y, fxxy);
-                        fxxx = fmaf(hq.y, t.x, fxxx);
+                for (int d = 1; d < 32; d <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, incl, d);
+                    if (lane >= d) incl += y;
+                }
+                int base = 0;
+                if (lane == 0 && nacc > 0) base = atomicAdd(&p.sc.words[1], nacc);
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (lane == 0) {
+                    sScal[1] = base;
+                    if ((long long)base + nacc > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
+                }
+                const int Gr = gr_base + lane + 1;
+                if (Gr >= 2 * ys && Gr < 2 * ys + 2 * S_act)
+                    p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
+            }
+            __syncthreads();
+            // ---- 5. per edgel: seven higher derivatives from the window into a
+            // deferred record (the FP64 epilogue runs when the ring is full)
+            {
+                const int base = sScal[1];
+                for (int j0 = 0; j0 < nacc;) {
+                    const int chunk = min(nacc - j0, C::NREC - nrec);
+                    for (int j = tid; j < chunk; j += kThreads) {
+                        const unsigned rec = sList[j0 + j];
+                        const int m = rec >> 8, c = rec & 255;
+                        const int a = m & 1, xe = c >> 1, b = c & 1;
+                        const int xv = b ? 2 : (a ? 1 : 0);
+                        const int yv = a ? 2 : (b ? 1 : 0);
+                        const float2* Pp = sP + xv * C::HS * kExt + xe;
+                        const float2* Qp = sP + (3 + xv) * C::HS * kExt + xe;
+                        const float4* tab = sTab + yv * C::NT;
+                        float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
+                        const int h0 = m >> 1;
+#pragma unroll
+                        for (int kk = 0; kk < C::NT; ++kk) {
+                            const float2 hp = Pp[(h0 + kk) * kExt];
+                            const float2 hq = Qp[(h0 + kk) * kExt];
+                            const float4 t = tab[C::NT - 1 - kk];
+                            fxy = fmaf(hp.y, t.y, fxy);
+                            fyy = fmaf(hp.x, t.z, fyy);
+                            fxyy = fmaf(hp.y, t.z, fxyy);
+                            fyyy = fmaf(hp.x, t.w, fyyy);
+                            fxx = fmaf(hq.x, t.x, fxx);
+                            fxxy = fmaf(hq.x, t.y, fxxy);
+                            fxxx = fmaf(hq.y, t.x, fxxx);
+                        }
+                        const NmsEval e = nms_eval(sMag, sFxy, m, c, p.thr);
+                        const int Gr = gr_base + m, Gc = gc_base + c;
+                        float* rc = sRec + (nrec + j) * C::RECW;
+                        rc[0] = e.gx; rc[1] = e.gy; rc[2] = e.mv; rc[3] = e.nx; rc[4] = e.ny; rc[5] = e.slope;
+                        rc[6] = e.Map; rc[7] = e.Mdp; rc[8] = e.Mam; rc[9] = e.Mdm;
+                        rc[10] = fxx; rc[11] = fxy; rc[12] = fyy; rc[13] = fxxy; rc[14] = fxyy; rc[15] = fxxx;
+                        rc[16] = fyyy;
+                        rc[17] = __int_as_float(Gr);
+                        rc[18] = __int_as_float(Gc);
+                        rc[19] = __int_as_float(base + j0 + j);
+                        rc[20] = __int_as_float(Gr * W2 + Gc);
                     }
-                    const NmsEval e = nms_eval(sMag, sFxy, m, c, p.thr);
-                    const int Gr = gr_base + m, Gc = gc_base + c;
-                    double x, y;
-                    float ori, str;
-                    if (HYB) {
-                        // peak fit in FP64 (cancellation in fm+fp-2f and fp-fm)
-                        const double s1 = e.slope;
-                        const double fp = (double)e.Map * (1.0 - s1) + (double)e.Mdp * s1;
-                        const double fm = (double)e.Mam * (1.0 - s1) + (double)e.Mdm * s1;
-                        const double num = fp - fm, den = fm + fp - 2.0 * (double)e.mv;
-                        const double ss = (double)sqrtf(1.f + e.slope * e.slope);
-                        const double rden = 1.0 / den;
-                        const double sst = -0.5 * num * ss * rden;
-                        const double maxf = (double)e.mv - 0.125 * num * num * rden;
-                        x = ((double)Gc + sst * (double)e.nx - 1.0) * 0.5;
-                        y = ((double)Gr + sst * (double)e.ny - 1.0) * 0.5;
-                        const float mf = (float)maxf;
-                        str = sqrtf((mf * e.nx) * (mf * e.nx) + (mf * e.ny) * (mf * e.ny));
-                        // third-order orientation in FP64 (cpu_toed.cpp:227-232)
-                        const double dfx = e.gx, dfy = e.gy, dxx = fxx, dxy = fxy, dyy = fyy;
-                        const double tix = dfx * (2.0 * dxx * dxx + 2.0 * dxy * dxy) +
-                                           dfy * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
-                                           2.0 * dfx * dfy * (double)fxxy + dfy * dfy * (double)fxyy +
-                                           dfx * dfx * (double)fxxx;
-                        const double tiy = dfx * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
-                                           dfy * (2.0 * dyy * dyy + 2.0 * dxy * dxy) +
-                                           2.0 * dfx * dfy * (double)fxyy + dfx * dfx * (double)fxxy +
-                                           dfy * dfy * (double)fyyy;
-                        ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000)
-                                                         : atan2f((float)tix, (float)(-tiy));
-                    } else {
-                        const float sl = e.slope;
-                        const float fp = e.Map * (1.f - sl) + e.Mdp * sl;
-                        const float fm = e.Mam * (1.f - sl) + e.Mdm * sl;
-                        const float num = fp - fm, den = fm + fp - 2.f * e.mv;
-                        const float ss = sqrtf(1.f + sl * sl);
-                        const float sst = -0.5f * num * ss / den;
-                        const float maxf = e.mv - 0.125f * num * num / den;
-                        x = ((double)((float)Gc + sst * e.nx) - 1.0) * 0.5;
-                        y = ((double)((float)Gr + sst * e.ny) - 1.0) * 0.5;
-                        str = sqrtf((maxf * e.nx) * (maxf * e.nx) + (maxf * e.ny) * (maxf * e.ny));
-                        const float tix = e.gx * (2.f * fxx * fxx + 2.f * fxy * fxy) +
-                                          e.gy * (2.f * fxx * fxy + 2.f * fyy * fxy) +
-                                          2.f * e.gx * e.gy * fxxy + e.gy * e.gy * fxyy + e.gx * e.gx * fxxx;
-                        const float tiy = e.gx * (2.f * fxx * fxy + 2.f * fyy * fxy) +
-                                          e.gy * (2.f * fyy * fyy + 2.f * fxy * fxy) +
-                                          2.f * e.gx * e.gy * fxyy + e.gx * e.gx * fxxy + e.gy * e.gy * fyyy;
-                        ori = (tix == 0.f && tiy == 0.f) ? __int_as_float(0x7fc00000) : atan2f(tix, -tiy);
-                    }
-                    const long long dst = (long long)base + j;
-                    if (dst < p.sc.staging_cap) {
-                        p.sc.staging[dst] = make_double4_32a(x, y, (double)ori, (double)str);
-                        p.sc.staging_idx[dst] = Gr * W2 + Gc;
+                    nrec += chunk;
+                    j0 += chunk;
+                    if (nrec == C::NREC) {
+                        __syncthreads();
+                        for (int r = tid; r < nrec; r += kThreads) finish_edgel<HYB>(sRec + r * C::RECW, p.sc);
+                        nrec = 0;
+                        __syncthreads();
                     }
                 }
             }
             __syncthreads();
             // ---- 6. slide the windows -------------------------------------
             if (s + 1 < nsteps) {
-                // row-pass window: slots [B, HS) -> [0, 2R+3), in phases of B rows so
-                // that no source slot is overwritten before it is read
-                for (int ph = 0; ph < 2 * R + 3; ph += B) {
-                    const int nr = min(B, 2 * R + 3 - ph);
-                    const int n4 = 6 * nr * (kExt / 2);
-                    for (int i = tid; i < n4; i += kThreads) {
-                        const int a = i / (nr * 16), rem = i - a * nr * 16;
+                // row-pass window: slots [B, HS) -> [0, 2R+3); every thread reads
+                // its share into registers before anyone writes (sources and
+                // destinations overlap when 2R+3 > B)
+                constexpr int NSH = 6 * (2 * R + 3) * (kExt / 2);
+                constexpr int PER = (NSH + kThreads - 1) / kThreads;
+                float4 keep[PER];
+#pragma unroll
+                for (int t = 0; t < PER; ++t) {
+                    const int i = tid + t * kThreads;
+                    if (i < NSH) {
+                        const int a = i / ((2 * R + 3) * 16), rem = i - a * (2 * R + 3) * 16;
                         const int rr = rem >> 4, cc = (rem & 15) * 2;
-                        const float4 v = *reinterpret_cast<const float4*>(sP + (a * C::HS + B + ph + rr) * kExt + cc);
-                        *reinterpret_cast<float4*>(sP + (a * C::HS + ph + rr) * kExt + cc) = v;
+                        keep[t] = *reinterpret_cast<const float4*>(sP + (a * C::HS + B + rr) * kExt + cc);
                     }
-                    __syncthreads();
+                }
+                __syncthreads();
+#pragma unroll
+                for (int t = 0; t < PER; ++t) {
+                    const int i = tid + t * kThreads;
+                    if (i < NSH) {
+                        const int a = i / ((2 * R + 3) * 16), rem = i - a * (2 * R + 3) * 16;
+                        const int rr = rem >> 4, cc = (rem & 15) * 2;
+                        *reinterpret_cast<float4*>(sP + (a * C::HS + rr) * kExt + cc) = keep[t];
+                    }
                 }
                 for (int i = tid; i < 2 * 64; i += kThreads) {
                     sMag[i] = sMag[2 * B * 64 + i];
@@ -463,6 +668,8 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
             }
         }
     }
+    // flush the records still in the ring (the loop exit follows a barrier)
+    for (int r = tid; r < nrec; r += kThreads) finish_edgel<HYB>(sRec + r * C::RECW, p.sc);
 }
 
 template <int R, bool HYB>

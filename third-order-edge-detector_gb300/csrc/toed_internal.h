@@ -19,6 +19,16 @@ DetectEntry detect_entry(int radius, bool hyb);
 
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
 
+// Fill d.tma / d.tma_align / d.tma_boxw and encode the image's row map for
+// TMA staging (kStepRows-row boxes, zero fill outside the image).  Leaves
+// d.tma = 0 -- plain loads -- when the driver entry point is unavailable or
+// the image's base or pitch is not 16-byte aligned.
+void encode_rows_map(CUtensorMap* m, DetImage& d, int radius);
+
+// Enqueue the adjoint kernels (toed_backward.cu); cot: sum(n_edgels) x 18 floats.
+cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_params* prm, int r, float* cot,
+                            double* gsig, cudaStream_t stream);
+
 // Scratch of the TO-correction pipeline (owned by the caller's context).
 struct SubScratch {
     Scratch sc;

@@ -149,6 +149,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     d.tile_base = 0;
     d.seg_base = 0;
     d.nseg = 2LL * im->height * nsc;
+    encode_rows_map(&p.tmap[0], d, r);
     p.n_units = d.nsc * d.nsr;
     p.n_tiles = (int)((d.nseg + kSegTile - 1) / kSegTile);
     p.sc.words = reinterpret_cast<int*>(base + kOffWords);

@@ -201,18 +201,21 @@ def ridge_map(H: int = 2048, W: int = 2048, seed: int = 5000, n_curves: int = 40
     return np.clip(E, 0.0, 1.0).astype(dtype)
 
 
-def ellipse_distance(px, py, e: Ellipse) -> np.ndarray:
-    """Euclidean distance from points to the boundary of ellipse ``e`` (FP64,
-    Newton on the parametric angle, 12 iterations from a radial start)."""
+def ellipse_closest(px, py, e: Ellipse):
+    """Closest point on the boundary of ellipse ``e`` to each (px, py) and
+    its distance (FP64; Newton on the parametric angle in the first
+    quadrant of the ellipse frame from three starts -- radial and both axes --
+    keeping the nearest)."""
     px = np.asarray(px, np.float64)
     py = np.asarray(py, np.float64)
     c, s = math.cos(e.theta), math.sin(e.theta)
     dx, dy = px - e.cx, py - e.cy
-    u = np.abs(dx * c + dy * s)
-    v = np.abs(-dx * s + dy * c)
+    u0 = dx * c + dy * s
+    v0 = -dx * s + dy * c
+    su, sv = np.where(u0 < 0, -1.0, 1.0), np.where(v0 < 0, -1.0, 1.0)
+    u, v = np.abs(u0), np.abs(v0)
     a, b = e.a, e.b
-    best = None
-    # Newton from three starts (radial, both axes); keep the closest boundary point
+    best_d = best_t = None
     for t0 in (np.arctan2(a * v, b * u), np.zeros_like(u), np.full_like(u, math.pi / 2)):
         t = t0.copy()
         for _ in range(16):
@@ -221,5 +224,33 @@ def ellipse_distance(px, py, e: Ellipse) -> np.ndarray:
             fp = (a * a - b * b) * (ct * ct - st * st) - u * a * ct - v * b * st
             t = np.clip(t - f / np.where(np.abs(fp) < 1e-30, 1e-30, fp), 0.0, math.pi / 2)
         d = np.hypot(u - a * np.cos(t), v - b * np.sin(t))
-        best = d if best is None else np.minimum(best, d)
+        if best_d is None:
+            best_d, best_t = d, t
+        else:
+            better = d < best_d
+            best_d, best_t = np.where(better, d, best_d), np.where(better, t, best_t)
+    qu, qv = su * a * np.cos(best_t), sv * b * np.sin(best_t)
+    qx = e.cx + qu * c - qv * s
+    qy = e.cy + qu * s + qv * c
+    return best_d, qx, qy
+
+
+def ellipse_distance(px, py, e: Ellipse) -> np.ndarray:
+    """Euclidean distance from points to the boundary of ellipse ``e``."""
+    return ellipse_closest(px, py, e)[0]
+
+
+def nearest_boundary_points(px, py, shapes):
+    """For each point, the closest boundary point over all ellipses of
+    ``shapes`` (polygons are ignored): returns (qx, qy, distance)."""
+    best = None
+    for e in shapes:
+        if not isinstance(e, Ellipse):
+            continue
+        d, qx, qy = ellipse_closest(px, py, e)
+        if best is None:
+            best = [qx, qy, d]
+        else:
+            m = d < best[2]
+            best = [np.where(m, qx, best[0]), np.where(m, qy, best[1]), np.where(m, d, best[2])]
     return best
