@@ -335,6 +335,44 @@ def side_measurements(toed, det, images, side, stream):
     return out
 
 
+def run_workload(args):
+    """One secondary workload alone (for profiling its kernels): 'fwd_bwd' =
+    the differentiable batch of 16 float32 512x512 ellipse images, sigma 1.5,
+    forward then backward per step; 'subpix' = TO correction of 8 float32
+    2048x2048 ridge maps.  Prints one JSON line of timings."""
+    if args.workload == "fwd_bwd":
+        jobs = [(512, 512, 4000 + k, "f32", True) for k in range(16)]
+    else:
+        jobs = [(2048, 2048, 5000 + k, "ridge", False) for k in range(8)]
+    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
+        ims = pool.map(_gen_shapes, jobs)
+    import torch
+    toed = _pkg()
+    if not os.path.exists(toed.LIB_PATH):
+        toed.build()
+    det = toed.Detector(0)
+    stream = torch.cuda.current_stream()
+    x = [torch.as_tensor(im).cuda() for im in ims]
+    npx = sum(im.size for im in ims)
+    if args.workload == "fwd_bwd":
+        o = det.alloc_outputs([im.shape for im in x], None)
+        prm = toed.make_params(SIGMA, 0, THRESH)
+        res = det.detect_batch(x, sigma=SIGMA)
+        gout = [torch.randn_like(r["edgels"]) for r in res]
+        idx = [r["index"] for r in res]
+        fwd = _time_ms(lambda: det.detect_into(x, o, prm, stream), args.steps, stream)
+        bwd = _time_ms(lambda: det.backward_batch(x, idx, gout, sigma=SIGMA), args.steps, stream)
+        line = {"workload": "fwd_bwd 16 x 512^2 float32, sigma 1.5", "fwd_ms": round(fwd, 4),
+                "bwd_ms": round(bwd, 4), "fwd_plus_bwd_over_fwd": round((fwd + bwd) / fwd, 3),
+                "edgels": int(sum(r["count"] for r in res))}
+    else:
+        tms = _time_ms(lambda: det.subpix_to_correct_batch(x, thresh=0.1, sigma=2.0, nbr_radius=2.0, dense=True),
+                       args.steps, stream)
+        line = {"workload": "subpix 8 x 2048^2 float32 ridge maps", "ms": round(tms, 3),
+                "mpx_s": round(npx / (tms * 1e-3) / 1e6, 1)}
+    print(json.dumps(line), flush=True)
+
+
 def flops_per_px(r: int) -> int:
     """Dense FP32 work of the fused kernel per original pixel: row pass
     4(2r+1)+8+4(2r+3) FMA + column pass of Ix, Iy at four sub-grids
@@ -490,9 +528,14 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-side", action="store_true", help="skip the other configurations' measurements")
+    ap.add_argument("--workload", default="batch", choices=["batch", "fwd_bwd", "subpix"],
+                    help="batch: the headline line; fwd_bwd / subpix: that secondary workload alone")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
+    if args.workload != "batch":
+        run_workload(args)
+        return
     ws, rank, local = dist_init()
     if args.impl == "reference":
         run_reference(args, ws, rank)

@@ -33,7 +33,19 @@ def _run(detector, img, sigma, **kw):
     return r["count"], e, i
 
 
-def _check(ref, got_e, got_i, exact_set=False, agree=AGREE, ori=ORI):
+def _undecidable(img, sigma, thr=2.0, tol=1e-5):
+    """2x-grid indices whose FP64 gradient magnitude lies within tol (relative)
+    of the threshold: FP32 derivative sums cannot decide them either way."""
+    import oracle as o
+    pl = o.detect(img.astype(np.float64), sigma, threshold=thr, planes=True)["planes"]
+    return np.flatnonzero(np.abs(pl[2].ravel() - thr) <= tol * thr)
+
+
+def _check(ref, got_e, got_i, exact_set=False, agree=AGREE, ori=ORI, skip=None):
+    if skip is not None and len(skip):
+        kr, kg = ~np.isin(ref["index"], skip), ~np.isin(got_i, skip)
+        ref = {"edges": ref["edges"][kr], "index": ref["index"][kr]}
+        got_e, got_i = got_e[kg], got_i[kg]
     m = compare_edgels(ref["edges"], ref["index"], got_e, got_i)
     if exact_set:
         assert m["n_ref"] == m["n_got"] == m["n_common"], m
@@ -95,7 +107,9 @@ def test_ragged_sizes(detector, oracle, synth, H, W):
                              scale_to_base=False, dtype=np.float32).image
     ref = oracle.detect(img.astype(np.float64), 1.5)
     n, e, i = _run(detector, img, 1.5)
-    _check(ref, e, i, exact_set=True)
+    # exact as sets, except pixels whose magnitude is within FP32 resolution
+    # of the threshold (127 x 91 holds one, 1.2e-7 above it)
+    _check(ref, e, i, exact_set=True, skip=_undecidable(img, 1.5))
 
 
 def test_threshold_and_border(detector, oracle, synth):
@@ -206,3 +220,23 @@ def test_tma_and_plain_loads_identical(detector, synth, dtype, W):
     b = detector.detect(buf[:, :W], sigma=1.5)
     assert a["count"] > 20
     assert t.equal(a["edgels"], b["edgels"]) and t.equal(a["index"], b["index"])
+
+
+def test_cuda_graph_replay(detector, synth, toed):
+    """The batched launch captured in a CUDA graph replays to the same edgels."""
+    t = _torch()
+    imgs = [t.as_tensor(synth.shapes_image(h, w, seed=70 + h, dtype=np.float32).image).cuda()
+            for h, w in [(200, 260), (96, 333), (300, 120)]]
+    params = toed.make_params(1.5)
+    outs = detector.alloc_outputs([im.shape for im in imgs], None)
+    g = detector.capture(imgs, outs, params)
+    ref = detector.detect_batch(imgs, sigma=1.5)
+    for o in outs:
+        o["edgels"].zero_()
+        o["count"].zero_()
+    g.replay()
+    t.cuda.synchronize()
+    for o, r in zip(outs, ref):
+        n = int(o["count"].item())
+        assert n == r["count"] > 20
+        assert t.equal(o["edgels"][:n], r["edgels"]) and t.equal(o["index"][:n], r["index"])

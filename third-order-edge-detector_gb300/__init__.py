@@ -271,6 +271,26 @@ class Detector:
         _check(lib().toed_detect_batch(self._ctx, arr, n, ctypes.byref(params),
                                        ctypes.c_void_p(s.cuda_stream)), "toed_detect_batch")
 
+    def capture(self, images, outs, params: toed_params, warmup: int = 1):
+        """Capture detect_into(images, outs, params) in a CUDA graph (the
+        persistent detection launch plus the ordering pass) and return it;
+        ``graph.replay()`` re-runs the batch on the same buffers with no host
+        work.  Scratch is reserved first, so nothing allocates under capture."""
+        t = self.torch
+        npx = sum(int(im.numel()) for im in images)
+        self.reserve(npx, sum(int(o["capacity"]) for o in outs), len(images))
+        s = t.cuda.Stream(self.device)
+        s.wait_stream(t.cuda.current_stream(self.device))
+        with t.cuda.stream(s):
+            for _ in range(warmup):
+                self.detect_into(images, outs, params, s)
+        s.synchronize()
+        g = t.cuda.CUDAGraph()
+        with t.cuda.graph(g, stream=s):
+            self.detect_into(images, outs, params, s)
+        t.cuda.current_stream(self.device).wait_stream(s)
+        return g
+
     def detect_batch(self, images, sigma=2.0, threshold=2.0, radius=0, border=10,
                      out_dtype=TOED_F32, precision=TOED_HYBRID, capacity=None, index=True,
                      stream=None):

@@ -149,29 +149,37 @@ __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int in0,
         float o_[2][12];
 #pragma unroll
         for (int o = 0; o < 2; ++o) {
-            float tG = 0.f, tGx = 0.f, tGxx = 0.f, tGxxx = 0.f;
+            // The taps are exactly symmetric (G, Gxx) or antisymmetric (Gx,
+            // Gxxx) about 0, and about -1/2 for the shifted set, so each
+            // mirrored pair of inputs is summed / differenced once and shared
+            // by the even / odd filters.
+            const int c = o + R + 1;  // centre: out(x) = sum_q in(x-q) X(q), in(x-q) = v[c-q]
+            float tG = v[c] * tp.v[0][R + 1], tGxx = v[c] * tp.v[2][R + 1], tGx = 0.f, tGxxx = 0.f;
 #pragma unroll
-            for (int q = -R; q <= R; ++q) {
-                const float x = v[o + R + 1 - q];
-                tG = fmaf(x, tp.v[0][q + R + 1], tG);
-                tGx = fmaf(x, tp.v[1][q + R + 1], tGx);
-                tGxx = fmaf(x, tp.v[2][q + R + 1], tGxx);
-                tGxxx = fmaf(x, tp.v[3][q + R + 1], tGxxx);
+            for (int q = 1; q <= R; ++q) {
+                const float sm = v[c - q] + v[c + q], df = v[c - q] - v[c + q];
+                tG = fmaf(sm, tp.v[0][q + R + 1], tG);
+                tGxx = fmaf(sm, tp.v[2][q + R + 1], tGxx);
+                tGx = fmaf(df, tp.v[1][q + R + 1], tGx);
+                tGxxx = fmaf(df, tp.v[3][q + R + 1], tGxxx);
             }
-            // full 2r+3-tap responses add the two outermost taps q = +-(r+1)
-            const float xl = v[o], xr = v[o + 2 * R + 2];
-            const float fG = fmaf(xr, tp.v[0][0], fmaf(xl, tp.v[0][2 * R + 2], tG));
-            const float fGx = fmaf(xr, tp.v[1][0], fmaf(xl, tp.v[1][2 * R + 2], tGx));
-            const float fGxx = fmaf(xr, tp.v[2][0], fmaf(xl, tp.v[2][2 * R + 2], tGxx));
-            const float fGxxx = fmaf(xr, tp.v[3][0], fmaf(xl, tp.v[3][2 * R + 2], tGxxx));
-            float sG = 0.f, sGx = 0.f, sGxx = 0.f, sGxxx = 0.f;
+            // full 2r+3-tap responses add the pair q = +-(r+1)
+            const float smo = v[c - R - 1] + v[c + R + 1], dfo = v[c - R - 1] - v[c + R + 1];
+            const float fG = fmaf(smo, tp.v[0][2 * R + 2], tG);
+            const float fGx = fmaf(dfo, tp.v[1][2 * R + 2], tGx);
+            const float fGxx = fmaf(smo, tp.v[2][2 * R + 2], tGxx);
+            const float fGxxx = fmaf(dfo, tp.v[3][2 * R + 2], tGxxx);
+            // shifted taps X(q + 1/2): pairs (q, -1-q) for q = 0..r, then q = r+1 alone
+            const float vl = v[c - R - 1];
+            float sG = vl * tp.v[4][2 * R + 2], sGx = vl * tp.v[5][2 * R + 2];
+            float sGxx = vl * tp.v[6][2 * R + 2], sGxxx = vl * tp.v[7][2 * R + 2];
 #pragma unroll
-            for (int q = -(R + 1); q <= R + 1; ++q) {
-                const float x = v[o + R + 1 - q];
-                sG = fmaf(x, tp.v[4][q + R + 1], sG);
-                sGx = fmaf(x, tp.v[5][q + R + 1], sGx);
-                sGxx = fmaf(x, tp.v[6][q + R + 1], sGxx);
-                sGxxx = fmaf(x, tp.v[7][q + R + 1], sGxxx);
+            for (int q = 0; q <= R; ++q) {
+                const float sm = v[c - q] + v[c + 1 + q], df = v[c - q] - v[c + 1 + q];
+                sG = fmaf(sm, tp.v[4][q + R + 1], sG);
+                sGxx = fmaf(sm, tp.v[6][q + R + 1], sGxx);
+                sGx = fmaf(df, tp.v[5][q + R + 1], sGx);
+                sGxxx = fmaf(df, tp.v[7][q + R + 1], sGxxx);
             }
             o_[o][0] = tG;  o_[o][1] = tGx;  o_[o][2] = fG;  o_[o][3] = fGx;
             o_[o][4] = sG;  o_[o][5] = sGx;  o_[o][6] = tGxx; o_[o][7] = tGxxx;
