@@ -146,8 +146,6 @@ struct toed_ctx {
     long long img_count_cap = 0;
     unsigned char* keep = nullptr;
     long long keep_cap = 0;
-    float* cot = nullptr;
-    long long cot_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
@@ -225,7 +223,6 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->win);
     cudaFree(c->img_count);
     cudaFree(c->keep);
-    cudaFree(c->cot);
     cudaSetDevice(prev);
     delete c;
     return TOED_OK;
@@ -561,19 +558,12 @@ extern "C" toed_status toed_backward_batch(toed_ctx* c, const toed_grad_image* i
     toed_status st = TOED_OK;
     {
         std::lock_guard<std::mutex> lk(c->mu);
-        st = grow(&c->cot, &c->cot_cap, std::max(1LL, tot * 18), stream);
-        if (st == TOED_OK) {
-            cudaError_t e = cudaMemsetAsync(grad_sigma, 0, sizeof(double), stream);
-            for (int i0 = 0; i0 < n && e == cudaSuccess; i0 += kBatchMax) {
-                const int cn = std::min(kBatchMax, n - i0);
-                long long off = 0;
-                for (int i = 0; i < i0; ++i) off += items[i].n_edgels;
-                e = backward_launch(items + i0, cn, prm, r, c->cot + off * 18, grad_sigma, stream);
-            }
-            if (e != cudaSuccess) {
-                g_last_cuda_error = std::string("backward: ") + cudaGetErrorString(e);
-                st = TOED_ERR_CUDA;
-            }
+        cudaError_t e = cudaMemsetAsync(grad_sigma, 0, sizeof(double), stream);
+        for (int i0 = 0; i0 < n && e == cudaSuccess; i0 += kBatchMax)
+            e = backward_launch(items + i0, std::min(kBatchMax, n - i0), prm, r, grad_sigma, stream);
+        if (e != cudaSuccess) {
+            g_last_cuda_error = std::string("backward: ") + cudaGetErrorString(e);
+            st = TOED_ERR_CUDA;
         }
     }
     if (prev != c->device) cudaSetDevice(prev);

@@ -3,17 +3,19 @@
 // respect to the image pixels and sigma.  The reference has no backward; the
 // forward whose adjoint this is follows cpu_toed.cpp:128-545.
 //
-// bw_adjoint<R>  one thread per edgel: re-evaluates, from the image, the nine
-//                derivatives at the edgel's 2x-grid point P and Ix, Iy at the
-//                four NMS neighbours of its (frozen) sector, each with its
-//                d/dsigma, then runs the chain rule through the peak fit and
-//                the third-order orientation in FP64; writes 17 cotangents
-//                per edgel and accumulates dL/dsigma.
-// bw_scatter<R>  one CTA per 32x32 pixel tile: finds the edgels whose
-//                windows reach the tile (binary search on the row-major grid
-//                index), adds each point's separable cotangent window
-//                sum_f X_f(q) V_f(p) into a shared-memory tile, writes the
-//                tile -- no global atomics; every pixel written once.
+// One kernel, bw_adjoint<R>, in three phases per block of 128 edgels:
+//   1. a warp per edgel re-evaluates, from the image, the nine derivatives
+//      at the edgel's 2x-grid point P and Ix, Iy at the four NMS neighbours
+//      of its (frozen) sector, each with its d/dsigma (one pass over the
+//      union window of the five points, coalesced rows);
+//   2. a thread per edgel runs the chain rule through the peak fit and the
+//      third-order orientation (FP64 where the forward needs it) and
+//      accumulates dL/dsigma;
+//   3. a warp per edgel adds the separable cotangent windows
+//      sum_f X_f(q) V_f(p) of its five points onto the pixel gradient with
+//      vector float reductions in global memory (the host clears it first).
+// Reductions from different edgels land in an unspecified order, so the
+// pixel gradient is reproducible to float rounding, not bit for bit.
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -23,8 +25,6 @@
 
 namespace toed {
 
-constexpr int kBwT = 32;    // scatter tile side
-constexpr int kCotW = 18;   // floats per edgel cotangent record (17 + sector bits)
 constexpr int kBwAdjThreads = 128;
 
 struct BwImage {
@@ -35,7 +35,6 @@ struct BwImage {
     float* gpix;
     int H, W, dtype, n;
     int edgel_base;
-    int ntx, nty, tile_base;
 };
 
 struct BwParams {
@@ -44,31 +43,9 @@ struct BwParams {
     int out_f64;
     int n_img;
     int n_edgels;
-    int n_tiles;
-    float* cot;               // n_edgels x kCotW
     double* gsig;
     BwImage img[kBatchMax];
 };
-
-// Shared tap tables per variant (0: unshifted, ends zeroed -- sub-grid (0,0);
-// 1: unshifted 2r+3 taps; 2: shifted): A = filters, S = d/dsigma.
-template <int R>
-__device__ __forceinline__ void build_tables(const BwParams& p, float4* sA, float4* sS)
-{
-    constexpr int NT = 2 * R + 3;
-    for (int i = threadIdx.x; i < 3 * NT; i += blockDim.x) {
-        const int v = i / NT, k = i - v * NT;
-        const int f = (v == 2) ? 4 : 0;
-        float4 a = make_float4(p.tap[f][k], p.tap[f + 1][k], p.tap[f + 2][k], p.tap[f + 3][k]);
-        float4 s = make_float4(p.tap[8 + f][k], p.tap[9 + f][k], p.tap[10 + f][k], p.tap[11 + f][k]);
-        if (v == 0 && (k == 0 || k == NT - 1)) {
-            a = make_float4(0.f, 0.f, 0.f, 0.f);
-            s = a;
-        }
-        sA[i] = a;
-        sS[i] = s;
-    }
-}
 
 __device__ __forceinline__ void variants(int rho, int kap, int* xv, int* yv)
 {
@@ -84,129 +61,320 @@ __device__ __forceinline__ float pix(const BwImage& im, int y, int x)
     return im.dtype == TOED_U8 ? (float)__ldg((const unsigned char*)im.src + o) : __ldg((const float*)im.src + o);
 }
 
-// Derivatives at 2x-grid point (rho, kap) as the reference defines them
-// (cpu_toed.cpp:204-344): f = sum_{p,q} I(i-p, j-q) X(q) Y(p), with their
-// d/dsigma.  FULL: all nine (fx fy fxx fxy fyy fxxy fxyy fxxx fyyy), else fx, fy.
-template <int R, bool FULL>
-__device__ __forceinline__ void eval_point(const BwImage& im, int rho, int kap, const float4* sA,
-                                           const float4* sS, float* d, float* ds)
+// Tap tables with two zero entries on each side: entry k + 2 holds tap k, so
+// a window offset by -1..+1 pixel (the NMS neighbours) indexes them without
+// bounds tests.
+template <int R>
+__device__ __forceinline__ void build_tables_padded(const BwParams& p, float4* sA, float4* sS)
 {
-    constexpr int NT = 2 * R + 3;
-    int xv, yv;
-    variants(rho, kap, &xv, &yv);
-    const int i = rho >> 1, j = kap >> 1;
-    const float4* XA = sA + xv * NT;
-    const float4* XS = sS + xv * NT;
-    const float4* YA = sA + yv * NT;
-    const float4* YS = sS + yv * NT;
-    constexpr int ND = FULL ? 9 : 2;
-#pragma unroll
-    for (int k = 0; k < ND; ++k) d[k] = ds[k] = 0.f;
-    for (int pp = 0; pp < NT; ++pp) {
-        const int y = i + R + 1 - pp;  // row i - p, p = pp - (R+1)
-        float h0 = 0.f, h1 = 0.f, h2 = 0.f, h3 = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
-#pragma unroll
-        for (int qq = 0; qq < NT; ++qq) {
-            const float v = pix(im, y, j + R + 1 - qq);
-            const float4 t = XA[qq], ts = XS[qq];
-            h0 = fmaf(v, t.x, h0);
-            h1 = fmaf(v, t.y, h1);
-            s0 = fmaf(v, ts.x, s0);
-            s1 = fmaf(v, ts.y, s1);
-            if (FULL) {
-                h2 = fmaf(v, t.z, h2);
-                h3 = fmaf(v, t.w, h3);
-                s2 = fmaf(v, ts.z, s2);
-                s3 = fmaf(v, ts.w, s3);
-            }
+    constexpr int NT = 2 * R + 3, NTP = NT + 4;
+    for (int i = threadIdx.x; i < 3 * NTP; i += blockDim.x) {
+        const int v = i / NTP, k = i - v * NTP - 2;
+        const int f = (v == 2) ? 4 : 0;
+        float4 a = make_float4(0.f, 0.f, 0.f, 0.f), s = a;
+        if (k >= 0 && k < NT && !(v == 0 && (k == 0 || k == NT - 1))) {
+            a = make_float4(p.tap[f][k], p.tap[f + 1][k], p.tap[f + 2][k], p.tap[f + 3][k]);
+            s = make_float4(p.tap[8 + f][k], p.tap[9 + f][k], p.tap[10 + f][k], p.tap[11 + f][k]);
         }
-        const float4 ya = YA[pp], ys = YS[pp];
-        // fx = (Gx, G), fy = (G, Gy)
-        d[0] = fmaf(h1, ya.x, d[0]);
-        ds[0] = fmaf(s1, ya.x, fmaf(h1, ys.x, ds[0]));
-        d[1] = fmaf(h0, ya.y, d[1]);
-        ds[1] = fmaf(s0, ya.y, fmaf(h0, ys.y, ds[1]));
-        if (FULL) {
-            d[2] = fmaf(h2, ya.x, d[2]);  // fxx  (Gxx, G)
-            ds[2] = fmaf(s2, ya.x, fmaf(h2, ys.x, ds[2]));
-            d[3] = fmaf(h1, ya.y, d[3]);  // fxy  (Gx, Gy)
-            ds[3] = fmaf(s1, ya.y, fmaf(h1, ys.y, ds[3]));
-            d[4] = fmaf(h0, ya.z, d[4]);  // fyy  (G, Gyy)
-            ds[4] = fmaf(s0, ya.z, fmaf(h0, ys.z, ds[4]));
-            d[5] = fmaf(h2, ya.y, d[5]);  // fxxy (Gxx, Gy)
-            ds[5] = fmaf(s2, ya.y, fmaf(h2, ys.y, ds[5]));
-            d[6] = fmaf(h1, ya.z, d[6]);  // fxyy (Gx, Gyy)
-            ds[6] = fmaf(s1, ya.z, fmaf(h1, ys.z, ds[6]));
-            d[7] = fmaf(h3, ya.x, d[7]);  // fxxx (Gxxx, G)
-            ds[7] = fmaf(s3, ya.x, fmaf(h3, ys.x, ds[7]));
-            d[8] = fmaf(h0, ya.w, d[8]);  // fyyy (G, Gyyy)
-            ds[8] = fmaf(s0, ya.w, fmaf(h0, ys.w, ds[8]));
-        }
+        sA[i] = a;
+        sS[i] = s;
     }
 }
 
+// Per edgel, the 34 values the chain rule needs: the nine derivatives at P
+// and their d/dsigma (0..17), then fx, fy, dfx/dsigma, dfy/dsigma at the four
+// NMS neighbours A+, D+, A-, D- (18..33); slot 34 holds the sector bits.
+constexpr int kNVal = 34;
+constexpr int kValsPad = 37;  // row stride in shared memory (odd: conflict-free per-thread rows)
+constexpr int kRedPad = 33;
+
+// Sum over the union columns of value k (lane k): red[k][0..n) in a fixed order.
+__device__ __forceinline__ float column_sum(const float* red_k, int n)
+{
+    float a = 0.f, b = 0.f;
+    int t = 0;
+    for (; t + 1 < n; t += 2) {
+        a += red_k[t];
+        b += red_k[t + 1];
+    }
+    if (t < n) a += red_k[t];
+    return a + b;
+}
+
+// The 34 values of one edgel, evaluated by a whole warp as the reference
+// defines the derivatives (cpu_toed.cpp:204-344): f = sum_{p,q} I(i-p, j-q)
+// X(q) Y(p).  All five points' windows lie in the (NT+2) x (NT+2) union
+// window around the edgel's pixel (i, j); lane c holds union column
+// j-R-2+c, loads the union rows once (coalesced), contracts them with each
+// point's y taps (lane-local), multiplies by its x taps, and the partial
+// products are summed per value through shared memory.  The neighbours
+// depend on the sector of P's (fx, fy), so P is summed first.  Lane 0's
+// results land in row[0..33], the sector bits in row[34].
+template <int R>
+__device__ __forceinline__ void eval_edgel_warp(const BwImage& im, int rho, int kap, int lane, const float4* sA,
+                                                const float4* sS, float (*red)[kRedPad], float* row)
+{
+    constexpr int NT = 2 * R + 3, NTP = NT + 4, NU = NT + 2;
+    const int i = rho >> 1, j = kap >> 1;
+    const int col = j - R - 2 + lane;
+    const bool okc = lane < NU && col >= 0 && col < im.W;
+    float v[NU];
+    if (im.dtype == TOED_U8) {
+        const unsigned char* src = (const unsigned char*)im.src + col;
+#pragma unroll
+        for (int u = 0; u < NU; ++u) {
+            const int y = i - R - 2 + u;
+            v[u] = (okc && (unsigned)y < (unsigned)im.H) ? (float)__ldg(src + (long long)y * im.pitch) : 0.f;
+        }
+    } else {
+        const float* src = (const float*)im.src + col;
+#pragma unroll
+        for (int u = 0; u < NU; ++u) {
+            const int y = i - R - 2 + u;
+            v[u] = (okc && (unsigned)y < (unsigned)im.H) ? __ldg(src + (long long)y * im.pitch) : 0.f;
+        }
+    }
+    // ---- P: nine derivatives and their d/dsigma ----
+    {
+        int xv, yv;
+        variants(rho, kap, &xv, &yv);
+        // y tap of union row u: pp = NT - u (entry NT + 2 - u); x tap of lane: qq = NT - lane
+        const float4* YA = sA + yv * NTP + NT + 2;
+        const float4* YS = sS + yv * NTP + NT + 2;
+        float c0 = 0.f, c1 = 0.f, c2 = 0.f, c3 = 0.f, s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f;
+#pragma unroll
+        for (int u = 0; u < NU; ++u) {
+            const float4 ya = YA[-u], ys = YS[-u];
+            c0 = fmaf(v[u], ya.x, c0); c1 = fmaf(v[u], ya.y, c1);
+            c2 = fmaf(v[u], ya.z, c2); c3 = fmaf(v[u], ya.w, c3);
+            s0 = fmaf(v[u], ys.x, s0); s1 = fmaf(v[u], ys.y, s1);
+            s2 = fmaf(v[u], ys.z, s2); s3 = fmaf(v[u], ys.w, s3);
+        }
+        if (lane < NU) {
+            const float4 xa = sA[xv * NTP + NT + 2 - lane], xs = sS[xv * NTP + NT + 2 - lane];
+            // fx (Gx,G) fy (G,Gy) fxx (Gxx,G) fxy (Gx,Gy) fyy (G,Gyy)
+            // fxxy (Gxx,Gy) fxyy (Gx,Gyy) fxxx (Gxxx,G) fyyy (G,Gyyy)
+            red[0][lane] = xa.y * c0;  red[9][lane] = fmaf(xs.y, c0, xa.y * s0);
+            red[1][lane] = xa.x * c1;  red[10][lane] = fmaf(xs.x, c1, xa.x * s1);
+            red[2][lane] = xa.z * c0;  red[11][lane] = fmaf(xs.z, c0, xa.z * s0);
+            red[3][lane] = xa.y * c1;  red[12][lane] = fmaf(xs.y, c1, xa.y * s1);
+            red[4][lane] = xa.x * c2;  red[13][lane] = fmaf(xs.x, c2, xa.x * s2);
+            red[5][lane] = xa.z * c1;  red[14][lane] = fmaf(xs.z, c1, xa.z * s1);
+            red[6][lane] = xa.y * c2;  red[15][lane] = fmaf(xs.y, c2, xa.y * s2);
+            red[7][lane] = xa.w * c0;  red[16][lane] = fmaf(xs.w, c0, xa.w * s0);
+            red[8][lane] = xa.x * c3;  red[17][lane] = fmaf(xs.x, c3, xa.x * s3);
+        }
+        __syncwarp();
+        if (lane < 18) row[lane] = column_sum(red[lane], NU);
+        __syncwarp();
+    }
+    // ---- the frozen sector (cpu_toed.cpp:415-462 in closed form) and the
+    // four neighbours' fx, fy with their d/dsigma ----
+    const float fx = row[0], fy = row[1];
+    const bool xmaj = fabsf(fx) >= fabsf(fy);
+    const int sx = fx >= 0.f ? 1 : -1, sy = fy >= 0.f ? 1 : -1;
+    const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+    const int nr[4] = {rho + ar, rho + sy, rho - ar, rho - sy};  // A+, D+, A-, D-
+    const int nc[4] = {kap + ac, kap + sx, kap - ac, kap - sx};
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        int xv, yv;
+        variants(nr[q], nc[q], &xv, &yv);
+        const int di = (nr[q] >> 1) - i, dj = (nc[q] >> 1) - j;
+        const float4* YA = sA + yv * NTP + NT + 2 + di;
+        const float4* YS = sS + yv * NTP + NT + 2 + di;
+        float cg = 0.f, cy = 0.f, sg = 0.f, sy_ = 0.f;
+#pragma unroll
+        for (int u = 0; u < NU; ++u) {
+            const float4 ya = YA[-u], ys = YS[-u];
+            cg = fmaf(v[u], ya.x, cg); cy = fmaf(v[u], ya.y, cy);
+            sg = fmaf(v[u], ys.x, sg); sy_ = fmaf(v[u], ys.y, sy_);
+        }
+        if (lane < NU) {
+            const float4 xa = sA[xv * NTP + NT + 2 + dj - lane], xs = sS[xv * NTP + NT + 2 + dj - lane];
+            red[18 + 4 * q][lane] = xa.y * cg;                   // fx (Gx, G)
+            red[19 + 4 * q][lane] = xa.x * cy;                   // fy (G, Gy)
+            red[20 + 4 * q][lane] = fmaf(xs.y, cg, xa.y * sg);   // d/dsigma
+            red[21 + 4 * q][lane] = fmaf(xs.x, cy, xa.x * sy_);
+        }
+    }
+    __syncwarp();
+    if (lane < 16) row[18 + lane] = column_sum(red[18 + lane], NU);
+    if (lane == 0) row[34] = __int_as_float((xmaj ? 1 : 0) | (sx > 0 ? 2 : 0) | (sy > 0 ? 4 : 0));
+    __syncwarp();
+}
+
+constexpr int kBwV = 12;  // y-vectors per union row: P's four, two per neighbour
+
+// Scatter of one edgel's cotangents onto the pixel gradient, by a whole
+// warp: grad I(u) += sum over the five points and their filters of
+// X_f(q) V_f(p), V_f = the y taps weighted by the point's cotangents.  All
+// five windows lie in the (NT+2) x (NT+2) union window around the edgel's
+// pixel; lane c takes union column c and holds the x taps of the five points
+// there (12 values), lane r first stages the y-vectors of union row r in
+// shared memory, then each union row is added with one vector reduction
+// (red.global.add.f32) per lane.  The grid pixels outside the image are the
+// zero padding and receive nothing.
+template <int R>
+__device__ __forceinline__ void scatter_edgel_warp(const BwImage& im, int rho, int kap, int lane, const float4* sA,
+                                                   const float* g, float4 (*sV)[kBwV / 4])
+{
+    constexpr int NT = 2 * R + 3, NTP = NT + 4, NU = NT + 2;
+    const int bits = __float_as_int(g[17]);
+    const bool xmaj = bits & 1;
+    const int sx = (bits & 2) ? 1 : -1, sy = (bits & 4) ? 1 : -1;
+    const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+    const int pr[5] = {rho, rho + ar, rho + sy, rho - ar, rho - sy};  // P, A+, D+, A-, D-
+    const int pc[5] = {kap, kap + ac, kap + sx, kap - ac, kap - sx};
+    const int i = rho >> 1, j = kap >> 1;
+    float4 xP = make_float4(0.f, 0.f, 0.f, 0.f);
+    float2 xN[4];
+    float4 v0 = make_float4(0.f, 0.f, 0.f, 0.f), v1 = v0, v2 = v0;
+    const int l = lane < NU ? lane : NU - 1;  // lanes past the window repeat the last column (unused)
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        int xv, yv;
+        variants(pr[q], pc[q], &xv, &yv);
+        const int di = (pr[q] >> 1) - i, dj = (pc[q] >> 1) - j;
+        // padded entries: x tap of union column l = NT + 2 + dj - l, y tap of union row l = NT + 2 + di - l
+        const float4 x = sA[xv * NTP + NT + 2 + dj - l];
+        const float4 y = sA[yv * NTP + NT + 2 + di - l];
+        if (q == 0) {
+            xP = x;
+            v0.x = g[1] * y.y + g[4] * y.z + g[8] * y.w;  // G    x (fy, fyy, fyyy)
+            v0.y = g[0] * y.x + g[3] * y.y + g[6] * y.z;  // Gx   x (fx, fxy, fxyy)
+            v0.z = g[2] * y.x + g[5] * y.y;               // Gxx  x (fxx, fxxy)
+            v0.w = g[7] * y.x;                            // Gxxx x fxxx
+        } else {
+            xN[q - 1] = make_float2(x.x, x.y);
+            const float a = g[8 + 2 * q] * y.y, b = g[7 + 2 * q] * y.x;  // G x fy, Gx x fx at the neighbour
+            if (q == 1) { v1.x = a; v1.y = b; }
+            else if (q == 2) { v1.z = a; v1.w = b; }
+            else if (q == 3) { v2.x = a; v2.y = b; }
+            else { v2.z = a; v2.w = b; }
+        }
+    }
+    if (lane < NU) {
+        sV[lane][0] = v0;
+        sV[lane][1] = v1;
+        sV[lane][2] = v2;
+    }
+    __syncwarp();
+    const int x = j - R - 2 + lane;
+    const bool okx = lane < NU && x >= 0 && x < im.W;
+    float* out = im.gpix + x;
+    for (int r = 0; r < NU; ++r) {
+        const int y = i - R - 2 + r;
+        const float4 a = sV[r][0], b = sV[r][1], c = sV[r][2];
+        float v = xP.x * a.x;
+        v = fmaf(xP.y, a.y, v);
+        v = fmaf(xP.z, a.z, v);
+        v = fmaf(xP.w, a.w, v);
+        v = fmaf(xN[0].x, b.x, v);
+        v = fmaf(xN[0].y, b.y, v);
+        v = fmaf(xN[1].x, b.z, v);
+        v = fmaf(xN[1].y, b.w, v);
+        v = fmaf(xN[2].x, c.x, v);
+        v = fmaf(xN[2].y, c.y, v);
+        v = fmaf(xN[3].x, c.z, v);
+        v = fmaf(xN[3].y, c.w, v);
+        if (okx && (unsigned)y < (unsigned)im.H) atomicAdd(out + (long long)y * im.W, v);
+    }
+    __syncwarp();
+}
+
+// bw_adjoint: a CTA of four warps owns 128 consecutive edgels.  Phase 1:
+// each warp evaluates its 32 edgels one after another (eval_edgel_warp).
+// Phase 2: one thread per edgel runs the chain rule.  The peak fit's
+// cancellations (fp - fm, fp + fm - 2f) and the third-order vector
+// (TIx, TIy) are formed in FP64, as in the forward; the rest is FP32.
+// Phase 3: each warp scatters its 32 edgels' cotangents onto the pixel
+// gradient (scatter_edgel_warp), which the host cleared beforehand.
 template <int R>
 __global__ void __launch_bounds__(kBwAdjThreads) bw_adjoint(const __grid_constant__ BwParams p)
 {
-    constexpr int NT = 2 * R + 3;
-    __shared__ float4 sA[3 * NT], sS[3 * NT];
-    build_tables<R>(p, sA, sS);
+    constexpr int NT = 2 * R + 3, NTP = NT + 4;
+    __shared__ float4 sA[3 * NTP], sS[3 * NTP];
+    __shared__ float sVal[kBwAdjThreads][kValsPad];
+    __shared__ float sRed[kBwAdjThreads / 32][kNVal][kRedPad];
+    __shared__ float4 sV[kBwAdjThreads / 32][NT + 2][kBwV / 4];
+    build_tables_padded<R>(p, sA, sS);
     __syncthreads();
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     const int e = blockIdx.x * blockDim.x + threadIdx.x;
+    // each lane resolves its own edgel's image and 2x-grid point
+    int my_k = 0, my_rho = 0, my_kap = 0;
+    if (e < p.n_edgels) {
+        my_k = find_image(p.n_img, e, [&](int i) { return p.img[i].edgel_base; });
+        const BwImage& im = p.img[my_k];
+        const int gi = im.gidx[e - im.edgel_base], W2 = 2 * im.W;
+        my_rho = gi / W2;
+        my_kap = gi - my_rho * W2;
+    }
+    // ---- phase 1: warp-cooperative evaluation, one edgel at a time ----
+    const int ebase = blockIdx.x * blockDim.x + wid * 32;
+    const int nw = min(32, p.n_edgels - ebase);
+    for (int jj = 0; jj < nw; ++jj) {
+        const int k = __shfl_sync(0xffffffffu, my_k, jj);
+        const int rho = __shfl_sync(0xffffffffu, my_rho, jj), kap = __shfl_sync(0xffffffffu, my_kap, jj);
+        eval_edgel_warp<R>(p.img[k], rho, kap, lane, sA, sS, sRed[wid], sVal[wid * 32 + jj]);
+    }
+    __syncthreads();
+    // ---- phase 2: the chain rule, one thread per edgel ----
     double gsig = 0.0;
     if (e < p.n_edgels) {
-        const int k = find_image(p.n_img, e, [&](int i) { return p.img[i].edgel_base; });
-        const BwImage& im = p.img[k];
+        const BwImage& im = p.img[my_k];
         const int local = e - im.edgel_base;
-        const int W2 = 2 * im.W;
-        const int gi = im.gidx[local];
-        const int rho = gi / W2, kap = gi - (gi / W2) * W2;
-        double go[4];
+        const float* row = sVal[threadIdx.x];
+        float go[4];
         if (p.out_f64) {
             const double* g = (const double*)im.gout + 4LL * local;
-            go[0] = g[0]; go[1] = g[1]; go[2] = g[2]; go[3] = g[3];
+            go[0] = (float)g[0]; go[1] = (float)g[1]; go[2] = (float)g[2]; go[3] = (float)g[3];
         } else {
             const float* g = (const float*)im.gout + 4LL * local;
             go[0] = g[0]; go[1] = g[1]; go[2] = g[2]; go[3] = g[3];
         }
-        float d[9], ds[9];
-        eval_point<R, true>(im, rho, kap, sA, sS, d, ds);
-        // the frozen sector (cpu_toed.cpp:415-462 in closed form)
-        const bool xmaj = fabsf(d[0]) >= fabsf(d[1]);
-        const int sx = d[0] >= 0.f ? 1 : -1, sy = d[1] >= 0.f ? 1 : -1;
-        const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
-        const int nr[4] = {rho + ar, rho + sy, rho - ar, rho - sy};  // A+, D+, A-, D-
-        const int nc[4] = {kap + ac, kap + sx, kap - ac, kap - sx};
-        float nd[4][2], nds[4][2];
+        const int bits = __float_as_int(row[34]);
+        const bool xmaj = bits & 1;
+        const int sx = (bits & 2) ? 1 : -1, sy = (bits & 4) ? 1 : -1;
+        const float fx = row[0], fy = row[1], fxx = row[2], fxy = row[3], fyy = row[4], fxxy = row[5],
+                    fxyy = row[6], fxxx = row[7], fyyy = row[8];
+        float nd[4][2], M[4];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) eval_point<R, false>(im, nr[q], nc[q], sA, sS, nd[q], nds[q]);
-
-        // ---- forward values in FP64 ----
-        const double fx = d[0], fy = d[1], fxx = d[2], fxy = d[3], fyy = d[4], fxxy = d[5], fxyy = d[6],
-                     fxxx = d[7], fyyy = d[8];
-        const double m = sqrt(fx * fx + fy * fy);
-        const double nx = fx / m, ny = fy / m;
-        const double c = (double)(sx * sy);
-        const double t = xmaj ? c * fy / fx : c * fx / fy;  // slope |ny|/|nx| or |nx|/|ny|
-        double M[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) M[q] = sqrt((double)nd[q][0] * nd[q][0] + (double)nd[q][1] * nd[q][1]);
-        const double fp = M[0] * (1.0 - t) + M[1] * t, fm = M[2] * (1.0 - t) + M[3] * t;
-        const double num = fp - fm, den = fm + fp - 2.0 * m;
-        const double S = sqrt(1.0 + t * t);
-        const double sst = -num * S / (2.0 * den);
+        for (int q = 0; q < 4; ++q) {
+            nd[q][0] = row[18 + 4 * q];
+            nd[q][1] = row[19 + 4 * q];
+            M[q] = sqrtf(nd[q][0] * nd[q][0] + nd[q][1] * nd[q][1]);
+        }
+        // ---- forward values ----
+        const float m = sqrtf(fx * fx + fy * fy);
+        const float rm = 1.f / m;
+        const float nx = fx * rm, ny = fy * rm;
+        const float c = (float)(sx * sy);
+        const float t = xmaj ? c * fy / fx : c * fx / fy;  // slope |ny|/|nx| or |nx|/|ny|
+        float num, den;
+        {
+            const double td = t;
+            const double fp = (double)M[0] * (1.0 - td) + (double)M[1] * td;
+            const double fm = (double)M[2] * (1.0 - td) + (double)M[3] * td;
+            num = (float)(fp - fm);
+            den = (float)(fm + fp - 2.0 * (double)m);
+        }
+        const float rden = 1.f / den;
+        const float S = sqrtf(1.f + t * t);
+        const float sst = -0.5f * num * S * rden;
         // ---- reverse: position, strength ----
-        const double g_sst = 0.5 * (go[0] * nx + go[1] * ny);
-        double g_nx = 0.5 * go[0] * sst, g_ny = 0.5 * go[1] * sst;
-        const double g_maxf = go[3];  // strength = |max_f| |n| = max_f (max_f > 0 at a maximum)
-        const double g_num = g_sst * (-S / (2.0 * den)) + g_maxf * (-num / (4.0 * den));
-        const double g_den = g_sst * (num * S / (2.0 * den * den)) + g_maxf * (num * num / (8.0 * den * den));
-        double g_t = g_sst * (-num / (2.0 * den)) * t / S;
-        double g_m = g_maxf - 2.0 * g_den;
-        const double g_fp = g_num + g_den, g_fm = -g_num + g_den;
-        const double gM[4] = {g_fp * (1.0 - t), g_fp * t, g_fm * (1.0 - t), g_fm * t};
+        const float g_sst = 0.5f * (go[0] * nx + go[1] * ny);
+        const float g_nx = 0.5f * go[0] * sst, g_ny = 0.5f * go[1] * sst;
+        const float g_maxf = go[3];  // strength = |max_f| |n| = max_f (max_f > 0 at a maximum)
+        const float g_num = -0.5f * S * rden * g_sst - 0.25f * num * rden * g_maxf;
+        const float g_den = 0.5f * num * S * rden * rden * g_sst + 0.125f * num * num * rden * rden * g_maxf;
+        float g_t = g_sst * (-0.5f * num * rden) * t / S;
+        const float g_m = g_maxf - 2.f * g_den;
+        const float g_fp = g_num + g_den, g_fm = -g_num + g_den;
+        const float gM[4] = {g_fp * (1.f - t), g_fp * t, g_fm * (1.f - t), g_fm * t};
         g_t += g_fp * (M[1] - M[0]) + g_fm * (M[3] - M[2]);
-        double gfx = 0.0, gfy = 0.0;
+        float gfx = 0.f, gfy = 0.f;
         if (xmaj) {
             gfx += g_t * (-t / fx);
             gfy += g_t * (c / fx);
@@ -214,184 +382,83 @@ __global__ void __launch_bounds__(kBwAdjThreads) bw_adjoint(const __grid_constan
             gfx += g_t * (c / fy);
             gfy += g_t * (-t / fy);
         }
-        const double m3 = m * m * m;
-        gfx += g_nx * (1.0 / m - fx * fx / m3) + g_ny * (-fx * fy / m3) + g_m * fx / m;
-        gfy += g_nx * (-fx * fy / m3) + g_ny * (1.0 / m - fy * fy / m3) + g_m * fy / m;
+        const float rm3 = rm * rm * rm;
+        gfx += g_nx * (rm - fx * fx * rm3) + g_ny * (-fx * fy * rm3) + g_m * fx * rm;
+        gfy += g_nx * (-fx * fy * rm3) + g_ny * (rm - fy * fy * rm3) + g_m * fy * rm;
         // ---- reverse: orientation atan2(TIx, -TIy) (cpu_toed.cpp:227-232) ----
-        const double TIx = fx * (2 * fxx * fxx + 2 * fxy * fxy) + fy * (2 * fxx * fxy + 2 * fyy * fxy) +
-                           2 * fx * fy * fxxy + fy * fy * fxyy + fx * fx * fxxx;
-        const double TIy = fx * (2 * fxx * fxy + 2 * fyy * fxy) + fy * (2 * fyy * fyy + 2 * fxy * fxy) +
-                           2 * fx * fy * fxyy + fx * fx * fxxy + fy * fy * fyyy;
-        const double q2 = TIx * TIx + TIy * TIy;
-        double gP[9];
-        gP[2] = gP[3] = gP[4] = gP[5] = gP[6] = gP[7] = gP[8] = 0.0;
-        if (q2 > 0.0 && go[2] != 0.0) {
-            const double gX = go[2] * (-TIy) / q2, gY = go[2] * TIx / q2;
-            gfx += gX * (2 * fxx * fxx + 2 * fxy * fxy + 2 * fy * fxxy + 2 * fx * fxxx) +
-                   gY * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fy * fxyy + 2 * fx * fxxy);
-            gfy += gX * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fx * fxxy + 2 * fy * fxyy) +
-                   gY * (2 * fyy * fyy + 2 * fxy * fxy + 2 * fx * fxyy + 2 * fy * fyyy);
-            gP[2] = gX * (4 * fx * fxx + 2 * fy * fxy) + gY * (2 * fx * fxy);
-            gP[3] = gX * (4 * fx * fxy + 2 * fy * fxx + 2 * fy * fyy) + gY * (2 * fx * fxx + 2 * fx * fyy + 4 * fy * fxy);
-            gP[4] = gX * (2 * fy * fxy) + gY * (2 * fx * fxy + 4 * fy * fyy);
-            gP[5] = gX * (2 * fx * fy) + gY * (fx * fx);
-            gP[6] = gX * (fy * fy) + gY * (2 * fx * fy);
-            gP[7] = gX * (fx * fx);
-            gP[8] = gY * (fy * fy);
+        float gP[9];
+        gP[2] = gP[3] = gP[4] = gP[5] = gP[6] = gP[7] = gP[8] = 0.f;
+        if (go[2] != 0.f) {
+            const double dx = fx, dy = fy, dxx = fxx, dxy = fxy, dyy = fyy;
+            const double TIx = dx * (2 * dxx * dxx + 2 * dxy * dxy) + dy * (2 * dxx * dxy + 2 * dyy * dxy) +
+                               2 * dx * dy * (double)fxxy + dy * dy * (double)fxyy + dx * dx * (double)fxxx;
+            const double TIy = dx * (2 * dxx * dxy + 2 * dyy * dxy) + dy * (2 * dyy * dyy + 2 * dxy * dxy) +
+                               2 * dx * dy * (double)fxyy + dx * dx * (double)fxxy + dy * dy * (double)fyyy;
+            const float tix = (float)TIx, tiy = (float)TIy;
+            const float q2 = tix * tix + tiy * tiy;
+            if (q2 > 0.f) {
+                const float gX = go[2] * (-tiy) / q2, gY = go[2] * tix / q2;
+                gfx += gX * (2 * fxx * fxx + 2 * fxy * fxy + 2 * fy * fxxy + 2 * fx * fxxx) +
+                       gY * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fy * fxyy + 2 * fx * fxxy);
+                gfy += gX * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fx * fxxy + 2 * fy * fxyy) +
+                       gY * (2 * fyy * fyy + 2 * fxy * fxy + 2 * fx * fxyy + 2 * fy * fyyy);
+                gP[2] = gX * (4 * fx * fxx + 2 * fy * fxy) + gY * (2 * fx * fxy);
+                gP[3] = gX * (4 * fx * fxy + 2 * fy * fxx + 2 * fy * fyy) + gY * (2 * fx * fxx + 2 * fx * fyy + 4 * fy * fxy);
+                gP[4] = gX * (2 * fy * fxy) + gY * (2 * fx * fxy + 4 * fy * fyy);
+                gP[5] = gX * (2 * fx * fy) + gY * (fx * fx);
+                gP[6] = gX * (fy * fy) + gY * (2 * fx * fy);
+                gP[7] = gX * (fx * fx);
+                gP[8] = gY * (fy * fy);
+            }
         }
         gP[0] = gfx;
         gP[1] = gfy;
-        float* rec = p.cot + (long long)e * kCotW;
+        // the cotangents replace the values in this thread's own row:
+        // [0..8] at P, [9 + 2q, 10 + 2q] = (gx, gy) at neighbour q, [17] sector
+        float* rec = sVal[threadIdx.x];
+        float gs = 0.f;
 #pragma unroll
-        for (int q = 0; q < 9; ++q) {
-            rec[q] = (float)gP[q];
-            gsig += gP[q] * (double)ds[q];
-        }
+        for (int q = 0; q < 9; ++q) gs = fmaf(gP[q], row[9 + q], gs);
+        float gN[8];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-            const double gx = gM[q] * nd[q][0] / M[q], gy = gM[q] * nd[q][1] / M[q];
-            rec[9 + 2 * q] = (float)gx;
-            rec[10 + 2 * q] = (float)gy;
-            gsig += gx * (double)nds[q][0] + gy * (double)nds[q][1];
+            const float rM = gM[q] / M[q];
+            gN[2 * q] = rM * nd[q][0];
+            gN[2 * q + 1] = rM * nd[q][1];
+            gs = fmaf(gN[2 * q], row[20 + 4 * q], fmaf(gN[2 * q + 1], row[21 + 4 * q], gs));
         }
-        rec[17] = __int_as_float((xmaj ? 1 : 0) | (sx > 0 ? 2 : 0) | (sy > 0 ? 4 : 0));
+        const float sec = row[34];
+#pragma unroll
+        for (int q = 0; q < 9; ++q) rec[q] = gP[q];
+#pragma unroll
+        for (int q = 0; q < 8; ++q) rec[9 + q] = gN[q];
+        rec[17] = sec;
+        gsig = gs;
     }
-    // dL/dsigma: warp sums, one FP64 atomic per warp
+    __syncwarp();
+    // ---- phase 3: scatter, a warp per edgel (scatter_edgel_warp) ----
+    for (int jj = 0; jj < nw; ++jj) {
+        const int k = __shfl_sync(0xffffffffu, my_k, jj);
+        const int rho = __shfl_sync(0xffffffffu, my_rho, jj), kap = __shfl_sync(0xffffffffu, my_kap, jj);
+        scatter_edgel_warp<R>(p.img[k], rho, kap, lane, sA, sVal[wid * 32 + jj], sV[wid]);
+    }
+    // dL/dsigma: warp sums in FP64, one FP64 atomic per warp
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) gsig += __shfl_down_sync(0xffffffffu, gsig, o);
-    if ((threadIdx.x & 31) == 0 && gsig != 0.0) atomicAdd(p.gsig, gsig);
-}
-
-__device__ __forceinline__ int lower_bound_i(const int* a, int n, int key)
-{
-    int lo = 0, hi = n;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (a[mid] < key) lo = mid + 1; else hi = mid;
-    }
-    return lo;
-}
-
-template <int R>
-__global__ void __launch_bounds__(256) bw_scatter(const __grid_constant__ BwParams p)
-{
-    constexpr int NT = 2 * R + 3;
-    __shared__ float acc[kBwT][kBwT + 1];
-    __shared__ float4 sA[3 * NT], sS[3 * NT];
-    __shared__ int sList[256];
-    __shared__ int sWarp[8], sRange[2];
-    __shared__ float sV[8][4][NT];
-    build_tables<R>(p, sA, sS);
-    const int t = blockIdx.x;
-    const int k = find_image(p.n_img, t, [&](int i) { return p.img[i].tile_base; });
-    const BwImage& im = p.img[k];
-    const int lt = t - im.tile_base;
-    const int ty = lt / im.ntx, tx = lt - ty * im.ntx;
-    const int i0 = ty * kBwT, j0 = tx * kBwT;
-    const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
-    const int W2 = 2 * im.W;
-    for (int q = tid; q < kBwT * kBwT; q += blockDim.x) acc[q >> 5][q & 31] = 0.f;
-    if (tid == 0) {
-        // edgels whose windows can reach the tile: original row of P in [i0-R-2, i0+kBwT+R+2)
-        const int r0 = max(0, 2 * (i0 - R - 2)), r1 = min(2 * im.H, 2 * (i0 + kBwT + R + 2));
-        sRange[0] = lower_bound_i(im.gidx, im.n, r0 * W2);
-        sRange[1] = lower_bound_i(im.gidx, im.n, r1 * W2);
-    }
-    __syncthreads();
-    const int lo = sRange[0], hi = sRange[1];
-    const int clo = j0 - R - 2, chi = j0 + kBwT + R + 2;
-    for (int base = lo; base < hi; base += 256) {
-        const int e = base + tid;
-        bool rel = false;
-        if (e < hi) {
-            const int kap = im.gidx[e] % W2;
-            const int j = kap >> 1;
-            rel = (j >= clo && j < chi);
-        }
-        const unsigned bal = __ballot_sync(0xffffffffu, rel);
-        if (lane == 0) sWarp[wid] = __popc(bal);
-        __syncthreads();
-        int off = 0, cnt = 0;
-#pragma unroll
-        for (int w = 0; w < 8; ++w) {
-            off += (w < wid) ? sWarp[w] : 0;
-            cnt += sWarp[w];
-        }
-        if (rel) sList[off + __popc(bal & ((1u << lane) - 1u))] = e;
-        __syncthreads();
-        // jobs: (edgel, point) pairs, one warp each
-        for (int job = wid; job < cnt * 5; job += 8) {
-            const int el = sList[job / 5], pt = job - (job / 5) * 5;
-            const int gi = im.gidx[el];
-            int rho = gi / W2, kap = gi - (gi / W2) * W2;
-            const float* rec = p.cot + (long long)(im.edgel_base + el) * kCotW;
-            const int bits = __float_as_int(rec[17]);
-            const bool xmaj = bits & 1;
-            const int sx = (bits & 2) ? 1 : -1, sy = (bits & 4) ? 1 : -1;
-            const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
-            if (pt == 1) { rho += ar; kap += ac; }
-            else if (pt == 2) { rho += sy; kap += sx; }
-            else if (pt == 3) { rho -= ar; kap -= ac; }
-            else if (pt == 4) { rho -= sy; kap -= sx; }
-            int xv, yv;
-            variants(rho, kap, &xv, &yv);
-            // y-vectors per x filter: V_f(p) = sum_k g_k Y_k(p)
-            if (lane < NT) {
-                const float4 y = sA[yv * NT + lane];
-                float v0, v1, v2 = 0.f, v3 = 0.f;
-                if (pt == 0) {
-                    v0 = rec[1] * y.y + rec[4] * y.z + rec[8] * y.w;  // G  x (fy, fyy, fyyy)
-                    v1 = rec[0] * y.x + rec[3] * y.y + rec[6] * y.z;  // Gx x (fx, fxy, fxyy)
-                    v2 = rec[2] * y.x + rec[5] * y.y;                 // Gxx x (fxx, fxxy)
-                    v3 = rec[7] * y.x;                                // Gxxx x fxxx
-                } else {
-                    v0 = rec[8 + 2 * pt] * y.y;  // fy at the neighbour
-                    v1 = rec[7 + 2 * pt] * y.x;  // fx at the neighbour
-                }
-                sV[wid][0][lane] = v0;
-                sV[wid][1][lane] = v1;
-                sV[wid][2][lane] = v2;
-                sV[wid][3][lane] = v3;
-            }
-            __syncwarp();
-            // window rows i - p, cols j - q (p = pp - R - 1) intersected with the tile
-            const int i = rho >> 1, j = kap >> 1;
-            const int pp0 = max(0, i + R + 1 - (i0 + kBwT - 1)), pp1 = min(NT - 1, i + R + 1 - i0);
-            const int qq0 = max(0, j + R + 1 - (j0 + kBwT - 1)), qq1 = min(NT - 1, j + R + 1 - j0);
-            const int nrr = pp1 - pp0 + 1, ncc = qq1 - qq0 + 1;
-            if (nrr > 0 && ncc > 0) {
-                for (int z = lane; z < nrr * ncc; z += 32) {
-                    const int pp = pp0 + z / ncc, qq = qq0 + z - (z / ncc) * ncc;
-                    const float4 x = sA[xv * NT + qq];
-                    const float v = x.x * sV[wid][0][pp] + x.y * sV[wid][1][pp] + x.z * sV[wid][2][pp] +
-                                    x.w * sV[wid][3][pp];
-                    atomicAdd(&acc[i + R + 1 - pp - i0][j + R + 1 - qq - j0], v);
-                }
-            }
-            __syncwarp();
-        }
-        __syncthreads();
-    }
-    for (int q = tid; q < kBwT * kBwT; q += blockDim.x) {
-        const int y = i0 + (q >> 5), x = j0 + (q & 31);
-        if (y < im.H && x < im.W) im.gpix[(long long)y * im.W + x] = acc[q >> 5][q & 31];
-    }
+    if (lane == 0 && gsig != 0.0) atomicAdd(p.gsig, gsig);
 }
 
 template <int R>
 static cudaError_t launch_bw(const BwParams& p, cudaStream_t stream)
 {
     void* args[] = {const_cast<BwParams*>(&p)};
-    cudaError_t e = cudaSuccess;
-    if (p.n_edgels > 0)
-        e = cudaLaunchKernel((const void*)bw_adjoint<R>, dim3((p.n_edgels + kBwAdjThreads - 1) / kBwAdjThreads),
-                             dim3(kBwAdjThreads), args, 0, stream);
-    if (e == cudaSuccess) e = cudaLaunchKernel((const void*)bw_scatter<R>, dim3(p.n_tiles), dim3(256), args, 0, stream);
-    return e;
+    if (p.n_edgels == 0) return cudaSuccess;
+    return cudaLaunchKernel((const void*)bw_adjoint<R>, dim3((p.n_edgels + kBwAdjThreads - 1) / kBwAdjThreads),
+                            dim3(kBwAdjThreads), args, 0, stream);
 }
 
-cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_params* prm, int r, float* cot,
-                            double* gsig, cudaStream_t stream)
+cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_params* prm, int r, double* gsig,
+                            cudaStream_t stream)
 {
     std::unique_ptr<BwParams> pp(new BwParams());
     BwParams& p = *pp;
@@ -416,9 +483,8 @@ cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_para
     p.r = r;
     p.out_f64 = prm->out_dtype == TOED_F64;
     p.n_img = n;
-    p.cot = cot;
     p.gsig = gsig;
-    int edg = 0, tiles = 0;
+    int edg = 0;
     for (int i = 0; i < n; ++i) {
         BwImage& d = p.img[i];
         d.src = items[i].pixels;
@@ -431,14 +497,13 @@ cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_para
         d.dtype = items[i].dtype;
         d.n = items[i].n_edgels;
         d.edgel_base = edg;
-        d.ntx = (d.W + kBwT - 1) / kBwT;
-        d.nty = (d.H + kBwT - 1) / kBwT;
-        d.tile_base = tiles;
         edg += d.n;
-        tiles += d.ntx * d.nty;
     }
     p.n_edgels = edg;
-    p.n_tiles = tiles;
+    for (int i = 0; i < n; ++i) {
+        const cudaError_t e = cudaMemsetAsync(p.img[i].gpix, 0, sizeof(float) * p.img[i].H * p.img[i].W, stream);
+        if (e != cudaSuccess) return e;
+    }
     switch (r) {
     case 1: return launch_bw<1>(p, stream);
     case 2: return launch_bw<2>(p, stream);

@@ -25,9 +25,10 @@ cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
 // the image's base or pitch is not 16-byte aligned.
 void encode_rows_map(CUtensorMap* m, DetImage& d, int radius);
 
-// Enqueue the adjoint kernels (toed_backward.cu); cot: sum(n_edgels) x 18 floats.
-cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_params* prm, int r, float* cot,
-                            double* gsig, cudaStream_t stream);
+// Enqueue the adjoint (toed_backward.cu): clears each item's grad_pixels,
+// then one kernel; dL/dsigma is added into *gsig.
+cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_params* prm, int r, double* gsig,
+                            cudaStream_t stream);
 
 // Scratch of the TO-correction pipeline (owned by the caller's context).
 struct SubScratch {
