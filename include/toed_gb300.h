@@ -187,6 +187,26 @@ toed_status toed_subpix_to_correct_batch(toed_ctx* ctx, const toed_edgemap* maps
 #define TOED_NOALLOC_MAX_EDGELS 262144
 toed_status toed_detect_noalloc(const toed_image* image, const toed_params* params, cudaStream_t stream);
 
+/* Launch-shape autotuning (no counterpart in the reference, whose GPU path
+ * has one fixed launch shape).  toed_autotune times each candidate -- strip
+ * height 14, 30, 62, 126, 254, 510 or 1022 rows, input rows staged by TMA or
+ * by plain loads -- on the caller's batch with CUDA events, `reps` timed runs
+ * after one untimed run each, keeps the fastest in the context for this
+ * radius and precision (later toed_detect_batch calls use it) and returns it.
+ * It is synchronous, runs the detection 14 * (reps + 1) times (the outputs hold
+ * the last run; every candidate gives the same result bit for bit) and is
+ * refused under stream capture.  toed_set_tuning installs a shape (NULL
+ * restores the built-in heuristic). */
+typedef struct toed_tuning {
+    int strip_rows;  /* 16k - 2 for k in 1, 2, 4, ..., 64 */
+    int staging;     /* 1: TMA (when the image allows it), 0: plain loads */
+    float ms;        /* measured time of one detection of the batch (autotune output) */
+} toed_tuning;
+
+toed_status toed_autotune(toed_ctx* ctx, const toed_image* images, int n_images, const toed_params* params,
+                          int reps, cudaStream_t stream, toed_tuning* best);
+toed_status toed_set_tuning(toed_ctx* ctx, const toed_params* params, const toed_tuning* tuning);
+
 /* Measurement hooks (used by bench.py).
  * toed_profile_begin: from now on every detection on `ctx` records a pair of
  * CUDA events just before and just after its fused detection kernel, on the

@@ -240,3 +240,34 @@ def test_cuda_graph_replay(detector, synth, toed):
         n = int(o["count"].item())
         assert n == r["count"] > 20
         assert t.equal(o["edgels"][:n], r["edgels"]) and t.equal(o["index"][:n], r["index"])
+
+
+def test_autotune_and_launch_shapes_agree(toed, synth):
+    """Every launch shape the autotuner may pick gives the same result bit for
+    bit; the autotuner keeps one of them."""
+    t = _torch()
+    det = toed.Detector(0)
+    sizes = [(300, 410), (97, 1000), (700, 64)]
+    imgs = [t.as_tensor(synth.shapes_image(h, w, seed=1300 + k, dtype=np.float32).image).cuda()
+            for k, (h, w) in enumerate(sizes)]
+    prm = toed.make_params(1.5)
+    ref = None
+    for rows in (14, 30, 62, 126, 254, 510, 1022):
+        for staging in (True, False):
+            det.set_tuning(prm, rows, staging)
+            outs = det.alloc_outputs([im.shape for im in imgs])
+            det.detect_into(imgs, outs, prm)
+            t.cuda.synchronize()
+            got = [(int(o["count"].item()), o["edgels"][:int(o["count"].item())].cpu(),
+                    o["index"][:int(o["count"].item())].cpu()) for o in outs]
+            if ref is None:
+                ref = got
+            for (n0, e0, i0), (n1, e1, i1) in zip(ref, got):
+                assert n0 == n1 and t.equal(e0, e1) and t.equal(i0, i1), (rows, staging)
+    det.set_tuning(prm, None)
+    outs = det.alloc_outputs([im.shape for im in imgs])
+    best = det.autotune(imgs, outs, prm, reps=2)
+    assert best["strip_rows"] in (14, 30, 62, 126, 254, 510, 1022) and best["ms"] > 0
+    t.cuda.synchronize()
+    for (n0, e0, i0), o in zip(ref, outs):
+        assert int(o["count"].item()) == n0 and t.equal(o["edgels"][:n0].cpu(), e0)

@@ -38,7 +38,8 @@ C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
     "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
-    "toed_subpix_to_correct_batch", "toed_detect_noalloc", "toed_backward_batch",
+    "toed_subpix_to_correct_batch", "toed_detect_noalloc", "toed_backward_batch", "toed_autotune",
+    "toed_set_tuning",
 ]
 
 
@@ -87,6 +88,10 @@ class toed_subpix_params(ctypes.Structure):
     ]
 
 
+class toed_tuning(ctypes.Structure):
+    _fields_ = [("strip_rows", ctypes.c_int), ("staging", ctypes.c_int), ("ms", ctypes.c_float)]
+
+
 _LIB = None
 
 
@@ -131,6 +136,9 @@ def lib():
         L.toed_subpix_to_correct_batch.argtypes = [vp, ctypes.POINTER(toed_edgemap), ip,
                                                    ctypes.POINTER(toed_subpix_params), vp]
         L.toed_detect_noalloc.argtypes = [ctypes.POINTER(toed_image), ctypes.POINTER(toed_params), vp]
+        L.toed_autotune.argtypes = [vp, ctypes.POINTER(toed_image), ip, ctypes.POINTER(toed_params), ip, vp,
+                                    ctypes.POINTER(toed_tuning)]
+        L.toed_set_tuning.argtypes = [vp, ctypes.POINTER(toed_params), ctypes.POINTER(toed_tuning)]
         L.toed_backward_batch.argtypes = [vp, ctypes.POINTER(toed_grad_image), ip, ctypes.POINTER(toed_params),
                                           vp, vp]
         for name in C_SYMBOLS:
@@ -270,6 +278,24 @@ class Detector:
         s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
         _check(lib().toed_detect_batch(self._ctx, arr, n, ctypes.byref(params),
                                        ctypes.c_void_p(s.cuda_stream)), "toed_detect_batch")
+
+    def autotune(self, images, outs, params: toed_params, reps: int = 3, stream=None) -> dict:
+        """Time every candidate launch shape on this batch and keep the
+        fastest for later calls with the same radius and precision
+        (synchronous; the outputs hold the last run)."""
+        n = len(images)
+        arr = (toed_image * n)(*[self._image_struct(im, o) for im, o in zip(images, outs)])
+        s = stream if stream is not None else self.torch.cuda.current_stream(self.device)
+        best = toed_tuning()
+        _check(lib().toed_autotune(self._ctx, arr, n, ctypes.byref(params), int(reps),
+                                   ctypes.c_void_p(s.cuda_stream), ctypes.byref(best)), "toed_autotune")
+        return {"strip_rows": best.strip_rows, "staging": "tma" if best.staging else "plain", "ms": best.ms}
+
+    def set_tuning(self, params: toed_params, strip_rows=None, staging: bool = True):
+        """Install a launch shape (strip_rows None: the built-in heuristic)."""
+        t = toed_tuning(int(strip_rows), 1 if staging else 0, 0.0) if strip_rows is not None else None
+        _check(lib().toed_set_tuning(self._ctx, ctypes.byref(params), ctypes.byref(t) if t is not None else None),
+               "toed_set_tuning")
 
     def capture(self, images, outs, params: toed_params, warmup: int = 1):
         """Capture detect_into(images, outs, params) in a CUDA graph (the

@@ -147,6 +147,8 @@ struct toed_ctx {
     unsigned char* keep = nullptr;
     long long keep_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
+    // launch shape chosen by toed_autotune per (radius, precision); strip_rows 0 = heuristic
+    toed_tuning tune[TOED_MAX_RADIUS + 1][2] = {};
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
     std::mutex mu;
@@ -275,7 +277,9 @@ extern "C" toed_status toed_reserve(toed_ctx* c, long long max_pixels, long long
     const long long segs = max_pixels / 15 + 2LL * 4096 + (long long)imgs * kSegTile;
     const long long tiles = segs / kSegTile + imgs + 1;
     std::lock_guard<std::mutex> lk(c->mu);
-    toed_status st = ensure_scratch(c, std::max(max_edgels, 1LL), segs, tiles, imgs, nullptr);
+    // staging slack: one reservation block per resident CTA (at most 4 per SM)
+    const long long slack = 4LL * c->num_sms * kStageBlk;
+    toed_status st = ensure_scratch(c, std::max(max_edgels, 1LL) + slack, segs, tiles, imgs, nullptr);
     cudaSetDevice(prev);
     return st;
 }
@@ -301,7 +305,7 @@ static int radius_of(const toed_params* p)
 // still gives every resident CTA several units to balance the queue.
 static int plan_strip_rows(const toed_image* images, int n, long long resident)
 {
-    static const int steps[] = {16, 8, 4, 2, 1};
+    static const int steps[] = {64, 32, 16, 8, 4, 2, 1};
     for (int st : steps) {
         const int S = st * kStepRows - 2;
         long long units = 0;
@@ -313,7 +317,7 @@ static int plan_strip_rows(const toed_image* images, int n, long long resident)
 }
 
 static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                                int r, bool first_chunk, cudaStream_t stream)
+                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr)
 {
     const bool hyb = prm->precision != TOED_FP32;
     DetectEntry ent = detect_entry(r, hyb);
@@ -331,7 +335,9 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     make_taps((double)prm->sigma, r, &p->taps);
     p->thr = prm->threshold;
     p->border = prm->border;
-    p->S = plan_strip_rows(images, n, resident);
+    const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0];
+    const toed_tuning* use = force ? force : (tuned.strip_rows > 0 ? &tuned : nullptr);
+    p->S = use ? use->strip_rows : plan_strip_rows(images, n, resident);
     p->n_img = n;
     p->out_f64 = (prm->out_dtype == TOED_F64) ? 1 : 0;
     p->radius = r;
@@ -354,6 +360,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
         encode_rows_map(&p->tmap[i], d, r);
+        if (use && !use->staging) d.tma = 0;
         const long long nseg = 2LL * im.height * d.nsc;
         d.nseg = nseg;
         units += (long long)d.nsc * d.nsr;
@@ -363,6 +370,9 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     if (units >= (1LL << 31) || tiles >= (1LL << 31)) return TOED_ERR_UNSUPPORTED;
     p->n_units = (int)units;
     p->n_tiles = (int)tiles;
+    // every resident CTA may leave up to one reservation block of staging unused
+    p->stage_blk = kStageBlk;
+    staging += resident * kStageBlk;
     toed_status st = ensure_scratch(c, std::max(staging, 1LL), tiles * kSegTile, tiles, n, stream);
     if (st != TOED_OK) return st;
     p->sc.words = c->words;
@@ -389,8 +399,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     return TOED_OK;
 }
 
-extern "C" toed_status toed_detect_batch(toed_ctx* c, const toed_image* images, int n,
-                                         const toed_params* prm, cudaStream_t stream)
+static toed_status check_batch(const toed_ctx* c, const toed_image* images, int n, const toed_params* prm)
 {
     if (!c || !images || n <= 0 || !prm) return TOED_ERR_INVALID_ARG;
     if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma) || !std::isfinite(prm->threshold)) return TOED_ERR_INVALID_ARG;
@@ -403,17 +412,110 @@ extern "C" toed_status toed_detect_batch(toed_ctx* c, const toed_image* images, 
         toed_status st = check_image(images[i]);
         if (st != TOED_OK) return st;
     }
+    return TOED_OK;
+}
+
+// The batch in chunks of kBatchMax images (caller holds c->mu, device set).
+static toed_status detect_all(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
+                              cudaStream_t stream, const toed_tuning* force = nullptr)
+{
+    const int r = radius_of(prm);
+    toed_status st = TOED_OK;
+    for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
+        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force);
+    return st;
+}
+
+extern "C" toed_status toed_detect_batch(toed_ctx* c, const toed_image* images, int n,
+                                         const toed_params* prm, cudaStream_t stream)
+{
+    toed_status st = check_batch(c, images, n, prm);
+    if (st != TOED_OK) return st;
     int prev = 0;
     TOED_CU(cudaGetDevice(&prev));
     if (prev != c->device) TOED_CU(cudaSetDevice(c->device));
-    toed_status st = TOED_OK;
     {
         std::lock_guard<std::mutex> lk(c->mu);
-        for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
-            st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream);
+        st = detect_all(c, images, n, prm, stream);
     }
     if (prev != c->device) cudaSetDevice(prev);
     return st;
+}
+
+// Times every candidate launch shape on the caller's batch (CUDA events on
+// its stream, after one untimed run each) and keeps the fastest.  The
+// candidates change only how the work is cut and staged -- strip height and
+// TMA vs plain row loads -- never the result, which is the same bit for bit.
+extern "C" toed_status toed_autotune(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
+                                     int reps, cudaStream_t stream, toed_tuning* best)
+{
+    toed_status st = check_batch(c, images, n, prm);
+    if (st != TOED_OK) return st;
+    if (reps < 1) return TOED_ERR_INVALID_ARG;
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    TOED_CU(cudaStreamIsCapturing(stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return TOED_ERR_CAPTURE;
+    const int r = radius_of(prm);
+    const int hyb = prm->precision != TOED_FP32 ? 1 : 0;
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    if (prev != c->device) TOED_CU(cudaSetDevice(c->device));
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    toed_tuning win = {};
+    win.ms = -1.f;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        cudaError_t ce = cudaEventCreate(&e0);
+        if (ce == cudaSuccess) ce = cudaEventCreate(&e1);
+        if (ce != cudaSuccess) {
+            g_last_cuda_error = std::string("autotune: ") + cudaGetErrorString(ce);
+            st = TOED_ERR_CUDA;
+        }
+        static const int steps[] = {1, 2, 4, 8, 16, 32, 64};
+        for (int staging = 1; staging >= 0 && st == TOED_OK; --staging)
+            for (int k = 0; k < 7 && st == TOED_OK; ++k) {
+                toed_tuning cand = {steps[k] * kStepRows - 2, staging, 0.f};
+                st = detect_all(c, images, n, prm, stream, &cand);  // untimed: scratch, caches
+                if (st != TOED_OK) break;
+                ce = cudaEventRecord(e0, stream);
+                for (int i = 0; i < reps && st == TOED_OK && ce == cudaSuccess; ++i)
+                    st = detect_all(c, images, n, prm, stream, &cand);
+                if (ce == cudaSuccess) ce = cudaEventRecord(e1, stream);
+                if (ce == cudaSuccess) ce = cudaEventSynchronize(e1);
+                float ms = 0.f;
+                if (ce == cudaSuccess) ce = cudaEventElapsedTime(&ms, e0, e1);
+                if (ce != cudaSuccess) {
+                    g_last_cuda_error = std::string("autotune: ") + cudaGetErrorString(ce);
+                    st = TOED_ERR_CUDA;
+                    break;
+                }
+                cand.ms = ms / (float)reps;
+                if (st == TOED_OK && (win.ms < 0.f || cand.ms < win.ms)) win = cand;
+            }
+        if (st == TOED_OK) c->tune[r][hyb] = win;
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    if (prev != c->device) cudaSetDevice(prev);
+    if (st == TOED_OK && best) *best = win;
+    return st;
+}
+
+extern "C" toed_status toed_set_tuning(toed_ctx* c, const toed_params* prm, const toed_tuning* t)
+{
+    if (!c || !prm) return TOED_ERR_INVALID_ARG;
+    const int r = radius_of(prm);
+    if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
+    toed_tuning v = {};
+    if (t) {
+        if (t->strip_rows < kStepRows - 2 || (t->strip_rows + 2) % kStepRows != 0 || t->strip_rows > 64 * kStepRows - 2 ||
+            (t->staging != 0 && t->staging != 1))
+            return TOED_ERR_INVALID_ARG;
+        v = *t;
+    }
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->tune[r][prm->precision != TOED_FP32 ? 1 : 0] = v;
+    return TOED_OK;
 }
 
 extern "C" toed_status toed_detect(toed_ctx* c, const toed_image* image, const toed_params* prm,

@@ -25,6 +25,7 @@ constexpr int kInner = kExt - 2;                   // 30 output columns per stri
 constexpr int kStepRows = 16;                      // original rows per sliding step (B)
 constexpr int kColRows = 8;                        // rows per column-pass thread (register blocking)
 constexpr int kSegTile = 1024;                     // segments per ordering-pass tile
+constexpr int kStageBlk = 256;                     // staging records a CTA reserves at a time
 
 // 1-D taps, index k <-> offset x = k - (r+1) (+0.5 for the shifted set).
 // Filters: 0 G, 1 Gx, 2 Gxx, 3 Gxxx, 4..7 the same shifted by +0.5.
@@ -74,6 +75,7 @@ struct BatchParams {
     int n_tiles;
     int out_f64;
     int radius;
+    int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
     Scratch sc;
     DetImage img[kBatchMax];
 };

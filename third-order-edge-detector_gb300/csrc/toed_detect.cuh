@@ -5,22 +5,29 @@
 // (32 with a one-pixel ring) by S output rows.  The CTA slides down the strip
 // in steps of B = 16 rows, keeping everything on chip:
 //
-//   1. load B new input rows (+ halo) into shared memory, converting to FP32;
-//   2. row pass: 12 horizontal 1-D filter responses per (row, column) --
-//      G/Gx/Gxx/Gxxx, each truncated to 2r+1 taps (T), full 2r+3 taps (F) and
-//      half-pixel shifted (S) -- into a sliding window of B+2r+3 rows;
+//   1. B new input rows (+ halo) arrive by TMA (or plain loads) and are
+//      converted to FP32 into a ring of input rows;
+//   2. row pass: the six horizontal responses the dense first derivatives
+//      need -- G and Gx, each truncated to 2r+1 taps (T), full 2r+3 taps (F)
+//      and half-pixel shifted (S) -- into a ring of row-pass rows;
 //   3. column pass: Ix and Iy at the four half-pixel sub-grids (the 2x grid
-//      of the reference, cpu_toed.cpp:204-355) for the B new rows, and
-//      |grad I| -- only the two first derivatives are evaluated densely;
-//   4. subpixel NMS along the gradient with the reference's 8-sector
-//      interpolation, max test and parabola fit (cpu_toed.cpp:399-495),
-//      decided in FP32; survivors are compacted with warp ballots in
-//      row-major order;
-//   5. per edgel only: the seven higher derivatives from the row-pass window,
-//      the third-order orientation (cpu_toed.cpp:227-232) and the peak fit
-//      in FP64 (HYBRID) or FP32; the record goes to a staging area and the
+//      of the reference, cpu_toed.cpp:204-355) for the B new rows, |grad I|,
+//      and the threshold test as one ballot mask per (2x row, column parity);
+//   4. the points above the threshold listed in row-major order; subpixel
+//      NMS along the gradient with the reference's 8-sector interpolation,
+//      max test and parabola fit (cpu_toed.cpp:399-495), decided in FP32;
+//      survivors compacted in order;
+//   5. per edgel only: the seven higher derivatives -- Gxx / Gxxx row
+//      responses recomputed from the input ring for the edgel's window rows,
+//      a thread per (edgel, row) -- then the third-order orientation
+//      (cpu_toed.cpp:227-232) and the peak fit with FP64 where they cancel
+//      (HYBRID) or in FP32; records are deferred in a ring and finished by
+//      all threads at once; the staged record goes to a staging area and the
 //      row's {offset, count} to the row-segment table that the ordering pass
 //      (toed_finalize.cu) turns into the reference's row-major edgel list.
+//
+// Both rings have a power-of-two number of rows and are indexed by absolute
+// row, so sliding the window moves no data.
 //
 // Compared with the reference kernel (direct 17x17 and 19x19 sums of nine
 // derivatives at every point, gpu_convolve.cu:114-131) this evaluates the
@@ -38,25 +45,25 @@ struct Cfg {
     static constexpr int B = kStepRows;
     static constexpr int NT = 2 * R + 3;            // taps of a full / shifted filter
     static constexpr int NIN = kExt + 2 * R + 2;    // input columns held per row
-    static constexpr int HS = B + 2 * R + 3;        // row-pass window slots
+    static constexpr int HS = B + 2 * R + 3;        // live rows of the row-pass window
+    static constexpr int RING = HS;                 // ring rows (input and row-pass rings)
     static constexpr int MS = 2 * B + 2;            // 2x-grid rows held for NMS
     static constexpr int NMS_ROWS = 2 * B;          // 2x-grid rows decided per step
     static constexpr int MAXC = NMS_ROWS * 2 * kInner;
     static constexpr int RECW = 21;                 // words per deferred edgel record (odd: no bank conflicts)
-    // the input rows and the per-step point list are never live together
-    static constexpr size_t sz_in = sizeof(float) * HS * NIN;
-    static constexpr size_t sz_list = sizeof(unsigned) * MAXC;
     static constexpr size_t sz_raw = kStepRows * 256;  // one TMA box: 16 rows x <= 256 bytes
     static constexpr size_t off_raw = 0;
     static constexpr size_t off_mbar = off_raw + sz_raw;
-    static constexpr size_t off_in = off_mbar + 16;
-    static constexpr size_t off_P = align_up(off_in + (sz_in > sz_list ? sz_in : sz_list), 16);
-    static constexpr size_t off_mag = off_P + sizeof(float2) * 6 * HS * kExt;
-    static constexpr size_t off_fxy = off_mag + sizeof(float) * MS * 64;
-    static constexpr size_t off_tab = off_fxy + sizeof(float2) * MS * 64;
-    static constexpr size_t off_misc = off_tab + sizeof(float4) * 3 * NT;
+    static constexpr size_t off_in = align_up(off_mbar + 16, 16);
+    static constexpr size_t off_P = align_up(off_in + sizeof(float) * RING * NIN, 16);
+    static constexpr size_t off_fxy = off_P + sizeof(float2) * 6 * RING * kExt;
+    static constexpr size_t off_mask = off_fxy + sizeof(float2) * MS * 64;
+    static constexpr size_t off_list = off_mask + sizeof(unsigned) * MS * 2;
+    static constexpr size_t off_tab = align_up(off_list + sizeof(unsigned) * MAXC, 16);
+    static constexpr size_t off_misc = align_up(off_tab + sizeof(float4) * 3 * NT, 16);
     static constexpr size_t off_rec = off_misc + sizeof(int) * 128;
     // deferred-edgel ring: as many records as keep two CTAs per SM (<= 112 KB each)
+    static constexpr int MINB = 2;
     static constexpr size_t budget = 112 * 1024;
     static constexpr int NREC_FIT = off_rec < budget ? (int)((budget - off_rec) / (RECW * 4) / 32 * 32) : 0;
     static constexpr int NREC = NREC_FIT > 256 ? 256 : (NREC_FIT < 64 ? 64 : NREC_FIT);
@@ -123,22 +130,27 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase)
     return false;
 }
 
+// Ring row of x for 0 <= x < 2 * N (every ring index the kernel forms).
+template <int N>
+__device__ __forceinline__ int ring_wrap(int x) { return x >= N ? x - N : x; }
+
 // ---------------------------------------------------------------------------
-// Row pass: for input rows [in0, in0+nrows) of sIn write window slots
-// [slot0, slot0+nrows).  Item = (row, pair of ext columns 2k, 2k+1).
+// Row pass: for ring rows p0, p0+1, ... (mod RING; nrows of them) of the
+// input ring write the same rows of the row-pass ring.  Item = (row, pair of ext columns 2k, 2k+1).
 // Planes: 0 PT=(T_G,T_Gx) 1 PF=(F_G,F_Gx) 2 PS=(S_G,S_Gx)
-//         3 QT=(T_Gxx,T_Gxxx) 4 QF 5 QS, each [HS][32] float2.
+//         3 QT=(T_Gxx,T_Gxxx) 4 QF 5 QS, each [RING][32] float2.
 // Convolution direction as the reference: out(x) = sum_q in(x-q) X(q).
 // ---------------------------------------------------------------------------
 template <int R>
-__device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int in0, int nrows, int slot0,
+__device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int p0, int nrows,
                                          float2* __restrict__ sP, const TapBlock& tp)
 {
     using C = Cfg<R>;
     constexpr int NV = 2 * R + 4;
     for (int item = threadIdx.x; item < nrows * 16; item += kThreads) {
         const int i = item >> 4, k = item & 15;
-        const float2* src = reinterpret_cast<const float2*>(sIn + (in0 + i) * C::NIN + 2 * k);
+        const int ph = ring_wrap<C::RING>(p0 + i);
+        const float2* src = reinterpret_cast<const float2*>(sIn + ph * C::NIN + 2 * k);
         float v[NV];
 #pragma unroll
         for (int t = 0; t < NV / 2; ++t) {
@@ -185,32 +197,35 @@ __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int in0,
             o_[o][4] = sG;  o_[o][5] = sGx;  o_[o][6] = tGxx; o_[o][7] = tGxxx;
             o_[o][8] = fGxx; o_[o][9] = fGxxx; o_[o][10] = sGxx; o_[o][11] = sGxxx;
         }
-        const int slot = slot0 + i;
 #pragma unroll
         for (int a = 0; a < 6; ++a) {
-            float4* dst = reinterpret_cast<float4*>(sP + (a * C::HS + slot) * kExt + 2 * k);
+            float4* dst = reinterpret_cast<float4*>(sP + (a * C::RING + ph) * kExt + 2 * k);
             *dst = make_float4(o_[0][2 * a], o_[0][2 * a + 1], o_[1][2 * a], o_[1][2 * a + 1]);
         }
     }
 }
 
 // ---------------------------------------------------------------------------
-// Column pass for one (column, sub-grid, 8-row group): Ix and Iy.
+// Column pass for one (column, sub-grid, 8-row group): Ix and Iy.  Window
+// rows are read from the row-pass ring: logical slot h <-> ring row
+// (rb + h) mod RING, rb the ring row of slot 0 at this step.
 // V = 0: unshifted y taps truncated to 2r+1 (sub-grid (0,0), cpu_toed.cpp:205-221)
 // V = 1: unshifted y taps, full 2r+3 (sub-grid (0,1/2), :246-262)
 // V = 2: shifted y taps (sub-grids (1/2, .), :287-344)
 // ---------------------------------------------------------------------------
 template <int R, int V>
-__device__ __forceinline__ void col_pass(const float2* __restrict__ P, int g, int lane,
+__device__ __forceinline__ void col_pass(const float2* __restrict__ P, int rb, int g, int lane,
                                          const TapBlock& tp, float (&fx)[kColRows],
                                          float (&fy)[kColRows])
 {
+    using C = Cfg<R>;
     constexpr int YF = (V == 2) ? 4 : 0;
 #pragma unroll
     for (int o = 0; o < kColRows; ++o) { fx[o] = 0.f; fy[o] = 0.f; }
+    const int r0 = rb + g * kColRows + 1;
 #pragma unroll
     for (int t = 0; t < kColRows + 2 * R + 2; ++t) {
-        const float2 h = P[(g * kColRows + 1 + t) * kExt + lane];
+        const float2 h = P[ring_wrap<C::RING>(r0 + t) * kExt + lane];
 #pragma unroll
         for (int o = 0; o < kColRows; ++o) {
             const int p = o + R + 1 - t;
@@ -223,6 +238,10 @@ __device__ __forceinline__ void col_pass(const float2* __restrict__ P, int g, in
     }
 }
 
+// |grad I| at a 2x-grid point from its (Ix, Iy); the column pass, the NMS
+// decision and the per-edgel epilogue all use this one expression.
+__device__ __forceinline__ float grad_mag(float2 g) { return sqrt_approx(fmaf(g.x, g.x, g.y * g.y)); }
+
 // NMS evaluation at 2x-grid slot (m, c) of the step window.  Shared by the
 // decision stage and the per-edgel epilogue so both see identical numbers.
 struct NmsEval {
@@ -230,14 +249,13 @@ struct NmsEval {
     bool cand;
 };
 
-__device__ __forceinline__ NmsEval nms_eval(const float* __restrict__ sMag,
-                                            const float2* __restrict__ sFxy, int m, int c, float thr)
+__device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int m, int c, float thr)
 {
     NmsEval r;
     r.cand = false;
-    r.mv = sMag[m * 64 + c];
-    if (!(r.mv > thr)) return r;  // cpu_toed.cpp:403 (also rejects NaN)
     const float2 g = sFxy[m * 64 + c];
+    r.mv = grad_mag(g);
+    if (!(r.mv > thr)) return r;  // cpu_toed.cpp:403 (also rejects NaN)
     r.gx = g.x;
     r.gy = g.y;
     if (fabsf(g.x) < 10e-6f && fabsf(g.y) < 10e-6f) return r;  // :407
@@ -250,10 +268,10 @@ __device__ __forceinline__ NmsEval nms_eval(const float* __restrict__ sMag,
     const int sx = (g.x >= 0.f) ? 1 : -1, sy = (g.y >= 0.f) ? 1 : -1;
     r.slope = xmaj ? __fdividef(fabsf(r.ny), fabsf(r.nx)) : __fdividef(fabsf(r.nx), fabsf(r.ny));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
-    r.Map = sMag[(m + ar) * 64 + c + ac];
-    r.Mdp = sMag[(m + sy) * 64 + c + sx];
-    r.Mam = sMag[(m - ar) * 64 + c - ac];
-    r.Mdm = sMag[(m - sy) * 64 + c - sx];
+    r.Map = grad_mag(sFxy[(m + ar) * 64 + c + ac]);
+    r.Mdp = grad_mag(sFxy[(m + sy) * 64 + c + sx]);
+    r.Mam = grad_mag(sFxy[(m - ar) * 64 + c - ac]);
+    r.Mdm = grad_mag(sFxy[(m - sy) * 64 + c - sx]);
     const float fp = r.Map * (1.f - r.slope) + r.Mdp * r.slope;
     const float fm = r.Mam * (1.f - r.slope) + r.Mdm * r.slope;
     const float mv = r.mv;
@@ -270,7 +288,7 @@ __device__ __forceinline__ NmsEval nms_eval(const float* __restrict__ sMag,
 // orientation (cpu_toed.cpp:227-232, FP64 in HYB mode), then the staged
 // output record (x, y, orientation, strength) at its reserved slot.
 template <bool HYB>
-__device__ __forceinline__ void finish_edgel(const float* __restrict__ rc, const Scratch& sc)
+__device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Scratch& sc)
 {
     const float gx = rc[0], gy = rc[1], mv = rc[2], nx = rc[3], ny = rc[4], sl = rc[5];
     const float Map = rc[6], Mdp = rc[7], Mam = rc[8], Mdm = rc[9];
@@ -281,18 +299,24 @@ __device__ __forceinline__ void finish_edgel(const float* __restrict__ rc, const
     double x, y;
     float ori, str;
     if (HYB) {
-        const double s1 = sl;
-        const double fp = (double)Map * (1.0 - s1) + (double)Mdp * s1;
-        const double fm = (double)Mam * (1.0 - s1) + (double)Mdm * s1;
-        const double num = fp - fm, den = fm + fp - 2.0 * (double)mv;
-        const double ss = (double)sqrtf(1.f + sl * sl);
-        const double rden = 1.0 / den;
-        const double sst = -0.5 * num * ss * rden;             // s* = -B / (2A)
-        const double maxf = (double)mv - 0.125 * num * num * rden;  // A s*^2 + B s* + C
-        x = ((double)Gc + sst * (double)nx - 1.0) * 0.5;       // (pos - 1) / 2, cpu_toed.cpp:516
-        y = ((double)Gr + sst * (double)ny - 1.0) * 0.5;
-        const float mf = (float)maxf;
-        str = sqrtf((mf * nx) * (mf * nx) + (mf * ny) * (mf * ny));
+        // fp - fm and fm + fp - 2f cancel: formed exactly from the FP32
+        // inputs in FP64, then the well-conditioned rest in FP32
+        float num, den;
+        {
+            const double s1 = sl, c1 = 1.0 - s1;
+            const double fp = (double)Map * c1 + (double)Mdp * s1;
+            const double fm = (double)Mam * c1 + (double)Mdm * s1;
+            num = (float)(fp - fm);
+            den = (float)(fm + fp - 2.0 * (double)mv);
+        }
+        const float ss = sqrtf(1.f + sl * sl);
+        const float sst = -0.5f * num * ss / den;           // s* = -B / (2A)
+        const float maxf = mv - 0.125f * num * num / den;   // A s*^2 + B s* + C
+        // (pos - 1) / 2, cpu_toed.cpp:516; the grid coordinate is exact, the
+        // subpixel offset is added in FP64 so that large coordinates keep it
+        x = (double)(0.5f * (float)(Gc - 1)) + (double)(0.5f * sst * nx);
+        y = (double)(0.5f * (float)(Gr - 1)) + (double)(0.5f * sst * ny);
+        str = sqrtf((maxf * nx) * (maxf * nx) + (maxf * ny) * (maxf * ny));
         const double dfx = gx, dfy = gy, dxx = fxx, dxy = fxy, dyy = fyy;
         const double tix = dfx * (2.0 * dxx * dxx + 2.0 * dxy * dxy) + dfy * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
                            2.0 * dfx * dfy * (double)fxxy + dfy * dfy * (double)fxyy + dfx * dfx * (double)fxxx;
@@ -348,16 +372,17 @@ __device__ __forceinline__ int cta_excl_scan(int v, int* sWarp, int* tot)
 }
 
 template <int R, bool HYB>
-__global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_constant__ BatchParams p)
+__global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(const __grid_constant__ BatchParams p)
 {
     using C = Cfg<R>;
     constexpr int B = C::B;
+    constexpr int NT = C::NT;
     extern __shared__ __align__(16) unsigned char smem[];
     float* sIn = reinterpret_cast<float*>(smem + C::off_in);
-    unsigned* sList = reinterpret_cast<unsigned*>(smem + C::off_in);  // aliases sIn (not live together)
     float2* sP = reinterpret_cast<float2*>(smem + C::off_P);
-    float* sMag = reinterpret_cast<float*>(smem + C::off_mag);
     float2* sFxy = reinterpret_cast<float2*>(smem + C::off_fxy);
+    unsigned* sMask = reinterpret_cast<unsigned*>(smem + C::off_mask);  // [MS][2] threshold ballots
+    unsigned* sList = reinterpret_cast<unsigned*>(smem + C::off_list);
     float4* sTab = reinterpret_cast<float4*>(smem + C::off_tab);
     int* sMisc = reinterpret_cast<int*>(smem + C::off_misc);
     float* sRec = reinterpret_cast<float*>(smem + C::off_rec);
@@ -365,7 +390,7 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
     int* sRowOff = sMisc + 32;   // [32]
     int* sAccCnt = sMisc + 64;   // [32] accepted edgels per NMS row
     int* sWarp = sMisc + 96;     // [8] scan scratch
-    int* sScal = sMisc + 112;    // [0] unit [1] staging base [2] list length [3] accepted
+    int* sScal = sMisc + 112;    // [0] unit [1] staging base [2] list length [3] [4] reserved staging range
     unsigned char* sRaw = smem + C::off_raw;  // TMA destination: one box of input rows
     const uint32_t bar = smem_addr(smem + C::off_mbar);
     uint32_t phase = 0;
@@ -374,15 +399,18 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
     const TapBlock& tp = p.taps;
 
     // y-direction tap table for the per-edgel stage: [variant][k] = (G, Gy, Gyy, Gyyy)
-    for (int i = tid; i < 3 * C::NT; i += kThreads) {
-        const int v = i / C::NT, k = i % C::NT;
+    for (int i = tid; i < 3 * NT; i += kThreads) {
+        const int v = i / NT, k = i % NT;
         const int f = (v == 2) ? 4 : 0;
         float4 t = make_float4(tp.v[f][k], tp.v[f + 1][k], tp.v[f + 2][k], tp.v[f + 3][k]);
-        if (v == 0 && (k == 0 || k == C::NT - 1)) t = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (v == 0 && (k == 0 || k == NT - 1)) t = make_float4(0.f, 0.f, 0.f, 0.f);
         sTab[i] = t;
     }
     int nrec = 0;  // deferred records in the ring (uniform across the CTA)
-    if (tid == 0) mbar_init(bar);
+    if (tid == 0) {
+        mbar_init(bar);
+        sScal[3] = sScal[4] = 0;  // this CTA's reserved staging range [next, end)
+    }
 
     for (;;) {
         __syncthreads();
@@ -412,15 +440,17 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
             shift = xin - x_al;
         }
         const int rawpitch = im.tma_boxw * (dtype == TOED_U8 ? 1 : 4);  // bytes per staged row
+        const int gc_base = 2 * (x0 - 1);
 
-        for (int i = tid; i < 2 * 64; i += kThreads) {
-            sMag[i] = 0.f;
-            sFxy[i] = make_float2(0.f, 0.f);
-        }
+        // 2x-grid rows 0 and 1 of the NMS window start empty
+        for (int i = tid; i < 2 * 64; i += kThreads) sFxy[i] = make_float2(0.f, 0.f);
+        if (tid < 4) sMask[tid] = 0u;
 
+        int rb = 0;
         for (int s = 0; s < nsteps; ++s) {
-            // ---- 1. input rows -> sIn (FP32, zero padded) -------------------
-            // slot h <-> ext row e = s*B - R - 2 + h <-> image row ys - 1 + e
+            // logical slot h <-> ring row (rb + h) mod RING <-> ext row
+            // s*B - R - 2 + h <-> image row ys - 1 + ext row
+            // ---- 1. input rows -> input ring (FP32, zero padded) -----------
             if (im.tma) {
                 // rows arrive by TMA (out-of-image texels read as zero, the
                 // reference's zero padding); step s+1's box is requested as
@@ -441,17 +471,17 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                         return;
                     }
                     const int nrows = min(B, C::HS - ((s == 0) ? ch * B : 0));
-                    const int dst0 = (s == 0) ? ch * B : 0;
+                    const int a0 = (s == 0) ? ch * B : rb + 2 * R + 3;  // ring row of box row 0 (before wrapping)
                     if (dtype == TOED_U8) {
                         for (int i = tid; i < nrows * C::NIN; i += kThreads) {
                             const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                            sIn[(dst0 + rr) * C::NIN + cc] = (float)sRaw[rr * rawpitch + shift + cc];
+                            sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = (float)sRaw[rr * rawpitch + shift + cc];
                         }
                     } else {
                         const float* rf = reinterpret_cast<const float*>(sRaw);
                         for (int i = tid; i < nrows * C::NIN; i += kThreads) {
                             const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                            sIn[(dst0 + rr) * C::NIN + cc] = rf[rr * im.tma_boxw + shift + cc];
+                            sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = rf[rr * im.tma_boxw + shift + cc];
                         }
                     }
                     __syncthreads();
@@ -464,62 +494,60 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                                   (uint32_t)(B * rawpitch));
             } else {
                 const int nrows = (s == 0) ? C::HS : B;
-                const int img_row0 = ys - 1 + s * B - R - 2 + ((s == 0) ? 0 : 2 * R + 3);
+                const int a0 = (s == 0) ? 0 : rb + 2 * R + 3;
+                const int img_row0 = (s == 0) ? ys - R - 3 : ys + s * B + R;
                 for (int i = tid; i < nrows * C::NIN; i += kThreads) {
                     const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                    sIn[i] = fetch_px(src, pitch, H, W, dtype, img_row0 + rr, xin + cc);
+                    sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = fetch_px(src, pitch, H, W, dtype, img_row0 + rr, xin + cc);
                 }
                 __syncthreads();
             }
             // ---- 2. row pass ------------------------------------------------
             if (s == 0)
-                row_pass<R>(sIn, 0, C::HS, 0, sP, tp);
+                row_pass<R>(sIn, 0, C::HS, sP, tp);
             else
-                row_pass<R>(sIn, 0, B, 2 * R + 3, sP, tp);
+                row_pass<R>(sIn, ring_wrap<C::RING>(rb + 2 * R + 3), B, sP, tp);
             __syncthreads();
-            // ---- 3. column pass: Ix, Iy, |grad I| for ext rows s*B .. s*B+B-1
+            // ---- 3. column pass: Ix, Iy for 2x rows m = 2..2B+1, and the
+            // threshold test as ballots over the strip's columns
+            const int gr_base = 2 * ys - 4 + 2 * s * B;  // global 2x row of NMS row m: gr_base + m
             {
                 const int sg = wid & 3, g = wid >> 2;
                 const int a = sg >> 1, b = sg & 1;
                 float fx[kColRows], fy[kColRows];
+                // sub-grid (a, b): x taps T / F / S for (0,0) / (1,0) / (.,1),
+                // y taps truncated for (0,0), full for (0,1), shifted for (1,.)
+                const float2* P = sP + (sg == 0 ? 0 : (sg == 2 ? 1 : 2)) * C::RING * kExt;
                 if (sg == 0)
-                    col_pass<R, 0>(sP + 0 * C::HS * kExt, g, lane, tp, fx, fy);
-                else if (sg == 2)
-                    col_pass<R, 2>(sP + 1 * C::HS * kExt, g, lane, tp, fx, fy);
+                    col_pass<R, 0>(P, rb, g, lane, tp, fx, fy);
                 else if (sg == 1)
-                    col_pass<R, 1>(sP + 2 * C::HS * kExt, g, lane, tp, fx, fy);
+                    col_pass<R, 1>(P, rb, g, lane, tp, fx, fy);
                 else
-                    col_pass<R, 2>(sP + 2 * C::HS * kExt, g, lane, tp, fx, fy);
+                    col_pass<R, 2>(P, rb, g, lane, tp, fx, fy);
+                const int c = 2 * lane + b, Gc = gc_base + c;
+                const bool colok = lane >= 1 && lane <= kInner && Gc >= col_lo && Gc < col_hi;
 #pragma unroll
                 for (int o = 0; o < kColRows; ++o) {
                     const int m = 2 * (g * kColRows + o) + a + 2;
-                    const int c = 2 * lane + b;
-                    sMag[m * 64 + c] = sqrt_approx(fmaf(fx[o], fx[o], fy[o] * fy[o]));
-                    sFxy[m * 64 + c] = make_float2(fx[o], fy[o]);
+                    const float2 f = make_float2(fx[o], fy[o]);
+                    sFxy[m * 64 + c] = f;
+                    const int Gr = gr_base + m;
+                    const bool kp = colok && Gr >= row_lo && Gr < row_hi && grad_mag(f) > p.thr;  // cpu_toed.cpp:403
+                    const unsigned bal = __ballot_sync(0xffffffffu, kp);
+                    if (lane == 0) sMask[m * 2 + b] = bal;
                 }
             }
             if (tid < 32) sAccCnt[tid] = 0;
             __syncthreads();
             // ---- 4a. points above the threshold, listed in row-major order ---
-            // NMS rows m = 1..2B (rho = 2sB-2+m), global 2x row Gr = gr_base + m
-            const int gr_base = 2 * ys - 4 + 2 * s * B;
-            const int gc_base = 2 * (x0 - 1);
-            unsigned bal0[4], bal1[4];
+            // NMS rows m = 1..2B; bit L of a mask <-> 2x column 2L + parity
+            unsigned mk0[4], mk1[4];
 #pragma unroll
             for (int t = 0; t < 4; ++t) {
                 const int m = 1 + wid + 8 * t;
-                const int Gr = gr_base + m;
-                const int c0 = 2 + 2 * lane;
-                const int Gc = gc_base + c0;
-                bool k0 = false, k1 = false;
-                if (Gr >= row_lo && Gr < row_hi && lane < kInner) {
-                    const float2 mv = *reinterpret_cast<const float2*>(sMag + m * 64 + c0);
-                    k0 = (Gc >= col_lo && Gc < col_hi) && (mv.x > p.thr);  // cpu_toed.cpp:403
-                    k1 = (Gc + 1 >= col_lo && Gc + 1 < col_hi) && (mv.y > p.thr);
-                }
-                bal0[t] = __ballot_sync(0xffffffffu, k0);
-                bal1[t] = __ballot_sync(0xffffffffu, k1);
-                if (lane == 0) sRowCnt[m - 1] = __popc(bal0[t]) + __popc(bal1[t]);
+                mk0[t] = sMask[m * 2];
+                mk1[t] = sMask[m * 2 + 1];
+                if (lane == 0) sRowCnt[m - 1] = __popc(mk0[t]) + __popc(mk1[t]);
             }
             __syncthreads();
             if (wid == 0) {
@@ -539,9 +567,9 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int m = 1 + wid + 8 * t;
-                    const bool k0 = (bal0[t] >> lane) & 1u, k1 = (bal1[t] >> lane) & 1u;
-                    const int pos = sRowOff[m - 1] + __popc(bal0[t] & lt) + __popc(bal1[t] & lt);
-                    const unsigned c0 = 2 + 2 * lane;
+                    const bool k0 = (mk0[t] >> lane) & 1u, k1 = (mk1[t] >> lane) & 1u;
+                    const int pos = sRowOff[m - 1] + __popc(mk0[t] & lt) + __popc(mk1[t] & lt);
+                    const unsigned c0 = 2 * lane;
                     if (k0) sList[pos] = ((unsigned)m << 8) | c0;
                     if (k1) sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
                 }
@@ -557,7 +585,7 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                 bool acc = false;
                 if (e < LA) {
                     rec = sList[e];
-                    acc = nms_eval(sMag, sFxy, rec >> 8, rec & 255, p.thr).cand;
+                    acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr).cand;
                 }
                 int tot;
                 const int rank = cta_excl_scan(acc ? 1 : 0, sWarp, &tot);
@@ -577,20 +605,31 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                     const int y = __shfl_up_sync(0xffffffffu, incl, d);
                     if (lane >= d) incl += y;
                 }
+                // staging slots: carved from this CTA's reserved range, which is
+                // refilled from the global cursor only when a step does not fit
                 int base = 0;
-                if (lane == 0 && nacc > 0) base = atomicAdd(&p.sc.words[1], nacc);
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (lane == 0) {
-                    sScal[1] = base;
+                if (lane == 0 && nacc > 0) {
+                    int next = sScal[3], end = sScal[4];
+                    if (next + nacc > end) {
+                        const int n = max(p.stage_blk, nacc);
+                        next = atomicAdd(&p.sc.words[1], n);
+                        end = next + n;
+                        sScal[4] = end;
+                    }
+                    base = next;
+                    sScal[3] = next + nacc;
                     if ((long long)base + nacc > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
                 }
+                base = __shfl_sync(0xffffffffu, base, 0);
+                if (lane == 0) sScal[1] = base;
                 const int Gr = gr_base + lane + 1;
                 if (Gr >= 2 * ys && Gr < 2 * ys + 2 * S_act)
                     p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
             }
             __syncthreads();
-            // ---- 5. per edgel: seven higher derivatives from the window into a
-            // deferred record (the FP64 epilogue runs when the ring is full)
+            // ---- 5. per edgel: the seven higher derivatives from the row-pass
+            // ring into a deferred record (the FP64 epilogue runs when the
+            // ring of records is full)
             {
                 const int base = sScal[1];
                 for (int j0 = 0; j0 < nacc;) {
@@ -601,16 +640,17 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                         const int a = m & 1, xe = c >> 1, b = c & 1;
                         const int xv = b ? 2 : (a ? 1 : 0);
                         const int yv = a ? 2 : (b ? 1 : 0);
-                        const float2* Pp = sP + xv * C::HS * kExt + xe;
-                        const float2* Qp = sP + (3 + xv) * C::HS * kExt + xe;
-                        const float4* tab = sTab + yv * C::NT;
+                        const float2* Pp = sP + xv * C::RING * kExt + xe;
+                        const float2* Qp = sP + (3 + xv) * C::RING * kExt + xe;
+                        const float4* tab = sTab + yv * NT;
                         float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
-                        const int h0 = m >> 1;
+                        const int h0 = rb + (m >> 1);
 #pragma unroll
-                        for (int kk = 0; kk < C::NT; ++kk) {
-                            const float2 hp = Pp[(h0 + kk) * kExt];
-                            const float2 hq = Qp[(h0 + kk) * kExt];
-                            const float4 t = tab[C::NT - 1 - kk];
+                        for (int kk = 0; kk < NT; ++kk) {
+                            const int ph = ring_wrap<C::RING>(h0 + kk) * kExt;
+                            const float2 hp = Pp[ph];
+                            const float2 hq = Qp[ph];
+                            const float4 t = tab[NT - 1 - kk];
                             fxy = fmaf(hp.y, t.y, fxy);
                             fyy = fmaf(hp.x, t.z, fyy);
                             fxyy = fmaf(hp.y, t.z, fxyy);
@@ -619,7 +659,7 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                             fxxy = fmaf(hq.x, t.y, fxxy);
                             fxxx = fmaf(hq.y, t.x, fxxx);
                         }
-                        const NmsEval e = nms_eval(sMag, sFxy, m, c, p.thr);
+                        const NmsEval e = nms_eval(sFxy, m, c, p.thr);
                         const int Gr = gr_base + m, Gc = gc_base + c;
                         float* rc = sRec + (nrec + j) * C::RECW;
                         rc[0] = e.gx; rc[1] = e.gy; rc[2] = e.mv; rc[3] = e.nx; rc[4] = e.ny; rc[5] = e.slope;
@@ -642,37 +682,11 @@ __global__ void __launch_bounds__(kThreads, 2) toed_detect_kernel(const __grid_c
                 }
             }
             __syncthreads();
-            // ---- 6. slide the windows -------------------------------------
+            // ---- 6. carry the last two 2x rows into the next step's rows 0, 1
+            rb = ring_wrap<C::RING>(rb + B);
             if (s + 1 < nsteps) {
-                // row-pass window: slots [B, HS) -> [0, 2R+3); every thread reads
-                // its share into registers before anyone writes (sources and
-                // destinations overlap when 2R+3 > B)
-                constexpr int NSH = 6 * (2 * R + 3) * (kExt / 2);
-                constexpr int PER = (NSH + kThreads - 1) / kThreads;
-                float4 keep[PER];
-#pragma unroll
-                for (int t = 0; t < PER; ++t) {
-                    const int i = tid + t * kThreads;
-                    if (i < NSH) {
-                        const int a = i / ((2 * R + 3) * 16), rem = i - a * (2 * R + 3) * 16;
-                        const int rr = rem >> 4, cc = (rem & 15) * 2;
-                        keep[t] = *reinterpret_cast<const float4*>(sP + (a * C::HS + B + rr) * kExt + cc);
-                    }
-                }
-                __syncthreads();
-#pragma unroll
-                for (int t = 0; t < PER; ++t) {
-                    const int i = tid + t * kThreads;
-                    if (i < NSH) {
-                        const int a = i / ((2 * R + 3) * 16), rem = i - a * (2 * R + 3) * 16;
-                        const int rr = rem >> 4, cc = (rem & 15) * 2;
-                        *reinterpret_cast<float4*>(sP + (a * C::HS + rr) * kExt + cc) = keep[t];
-                    }
-                }
-                for (int i = tid; i < 2 * 64; i += kThreads) {
-                    sMag[i] = sMag[2 * B * 64 + i];
-                    sFxy[i] = sFxy[2 * B * 64 + i];
-                }
+                for (int i = tid; i < 2 * 64; i += kThreads) sFxy[i] = sFxy[2 * B * 64 + i];
+                if (tid < 4) sMask[tid] = sMask[2 * B * 2 + tid];
             }
         }
     }

@@ -120,6 +120,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     p.n_img = 1;
     p.out_f64 = prm->out_dtype == TOED_F64;
     p.radius = r;
+    p.stage_blk = 1;  // staging sized to the capacity exactly: reserve each step's edgels alone
     // strip height: the tallest of 254 / 126 / 62 / 30 / 14 rows that still
     // gives every resident CTA a few strips
     const int nsc = (im->width + kInner - 1) / kInner;
