@@ -345,32 +345,6 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
     }
 }
 
-// Block-wide exclusive scan of one int per thread (256 threads); returns the
-// prefix and leaves the total in *tot.  Three barriers' worth of traffic on
-// sWarp[9].
-__device__ __forceinline__ int cta_excl_scan(int v, int* sWarp, int* tot)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-    }
-    if (lane == 31) sWarp[wid] = incl;
-    __syncthreads();
-    int off = 0, t = 0;
-#pragma unroll
-    for (int w = 0; w < kThreads / 32; ++w) {
-        const int x = sWarp[w];
-        off += (w < wid) ? x : 0;
-        t += x;
-    }
-    *tot = t;
-    __syncthreads();
-    return off + incl - v;
-}
-
 template <int R, bool HYB>
 __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(const __grid_constant__ BatchParams p)
 {
@@ -386,11 +360,10 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
     float4* sTab = reinterpret_cast<float4*>(smem + C::off_tab);
     int* sMisc = reinterpret_cast<int*>(smem + C::off_misc);
     float* sRec = reinterpret_cast<float*>(smem + C::off_rec);
-    int* sRowCnt = sMisc;        // [32] points above threshold per NMS row
     int* sRowOff = sMisc + 32;   // [32]
     int* sAccCnt = sMisc + 64;   // [32] accepted edgels per NMS row
-    int* sWarp = sMisc + 96;     // [8] scan scratch
-    int* sScal = sMisc + 112;    // [0] unit [1] staging base [2] list length [3] [4] reserved staging range
+    int* sWarp = sMisc + 96;     // [2][8] warp counts of the NMS compaction
+    int* sScal = sMisc + 112;    // [0] unit [1] staging refill [2] list length
     unsigned char* sRaw = smem + C::off_raw;  // TMA destination: one box of input rows
     const uint32_t bar = smem_addr(smem + C::off_mbar);
     uint32_t phase = 0;
@@ -407,10 +380,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         sTab[i] = t;
     }
     int nrec = 0;  // deferred records in the ring (uniform across the CTA)
-    if (tid == 0) {
-        mbar_init(bar);
-        sScal[3] = sScal[4] = 0;  // this CTA's reserved staging range [next, end)
-    }
+    int stg_next = 0, stg_end = 0;  // this CTA's reserved staging range [next, end) (uniform)
+    if (tid == 0) mbar_init(bar);
 
     for (;;) {
         __syncthreads();
@@ -503,10 +474,14 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 __syncthreads();
             }
             // ---- 2. row pass ------------------------------------------------
-            if (s == 0)
+            if (s == 0) {
                 row_pass<R>(sIn, 0, C::HS, sP, tp);
-            else
+            } else {
                 row_pass<R>(sIn, ring_wrap<C::RING>(rb + 2 * R + 3), B, sP, tp);
+                // the previous step's last two 2x rows become rows 0 and 1
+                for (int i = tid; i < 2 * 64; i += kThreads) sFxy[i] = sFxy[2 * B * 64 + i];
+                if (tid < 4) sMask[tid] = sMask[2 * B * 2 + tid];
+            }
             __syncthreads();
             // ---- 3. column pass: Ix, Iy for 2x rows m = 2..2B+1, and the
             // threshold test as ballots over the strip's columns
@@ -540,18 +515,10 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             if (tid < 32) sAccCnt[tid] = 0;
             __syncthreads();
             // ---- 4a. points above the threshold, listed in row-major order ---
-            // NMS rows m = 1..2B; bit L of a mask <-> 2x column 2L + parity
-            unsigned mk0[4], mk1[4];
-#pragma unroll
-            for (int t = 0; t < 4; ++t) {
-                const int m = 1 + wid + 8 * t;
-                mk0[t] = sMask[m * 2];
-                mk1[t] = sMask[m * 2 + 1];
-                if (lane == 0) sRowCnt[m - 1] = __popc(mk0[t]) + __popc(mk1[t]);
-            }
-            __syncthreads();
+            // NMS rows m = 1..2B; bit L of a mask <-> 2x column 2L + parity.
+            // Warp 0 counts and scans the rows (lane L <-> row L + 1).
             if (wid == 0) {
-                const int cnt = sRowCnt[lane];
+                const int cnt = __popc(sMask[(lane + 1) * 2]) + __popc(sMask[(lane + 1) * 2 + 1]);
                 int incl = cnt;
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
@@ -567,8 +534,9 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
 #pragma unroll
                 for (int t = 0; t < 4; ++t) {
                     const int m = 1 + wid + 8 * t;
-                    const bool k0 = (mk0[t] >> lane) & 1u, k1 = (mk1[t] >> lane) & 1u;
-                    const int pos = sRowOff[m - 1] + __popc(mk0[t] & lt) + __popc(mk1[t] & lt);
+                    const unsigned mk0 = sMask[m * 2], mk1 = sMask[m * 2 + 1];
+                    const bool k0 = (mk0 >> lane) & 1u, k1 = (mk1 >> lane) & 1u;
+                    const int pos = sRowOff[m - 1] + __popc(mk0 & lt) + __popc(mk1 & lt);
                     const unsigned c0 = 2 * lane;
                     if (k0) sList[pos] = ((unsigned)m << 8) | c0;
                     if (k1) sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
@@ -576,10 +544,12 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             }
             __syncthreads();
             // ---- 4b. NMS on the list with full warps; survivors compacted in
-            // place, order kept (their rank never exceeds their list position)
+            // place, order kept (their rank never exceeds their list position).
+            // One barrier per round: the warp counts alternate between two
+            // halves of sWarp.
             const int LA = sScal[2];
             int nacc = 0;
-            for (int r0 = 0; r0 < LA; r0 += kThreads) {
+            for (int r0 = 0, rd = 0; r0 < LA; r0 += kThreads, rd ^= 1) {
                 const int e = r0 + tid;
                 unsigned rec = 0;
                 bool acc = false;
@@ -587,16 +557,39 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     rec = sList[e];
                     acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr).cand;
                 }
-                int tot;
-                const int rank = cta_excl_scan(acc ? 1 : 0, sWarp, &tot);
+                const unsigned bal = __ballot_sync(0xffffffffu, acc);
+                int* wc = sWarp + 8 * rd;
+                if (lane == 0) wc[wid] = __popc(bal);
+                __syncthreads();
+                int off = 0, tot = 0;
+#pragma unroll
+                for (int w = 0; w < kThreads / 32; ++w) {
+                    const int x = wc[w];
+                    off += (w < wid) ? x : 0;
+                    tot += x;
+                }
                 if (acc) {
-                    sList[nacc + rank] = rec;
+                    sList[nacc + off + __popc(bal & ((1u << lane) - 1u))] = rec;
                     atomicAdd(&sAccCnt[(rec >> 8) - 1], 1);
                 }
                 nacc += tot;
             }
             __syncthreads();
-            // ---- 4c. staging slots and the row-segment table ---------------
+            // ---- 4c. staging slots: carved from this CTA's reserved range
+            // (tracked identically by every thread), refilled from the global
+            // cursor only when a step does not fit
+            if (nacc > 0 && stg_next + nacc > stg_end) {
+                const int n = max(p.stage_blk, nacc);
+                if (tid == 0) sScal[1] = atomicAdd(&p.sc.words[1], n);
+                __syncthreads();
+                stg_next = sScal[1];
+                stg_end = stg_next + n;
+            }
+            const int base = stg_next;
+            stg_next += nacc;
+            if (tid == 0 && (long long)base + nacc > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
+            // warp 0: the row-segment table {staging offset, count} per 2x row,
+            // while the other warps gather the edgels
             if (wid == 0) {
                 const int cnt = sAccCnt[lane];
                 int incl = cnt;
@@ -605,36 +598,17 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     const int y = __shfl_up_sync(0xffffffffu, incl, d);
                     if (lane >= d) incl += y;
                 }
-                // staging slots: carved from this CTA's reserved range, which is
-                // refilled from the global cursor only when a step does not fit
-                int base = 0;
-                if (lane == 0 && nacc > 0) {
-                    int next = sScal[3], end = sScal[4];
-                    if (next + nacc > end) {
-                        const int n = max(p.stage_blk, nacc);
-                        next = atomicAdd(&p.sc.words[1], n);
-                        end = next + n;
-                        sScal[4] = end;
-                    }
-                    base = next;
-                    sScal[3] = next + nacc;
-                    if ((long long)base + nacc > p.sc.staging_cap) atomicOr(&p.sc.words[2], TOED_FLAG_STAGING_FULL);
-                }
-                base = __shfl_sync(0xffffffffu, base, 0);
-                if (lane == 0) sScal[1] = base;
                 const int Gr = gr_base + lane + 1;
                 if (Gr >= 2 * ys && Gr < 2 * ys + 2 * S_act)
                     p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
             }
-            __syncthreads();
             // ---- 5. per edgel: the seven higher derivatives from the row-pass
             // ring into a deferred record (the FP64 epilogue runs when the
             // ring of records is full)
             {
-                const int base = sScal[1];
                 for (int j0 = 0; j0 < nacc;) {
                     const int chunk = min(nacc - j0, C::NREC - nrec);
-                    for (int j = tid; j < chunk; j += kThreads) {
+                    for (int j = tid - 32; wid > 0 && j < chunk; j += kThreads - 32) {
                         const unsigned rec = sList[j0 + j];
                         const int m = rec >> 8, c = rec & 255;
                         const int a = m & 1, xe = c >> 1, b = c & 1;
@@ -681,13 +655,9 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     }
                 }
             }
-            __syncthreads();
-            // ---- 6. carry the last two 2x rows into the next step's rows 0, 1
+            // (no barrier here: the next step's first barrier, before its row
+            // pass and its carry of rows 0 and 1, orders this step's reads)
             rb = ring_wrap<C::RING>(rb + B);
-            if (s + 1 < nsteps) {
-                for (int i = tid; i < 2 * 64; i += kThreads) sFxy[i] = sFxy[2 * B * 64 + i];
-                if (tid < 4) sMask[tid] = sMask[2 * B * 2 + tid];
-            }
         }
     }
     // flush the records still in the ring (the loop exit follows a barrier)
