@@ -187,6 +187,43 @@ toed_status toed_subpix_to_correct_batch(toed_ctx* ctx, const toed_edgemap* maps
 #define TOED_NOALLOC_MAX_EDGELS 262144
 toed_status toed_detect_noalloc(const toed_image* image, const toed_params* params, cudaStream_t stream);
 
+/* Detection of images held in host memory -- the reference's flow (copy the
+ * image in, detect, copy the edgel list back, gpu_toed.hpp:141-231 and
+ * :415-441) for a whole batch, pipelined: the batch is cut into `chunks`
+ * groups of consecutive images with similar pixel counts; the copy of group
+ * k+1 to the device overlaps the detection of group k and the copy back of
+ * group k-1 (three streams of the context, ordered by events).  Synchronous:
+ * returns when every count and list is in host memory.  Device staging for
+ * the images and lists is kept in the context and grows on demand.  Host
+ * buffers should be page-locked for full copy speed.  Returns
+ * TOED_ERR_TIMEOUT if a bounded device wait gave up; more edgels than
+ * `capacity` show as count > capacity (the list holds the first capacity). */
+typedef struct toed_host_image {
+    const void* pixels; /* host: height x pitch elements of `dtype` */
+    int height;
+    int width;
+    int pitch;          /* elements between row starts, >= width */
+    int dtype;          /* TOED_U8 or TOED_F32 */
+    void* edgels;       /* host: capacity x 4 of params->out_dtype */
+    int capacity;
+    int* count;         /* host: 1 int */
+    int* grid_index;    /* optional host: capacity ints */
+} toed_host_image;
+
+toed_status toed_detect_host_batch(toed_ctx* ctx, const toed_host_image* images, int n_images,
+                                   const toed_params* params, int chunks, cudaStream_t stream);
+
+/* After detection (the reference's drivers; no kernel counterpart there).
+ * toed_edgels_to_columns: the n x 4 device list (TOED_F32 or TOED_F64) as the
+ * column-major n x 4 double array curvelet formation reads
+ * (form_curvelet_process, main_cpu_DP.cpp:225-236), on the device.
+ * toed_write_edgels_txt: a host list as the text file non_maximum_suppresion
+ * writes -- each value followed by a tab, a newline per edgel, `precision`
+ * significant digits: 6 for data_final_output_cpu.txt (cpu_toed.cpp:556-580),
+ * 10 for data_final_output_gpu.txt (gpu_toed.hpp:452-478). */
+toed_status toed_edgels_to_columns(const void* edgels, int dtype, int n, double* columns, cudaStream_t stream);
+toed_status toed_write_edgels_txt(const char* path, const void* edgels, int dtype, int n, int precision);
+
 /* Launch-shape autotuning (no counterpart in the reference, whose GPU path
  * has one fixed launch shape).  toed_autotune times each candidate -- strip
  * height 14, 30, 62, 126, 254, 510 or 1022 rows, input rows staged by TMA or

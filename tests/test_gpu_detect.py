@@ -271,3 +271,32 @@ def test_autotune_and_launch_shapes_agree(toed, synth):
     t.cuda.synchronize()
     for (n0, e0, i0), o in zip(ref, outs):
         assert int(o["count"].item()) == n0 and t.equal(o["edgels"][:n0].cpu(), e0)
+
+
+@pytest.mark.parametrize("chunks", [1, 3])
+def test_host_batch_matches_device_batch(toed, synth, chunks):
+    """toed_detect_host_batch (host buffers, pipelined copies) returns the same
+    lists as the device-buffer batch, for uint8 / float32, a host pitch wider
+    than the image, and a capacity smaller than the edgel count."""
+    t = _torch()
+    det = toed.Detector(0)
+    sizes = [(200, 300), (97, 1000), (333, 129), (64, 64), (450, 211)]
+    host = []
+    for k, (h, w) in enumerate(sizes):
+        im = synth.shapes_image(h, w, seed=1400 + k, dtype=np.uint8 if k == 2 else np.float32).image
+        host.append(t.as_tensor(im))
+    wide = t.zeros((sizes[0][0], sizes[0][1] + 17), dtype=t.float32)
+    wide[:, :sizes[0][1]] = host[0]
+    host[0] = wide[:, :sizes[0][1]]  # pitch > width in host memory
+    prm = toed.make_params(1.5)
+    ref = det.detect_batch([im.contiguous().cuda() for im in host], sigma=1.5)
+    outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True)
+    small = 3  # image 3: capacity below its edgel count
+    outs[small]["capacity"] = max(1, ref[small]["count"] // 2)
+    det.detect_host(host, outs, prm, chunks=chunks)
+    for k, (r, o) in enumerate(zip(ref, outs)):
+        n = int(o["count"].item())
+        assert n == r["count"], k
+        m = min(n, o["capacity"])
+        assert t.equal(o["edgels"][:m], r["edgels"][:m].cpu()), k
+        assert t.equal(o["index"][:m], r["index"][:m].cpu()), k

@@ -39,7 +39,7 @@ C_SYMBOLS = [
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
     "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
     "toed_subpix_to_correct_batch", "toed_detect_noalloc", "toed_backward_batch", "toed_autotune",
-    "toed_set_tuning",
+    "toed_set_tuning", "toed_detect_host_batch", "toed_edgels_to_columns", "toed_write_edgels_txt",
 ]
 
 
@@ -85,6 +85,14 @@ class toed_subpix_params(ctypes.Structure):
     _fields_ = [
         ("thresh", ctypes.c_float), ("sigma", ctypes.c_float), ("nbr_radius", ctypes.c_float),
         ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
+    ]
+
+
+class toed_host_image(ctypes.Structure):
+    _fields_ = [
+        ("pixels", ctypes.c_void_p), ("height", ctypes.c_int), ("width", ctypes.c_int),
+        ("pitch", ctypes.c_int), ("dtype", ctypes.c_int), ("edgels", ctypes.c_void_p),
+        ("capacity", ctypes.c_int), ("count", ctypes.c_void_p), ("grid_index", ctypes.c_void_p),
     ]
 
 
@@ -139,6 +147,10 @@ def lib():
         L.toed_autotune.argtypes = [vp, ctypes.POINTER(toed_image), ip, ctypes.POINTER(toed_params), ip, vp,
                                     ctypes.POINTER(toed_tuning)]
         L.toed_set_tuning.argtypes = [vp, ctypes.POINTER(toed_params), ctypes.POINTER(toed_tuning)]
+        L.toed_edgels_to_columns.argtypes = [vp, ip, ip, vp, vp]
+        L.toed_write_edgels_txt.argtypes = [ctypes.c_char_p, vp, ip, ip, ip]
+        L.toed_detect_host_batch.argtypes = [vp, ctypes.POINTER(toed_host_image), ip, ctypes.POINTER(toed_params),
+                                             ip, vp]
         L.toed_backward_batch.argtypes = [vp, ctypes.POINTER(toed_grad_image), ip, ctypes.POINTER(toed_params),
                                           vp, vp]
         for name in C_SYMBOLS:
@@ -297,6 +309,41 @@ class Detector:
         _check(lib().toed_set_tuning(self._ctx, ctypes.byref(params), ctypes.byref(t) if t is not None else None),
                "toed_set_tuning")
 
+    def alloc_host_outputs(self, shapes, capacity=None, out_dtype=TOED_F32, index=False, pin=True):
+        """Page-locked host edgel / count (/ index) buffers for detect_host."""
+        t = self.torch
+        dt = t.float64 if out_dtype == TOED_F64 else t.float32
+        outs = []
+        for (H, W) in shapes:
+            cap = int(capacity) if capacity is not None else 4 * H * W
+            o = {"edgels": t.empty((max(cap, 1), 4), dtype=dt), "count": t.zeros(1, dtype=t.int32),
+                 "index": t.empty(max(cap, 1), dtype=t.int32) if index else None, "capacity": cap}
+            if pin:
+                o = {k: (v.pin_memory() if isinstance(v, t.Tensor) else v) for k, v in o.items()}
+            outs.append(o)
+        return outs
+
+    def detect_host(self, images, outs, params: toed_params, chunks: int = 4, stream=None):
+        """Detect edgels in images held in host memory (2-D CPU tensors,
+        page-locked for full speed) into host buffers from
+        alloc_host_outputs: copies in, detection and copies out are
+        pipelined over ``chunks`` groups (synchronous)."""
+        t = self.torch
+        arr = (toed_host_image * len(images))()
+        for k, (im, o) in enumerate(zip(images, outs)):
+            if im.dim() != 2 or im.device.type != "cpu" or im.stride(1) != 1:
+                raise ValueError("host images must be 2-D CPU tensors with contiguous rows")
+            dt = TOED_U8 if im.dtype == t.uint8 else (TOED_F32 if im.dtype == t.float32 else None)
+            if dt is None:
+                raise ValueError("image dtype must be uint8 or float32")
+            H, W = im.shape
+            arr[k] = toed_host_image(im.data_ptr(), H, W, im.stride(0), dt, o["edgels"].data_ptr(), o["capacity"],
+                                     o["count"].data_ptr(),
+                                     o["index"].data_ptr() if o.get("index") is not None else None)
+        s = stream if stream is not None else t.cuda.current_stream(self.device)
+        _check(lib().toed_detect_host_batch(self._ctx, arr, len(images), ctypes.byref(params), int(chunks),
+                                            ctypes.c_void_p(s.cuda_stream)), "toed_detect_host_batch")
+
     def capture(self, images, outs, params: toed_params, warmup: int = 1):
         """Capture detect_into(images, outs, params) in a CUDA graph (the
         persistent detection launch plus the ordering pass) and return it;
@@ -437,6 +484,35 @@ def detect(image, sigma=2.0, **kw):
 def detect_batch(images, sigma=2.0, **kw):
     dev = images[0].device.index or 0
     return _default_detector(dev).detect_batch(images, sigma=sigma, **kw)
+
+
+def edgels_to_columns(edgels, stream=None):
+    """The n x 4 CUDA edgel list (float32 or float64) as the column-major
+    double array curvelet formation reads (main_cpu_DP.cpp:225-236):
+    returns a (4, n) float64 CUDA tensor whose row j is column j."""
+    import torch
+    if edgels.device.type != "cuda" or edgels.dim() != 2 or edgels.shape[1] != 4 or not edgels.is_contiguous():
+        raise ValueError("edgels must be a contiguous n x 4 CUDA tensor")
+    dt = TOED_F64 if edgels.dtype == torch.float64 else TOED_F32
+    n = edgels.shape[0]
+    out = torch.empty((4, n), dtype=torch.float64, device=edgels.device)
+    s = stream if stream is not None else torch.cuda.current_stream(edgels.device)
+    _check(lib().toed_edgels_to_columns(ctypes.c_void_p(edgels.data_ptr()), dt, n, ctypes.c_void_p(out.data_ptr()),
+                                        ctypes.c_void_p(s.cuda_stream)), "toed_edgels_to_columns")
+    return out
+
+
+def write_edgels_txt(path: str, edgels, precision: int = 10):
+    """Write a host n x 4 list (numpy float32/float64) in the reference's text
+    format: precision 6 = data_final_output_cpu.txt (cpu_toed.cpp:556-580),
+    10 = data_final_output_gpu.txt (gpu_toed.hpp:452-478)."""
+    import numpy as np
+    a = np.ascontiguousarray(edgels)
+    if a.ndim != 2 or a.shape[1] != 4 or a.dtype not in (np.float32, np.float64):
+        raise ValueError("edgels must be an n x 4 float32 or float64 array")
+    dt = TOED_F64 if a.dtype == np.float64 else TOED_F32
+    _check(lib().toed_write_edgels_txt(os.fsencode(path), a.ctypes.data_as(ctypes.c_void_p), dt, a.shape[0],
+                                       int(precision)), "toed_write_edgels_txt")
 
 
 class ThirdOrderEdgeDetectionGPU:

@@ -94,7 +94,7 @@ void encode_rows_map(CUtensorMap* m, DetImage& d, int r)
     const int boxw = (nin + align - 1 + align - 1) / align * align;
     auto fn = encode_fn();
     if (!fn || (reinterpret_cast<uintptr_t>(d.src) & 15u) != 0 || ((long long)d.pitch * esz) % 16 != 0 ||
-        boxw * esz > 256)
+        boxw * esz > kRawRowBytes)
         return;
     const cuuint64_t dims[2] = {(cuuint64_t)d.W, (cuuint64_t)d.H};
     const cuuint64_t strides[1] = {(cuuint64_t)d.pitch * esz};
@@ -151,6 +151,19 @@ struct toed_ctx {
     toed_tuning tune[TOED_MAX_RADIUS + 1][2] = {};
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
+    // toed_detect_host_batch: device staging of images / lists / counts, a
+    // page-locked count buffer and the copy streams
+    unsigned char* hb_in = nullptr;
+    long long hb_in_cap = 0;
+    unsigned char* hb_out = nullptr;
+    long long hb_out_cap = 0;
+    int* hb_idx = nullptr;
+    long long hb_idx_cap = 0;
+    int* hb_cnt = nullptr;
+    long long hb_cnt_cap = 0;
+    int* hb_cnt_host = nullptr;
+    long long hb_cnt_host_cap = 0;
+    cudaStream_t s_in = nullptr, s_out = nullptr;
     std::mutex mu;
 };
 
@@ -225,6 +238,13 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->win);
     cudaFree(c->img_count);
     cudaFree(c->keep);
+    cudaFree(c->hb_in);
+    cudaFree(c->hb_out);
+    cudaFree(c->hb_idx);
+    cudaFree(c->hb_cnt);
+    if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
+    if (c->s_in) cudaStreamDestroy(c->s_in);
+    if (c->s_out) cudaStreamDestroy(c->s_out);
     cudaSetDevice(prev);
     delete c;
     return TOED_OK;
@@ -522,6 +542,157 @@ extern "C" toed_status toed_detect(toed_ctx* c, const toed_image* image, const t
                                    cudaStream_t stream)
 {
     return toed_detect_batch(c, image, 1, prm, stream);
+}
+
+// Host-memory batch, pipelined over `chunks` groups of images (see the
+// header).  Streams: s_in (H2D), the caller's stream (detection), s_out
+// (D2H); events order them per group.  The counts of group k are read on
+// the host before its lists are copied, while later groups still run.
+extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image* images, int n,
+                                              const toed_params* prm, int chunks, cudaStream_t stream)
+{
+    if (!c || !images || n <= 0 || !prm) return TOED_ERR_INVALID_ARG;
+    std::vector<toed_image> dev(n);
+    std::vector<long long> in_off(n), out_off(n), idx_off(n);
+    const int rec = prm->out_dtype == TOED_F64 ? 32 : 16;
+    long long in_b = 0, out_b = 0, idx_n = 0, total_px = 0;
+    for (int i = 0; i < n; ++i) {
+        const toed_host_image& h = images[i];
+        if (!h.pixels || !h.edgels || !h.count || h.height <= 0 || h.width <= 0 || h.pitch < h.width ||
+            h.capacity < 0)
+            return TOED_ERR_INVALID_ARG;
+        if (h.dtype != TOED_U8 && h.dtype != TOED_F32) return TOED_ERR_UNSUPPORTED;
+        const int esz = h.dtype == TOED_U8 ? 1 : 4;
+        const long long dpitch = ((long long)h.width * esz + 15) / 16 * 16;  // 16-byte rows: TMA-eligible
+        in_off[i] = in_b;
+        in_b += (dpitch * h.height + 255) / 256 * 256;
+        out_off[i] = out_b;
+        out_b += ((long long)std::max(h.capacity, 1) * rec + 255) / 256 * 256;
+        idx_off[i] = idx_n;
+        if (h.grid_index) idx_n += std::max(h.capacity, 1);
+        total_px += (long long)h.height * h.width;
+        dev[i].height = h.height;
+        dev[i].width = h.width;
+        dev[i].pitch = (int)(dpitch / esz);
+        dev[i].dtype = h.dtype;
+        dev[i].capacity = h.capacity;
+    }
+    chunks = std::max(1, std::min(chunks, n));
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    TOED_CU(cudaStreamIsCapturing(stream, &cs));
+    if (cs != cudaStreamCaptureStatusNone) return TOED_ERR_CAPTURE;
+    int prev = 0;
+    TOED_CU(cudaGetDevice(&prev));
+    if (prev != c->device) TOED_CU(cudaSetDevice(c->device));
+    std::lock_guard<std::mutex> lk(c->mu);
+    toed_status st = TOED_OK;
+    std::vector<cudaEvent_t> ev_in(chunks, nullptr), ev_det(chunks, nullptr);
+    std::vector<int> first(chunks + 1, n);
+    auto fail = [&](toed_status s) {
+        for (auto e : ev_in)
+            if (e) cudaEventDestroy(e);
+        for (auto e : ev_det)
+            if (e) cudaEventDestroy(e);
+        if (prev != c->device) cudaSetDevice(prev);
+        return s;
+    };
+#define TOED_HB(call)                                                                     \
+    do {                                                                                  \
+        cudaError_t e_ = (call);                                                          \
+        if (e_ != cudaSuccess) {                                                          \
+            g_last_cuda_error = std::string(#call) + ": " + cudaGetErrorString(e_);       \
+            return fail(TOED_ERR_CUDA);                                                   \
+        }                                                                                 \
+    } while (0)
+    if ((st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
+    if ((st = grow(&c->hb_out, &c->hb_out_cap, std::max(out_b, 1LL), stream)) != TOED_OK) return fail(st);
+    if ((st = grow(&c->hb_idx, &c->hb_idx_cap, std::max(idx_n, 1LL), stream)) != TOED_OK) return fail(st);
+    if ((st = grow(&c->hb_cnt, &c->hb_cnt_cap, (long long)n + chunks, stream)) != TOED_OK) return fail(st);
+    if (c->hb_cnt_host_cap < (long long)n + chunks) {
+        if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
+        c->hb_cnt_host = nullptr;
+        c->hb_cnt_host_cap = 0;
+        TOED_HB(cudaMallocHost((void**)&c->hb_cnt_host, sizeof(int) * (size_t)(n + chunks)));
+        c->hb_cnt_host_cap = n + chunks;
+    }
+    if (!c->s_in) TOED_HB(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));
+    if (!c->s_out) TOED_HB(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
+    for (int i = 0; i < n; ++i) {
+        dev[i].pixels = c->hb_in + in_off[i];
+        dev[i].edgels = c->hb_out + out_off[i];
+        dev[i].count = c->hb_cnt + i;
+        dev[i].grid_index = images[i].grid_index ? c->hb_idx + idx_off[i] : nullptr;
+    }
+    for (int i = 0; i < n; ++i) {
+        st = check_image(dev[i]);
+        if (st != TOED_OK) return fail(st);
+    }
+    // groups of consecutive images with similar pixel counts
+    {
+        long long acc = 0;
+        int k = 0;
+        first[0] = 0;
+        for (int i = 0; i < n && k + 1 < chunks; ++i) {
+            acc += (long long)images[i].height * images[i].width;
+            if (acc * chunks >= total_px * (k + 1) && i + 1 < n) first[++k] = i + 1;
+        }
+        chunks = k + 1;
+        first[chunks] = n;
+    }
+    for (int k = 0; k < chunks; ++k) {
+        TOED_HB(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
+        TOED_HB(cudaEventCreateWithFlags(&ev_det[k], cudaEventDisableTiming));
+    }
+    // 1. every group's images to the device, in order
+    for (int k = 0; k < chunks; ++k) {
+        for (int i = first[k]; i < first[k + 1]; ++i) {
+            const toed_host_image& h = images[i];
+            const int esz = h.dtype == TOED_U8 ? 1 : 4;
+            TOED_HB(cudaMemcpy2DAsync(const_cast<void*>(dev[i].pixels), (size_t)dev[i].pitch * esz, h.pixels,
+                                      (size_t)h.pitch * esz, (size_t)h.width * esz, (size_t)h.height,
+                                      cudaMemcpyHostToDevice, c->s_in));
+        }
+        TOED_HB(cudaEventRecord(ev_in[k], c->s_in));
+    }
+    // 2. detection of each group once its images are in
+    for (int k = 0; k < chunks; ++k) {
+        TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
+        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream);
+        if (st != TOED_OK) return fail(st);
+        TOED_HB(cudaMemcpyAsync(c->hb_cnt + n + k, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
+        TOED_HB(cudaEventRecord(ev_det[k], stream));
+    }
+    // 3. per group: counts (and the group's device flags) to the host, then
+    // the lists, while later groups are still being copied in or detected
+    int flags = 0;
+    for (int k = 0; k < chunks; ++k) {
+        TOED_HB(cudaStreamWaitEvent(c->s_out, ev_det[k], 0));
+        const int i0 = first[k], nk = first[k + 1] - first[k];
+        TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + i0, c->hb_cnt + i0, sizeof(int) * nk, cudaMemcpyDeviceToHost,
+                                c->s_out));
+        TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + n + k, c->hb_cnt + n + k, sizeof(int), cudaMemcpyDeviceToHost,
+                                c->s_out));
+        TOED_HB(cudaStreamSynchronize(c->s_out));
+        flags |= c->hb_cnt_host[n + k];
+        for (int i = i0; i < i0 + nk; ++i) {
+            const toed_host_image& h = images[i];
+            const int cnt = c->hb_cnt_host[i];
+            *h.count = cnt;
+            const long long m = std::min(cnt, h.capacity);
+            if (m <= 0) continue;
+            TOED_HB(cudaMemcpyAsync(h.edgels, dev[i].edgels, (size_t)m * rec, cudaMemcpyDeviceToHost, c->s_out));
+            if (h.grid_index)
+                TOED_HB(cudaMemcpyAsync(h.grid_index, dev[i].grid_index, sizeof(int) * (size_t)m,
+                                        cudaMemcpyDeviceToHost, c->s_out));
+        }
+    }
+    TOED_HB(cudaStreamSynchronize(c->s_out));
+    TOED_HB(cudaStreamSynchronize(stream));
+#undef TOED_HB
+    fail(TOED_OK);  // releases the events, restores the device
+    if (flags & TOED_FLAG_TIMEOUT) return TOED_ERR_TIMEOUT;
+    if (flags & TOED_FLAG_STAGING_FULL) return TOED_ERR_CAPACITY;
+    return TOED_OK;
 }
 
 extern "C" toed_status toed_device_flags(toed_ctx* c, cudaStream_t stream, int* flags)

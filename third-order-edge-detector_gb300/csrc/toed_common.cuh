@@ -22,6 +22,8 @@ constexpr int kBatchMax = 64;                      // images per launch (larger 
 constexpr int kThreads = 256;                      // threads per detection CTA
 constexpr int kExt = 32;                           // strip width incl. a 1-pixel ring each side
 constexpr int kInner = kExt - 2;                   // 30 output columns per strip
+constexpr int kHalves = kExt / 32;                 // warp-wide column groups of a strip
+constexpr int kRawRowBytes = 256;                  // bytes per staged input row (TMA box row) at most
 constexpr int kStepRows = 16;                      // original rows per sliding step (B)
 constexpr int kColRows = 8;                        // rows per column-pass thread (register blocking)
 constexpr int kSegTile = 1024;                     // segments per ordering-pass tile

@@ -51,17 +51,18 @@ struct Cfg {
     static constexpr int NMS_ROWS = 2 * B;          // 2x-grid rows decided per step
     static constexpr int MAXC = NMS_ROWS * 2 * kInner;
     static constexpr int RECW = 21;                 // words per deferred edgel record (odd: no bank conflicts)
-    static constexpr size_t sz_raw = kStepRows * 256;  // one TMA box: 16 rows x <= 256 bytes
+    static constexpr int FW = 2 * kExt;             // 2x-grid columns held per row
+    static constexpr size_t sz_raw = kStepRows * kRawRowBytes;  // one TMA box of input rows
     static constexpr size_t off_raw = 0;
     static constexpr size_t off_mbar = off_raw + sz_raw;
     static constexpr size_t off_in = align_up(off_mbar + 16, 16);
     static constexpr size_t off_P = align_up(off_in + sizeof(float) * RING * NIN, 16);
     static constexpr size_t off_fxy = off_P + sizeof(float2) * 6 * RING * kExt;
-    static constexpr size_t off_mask = off_fxy + sizeof(float2) * MS * 64;
-    static constexpr size_t off_list = off_mask + sizeof(unsigned) * MS * 2;
+    static constexpr size_t off_mask = off_fxy + sizeof(float2) * MS * FW;
+    static constexpr size_t off_list = off_mask + sizeof(unsigned) * MS * 2 * kHalves;
     static constexpr size_t off_tab = align_up(off_list + sizeof(unsigned) * MAXC, 16);
     static constexpr size_t off_misc = align_up(off_tab + sizeof(float4) * 3 * NT, 16);
-    static constexpr size_t off_rec = off_misc + sizeof(int) * 128;
+    static constexpr size_t off_rec = off_misc + sizeof(int) * 256;
     // deferred-edgel ring: as many records as keep two CTAs per SM (<= 112 KB each)
     static constexpr int MINB = 2;
     static constexpr size_t budget = 112 * 1024;
@@ -147,8 +148,8 @@ __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int p0, 
 {
     using C = Cfg<R>;
     constexpr int NV = 2 * R + 4;
-    for (int item = threadIdx.x; item < nrows * 16; item += kThreads) {
-        const int i = item >> 4, k = item & 15;
+    for (int item = threadIdx.x; item < nrows * (kExt / 2); item += kThreads) {
+        const int i = item / (kExt / 2), k = item % (kExt / 2);
         const int ph = ring_wrap<C::RING>(p0 + i);
         const float2* src = reinterpret_cast<const float2*>(sIn + ph * C::NIN + 2 * k);
         float v[NV];
@@ -214,7 +215,7 @@ __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int p0, 
 // V = 2: shifted y taps (sub-grids (1/2, .), :287-344)
 // ---------------------------------------------------------------------------
 template <int R, int V>
-__device__ __forceinline__ void col_pass(const float2* __restrict__ P, int rb, int g, int lane,
+__device__ __forceinline__ void col_pass(const float2* __restrict__ P, int rb, int g, int col,
                                          const TapBlock& tp, float (&fx)[kColRows],
                                          float (&fy)[kColRows])
 {
@@ -225,7 +226,7 @@ __device__ __forceinline__ void col_pass(const float2* __restrict__ P, int rb, i
     const int r0 = rb + g * kColRows + 1;
 #pragma unroll
     for (int t = 0; t < kColRows + 2 * R + 2; ++t) {
-        const float2 h = P[ring_wrap<C::RING>(r0 + t) * kExt + lane];
+        const float2 h = P[ring_wrap<C::RING>(r0 + t) * kExt + col];
 #pragma unroll
         for (int o = 0; o < kColRows; ++o) {
             const int p = o + R + 1 - t;
@@ -253,7 +254,8 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 {
     NmsEval r;
     r.cand = false;
-    const float2 g = sFxy[m * 64 + c];
+    constexpr int FW = 2 * kExt;
+    const float2 g = sFxy[m * FW + c];
     r.mv = grad_mag(g);
     if (!(r.mv > thr)) return r;  // cpu_toed.cpp:403 (also rejects NaN)
     r.gx = g.x;
@@ -268,10 +270,10 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     const int sx = (g.x >= 0.f) ? 1 : -1, sy = (g.y >= 0.f) ? 1 : -1;
     r.slope = xmaj ? __fdividef(fabsf(r.ny), fabsf(r.nx)) : __fdividef(fabsf(r.nx), fabsf(r.ny));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
-    r.Map = grad_mag(sFxy[(m + ar) * 64 + c + ac]);
-    r.Mdp = grad_mag(sFxy[(m + sy) * 64 + c + sx]);
-    r.Mam = grad_mag(sFxy[(m - ar) * 64 + c - ac]);
-    r.Mdm = grad_mag(sFxy[(m - sy) * 64 + c - sx]);
+    r.Map = grad_mag(sFxy[(m + ar) * FW + c + ac]);
+    r.Mdp = grad_mag(sFxy[(m + sy) * FW + c + sx]);
+    r.Mam = grad_mag(sFxy[(m - ar) * FW + c - ac]);
+    r.Mdm = grad_mag(sFxy[(m - sy) * FW + c - sx]);
     const float fp = r.Map * (1.f - r.slope) + r.Mdp * r.slope;
     const float fm = r.Mam * (1.f - r.slope) + r.Mdm * r.slope;
     const float mv = r.mv;
@@ -351,6 +353,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
     using C = Cfg<R>;
     constexpr int B = C::B;
     constexpr int NT = C::NT;
+    static_assert(kThreads / 32 == 8 * kHalves, "column pass: one warp per (sub-grid, 8-row group, half)");
+    static_assert(2 * B == 32, "row scans: one lane per NMS row");
     extern __shared__ __align__(16) unsigned char smem[];
     float* sIn = reinterpret_cast<float*>(smem + C::off_in);
     float2* sP = reinterpret_cast<float2*>(smem + C::off_P);
@@ -362,8 +366,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
     float* sRec = reinterpret_cast<float*>(smem + C::off_rec);
     int* sRowOff = sMisc + 32;   // [32]
     int* sAccCnt = sMisc + 64;   // [32] accepted edgels per NMS row
-    int* sWarp = sMisc + 96;     // [2][8] warp counts of the NMS compaction
-    int* sScal = sMisc + 112;    // [0] unit [1] staging refill [2] list length
+    int* sWarp = sMisc + 96;     // [2][16] warp counts of the NMS compaction
+    int* sScal = sMisc + 128;    // [0] unit [1] staging refill [2] list length
     unsigned char* sRaw = smem + C::off_raw;  // TMA destination: one box of input rows
     const uint32_t bar = smem_addr(smem + C::off_mbar);
     uint32_t phase = 0;
@@ -414,8 +418,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         const int gc_base = 2 * (x0 - 1);
 
         // 2x-grid rows 0 and 1 of the NMS window start empty
-        for (int i = tid; i < 2 * 64; i += kThreads) sFxy[i] = make_float2(0.f, 0.f);
-        if (tid < 4) sMask[tid] = 0u;
+        for (int i = tid; i < 2 * C::FW; i += kThreads) sFxy[i] = make_float2(0.f, 0.f);
+        if (tid < 4 * kHalves) sMask[tid] = 0u;
 
         int rb = 0;
         for (int s = 0; s < nsteps; ++s) {
@@ -433,29 +437,33 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     // the previous chunk, steady-state boxes at the end of the previous step
                     if (s == 0 && ch == 0 && tid == 0)
                         tma_load_rows(&p.tmap[k], smem_addr(sRaw), bar, x_al, row0, (uint32_t)(B * rawpitch));
-                    bool ok = mbar_wait(bar, phase);
+                    // no barrier before the conversion: the input ring rows it
+                    // writes are read only by this step's row pass, so threads
+                    // still busy with the previous step's gather join late
+                    const bool ok = mbar_wait(bar, phase);
                     phase ^= 1u;
+                    const int nrows = min(B, C::HS - ((s == 0) ? ch * B : 0));
+                    const int a0 = (s == 0) ? ch * B : rb + 2 * R + 3;  // ring row of box row 0 (before wrapping)
+                    if (ok) {
+                        if (dtype == TOED_U8) {
+                            for (int i = tid; i < nrows * C::NIN; i += kThreads) {
+                                const int rr = i / C::NIN, cc = i - rr * C::NIN;
+                                sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = (float)sRaw[rr * rawpitch + shift + cc];
+                            }
+                        } else {
+                            const float* rf = reinterpret_cast<const float*>(sRaw);
+                            for (int i = tid; i < nrows * C::NIN; i += kThreads) {
+                                const int rr = i / C::NIN, cc = i - rr * C::NIN;
+                                sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = rf[rr * im.tma_boxw + shift + cc];
+                            }
+                        }
+                    }
                     if (__syncthreads_or(!ok)) {
                         // give up on this CTA: flag it, drain the copy in flight, leave
                         if (tid == 0) atomicOr(&p.sc.words[2], TOED_FLAG_TIMEOUT);
                         mbar_wait(bar, phase ^ 1u);
                         return;
                     }
-                    const int nrows = min(B, C::HS - ((s == 0) ? ch * B : 0));
-                    const int a0 = (s == 0) ? ch * B : rb + 2 * R + 3;  // ring row of box row 0 (before wrapping)
-                    if (dtype == TOED_U8) {
-                        for (int i = tid; i < nrows * C::NIN; i += kThreads) {
-                            const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                            sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = (float)sRaw[rr * rawpitch + shift + cc];
-                        }
-                    } else {
-                        const float* rf = reinterpret_cast<const float*>(sRaw);
-                        for (int i = tid; i < nrows * C::NIN; i += kThreads) {
-                            const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                            sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = rf[rr * im.tma_boxw + shift + cc];
-                        }
-                    }
-                    __syncthreads();
                     if (s == 0 && ch + 1 < nch && tid == 0)
                         tma_load_rows(&p.tmap[k], smem_addr(sRaw), bar, x_al, row0 + B, (uint32_t)(B * rawpitch));
                 }
@@ -479,46 +487,51 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             } else {
                 row_pass<R>(sIn, ring_wrap<C::RING>(rb + 2 * R + 3), B, sP, tp);
                 // the previous step's last two 2x rows become rows 0 and 1
-                for (int i = tid; i < 2 * 64; i += kThreads) sFxy[i] = sFxy[2 * B * 64 + i];
-                if (tid < 4) sMask[tid] = sMask[2 * B * 2 + tid];
+                for (int i = tid; i < 2 * C::FW; i += kThreads) sFxy[i] = sFxy[2 * B * C::FW + i];
+                if (tid < 4 * kHalves) sMask[tid] = sMask[2 * B * 2 * kHalves + tid];
             }
             __syncthreads();
             // ---- 3. column pass: Ix, Iy for 2x rows m = 2..2B+1, and the
             // threshold test as ballots over the strip's columns
             const int gr_base = 2 * ys - 4 + 2 * s * B;  // global 2x row of NMS row m: gr_base + m
             {
-                const int sg = wid & 3, g = wid >> 2;
+                // warp -> (sub-grid, 8-row group, 32-column half of the strip)
+                const int sg = wid & 3, g = (wid >> 2) & 1, h = wid >> 3;
                 const int a = sg >> 1, b = sg & 1;
+                const int col = 32 * h + lane;  // ext column
                 float fx[kColRows], fy[kColRows];
                 // sub-grid (a, b): x taps T / F / S for (0,0) / (1,0) / (.,1),
                 // y taps truncated for (0,0), full for (0,1), shifted for (1,.)
                 const float2* P = sP + (sg == 0 ? 0 : (sg == 2 ? 1 : 2)) * C::RING * kExt;
                 if (sg == 0)
-                    col_pass<R, 0>(P, rb, g, lane, tp, fx, fy);
+                    col_pass<R, 0>(P, rb, g, col, tp, fx, fy);
                 else if (sg == 1)
-                    col_pass<R, 1>(P, rb, g, lane, tp, fx, fy);
+                    col_pass<R, 1>(P, rb, g, col, tp, fx, fy);
                 else
-                    col_pass<R, 2>(P, rb, g, lane, tp, fx, fy);
-                const int c = 2 * lane + b, Gc = gc_base + c;
-                const bool colok = lane >= 1 && lane <= kInner && Gc >= col_lo && Gc < col_hi;
+                    col_pass<R, 2>(P, rb, g, col, tp, fx, fy);
+                const int c = 2 * col + b, Gc = gc_base + c;
+                const bool colok = col >= 1 && col <= kInner && Gc >= col_lo && Gc < col_hi;
 #pragma unroll
                 for (int o = 0; o < kColRows; ++o) {
                     const int m = 2 * (g * kColRows + o) + a + 2;
                     const float2 f = make_float2(fx[o], fy[o]);
-                    sFxy[m * 64 + c] = f;
+                    sFxy[m * C::FW + c] = f;
                     const int Gr = gr_base + m;
                     const bool kp = colok && Gr >= row_lo && Gr < row_hi && grad_mag(f) > p.thr;  // cpu_toed.cpp:403
                     const unsigned bal = __ballot_sync(0xffffffffu, kp);
-                    if (lane == 0) sMask[m * 2 + b] = bal;
+                    if (lane == 0) sMask[(m * 2 + b) * kHalves + h] = bal;
                 }
             }
             if (tid < 32) sAccCnt[tid] = 0;
             __syncthreads();
             // ---- 4a. points above the threshold, listed in row-major order ---
-            // NMS rows m = 1..2B; bit L of a mask <-> 2x column 2L + parity.
-            // Warp 0 counts and scans the rows (lane L <-> row L + 1).
+            // NMS rows m = 1..2B; mask (m, parity, half): bit L <-> 2x column
+            // 2 (32 half + L) + parity.  Warp 0 counts and scans the rows
+            // (lane L <-> row L + 1).
             if (wid == 0) {
-                const int cnt = __popc(sMask[(lane + 1) * 2]) + __popc(sMask[(lane + 1) * 2 + 1]);
+                int cnt = 0;
+#pragma unroll
+                for (int q = 0; q < 2 * kHalves; ++q) cnt += __popc(sMask[(lane + 1) * 2 * kHalves + q]);
                 int incl = cnt;
 #pragma unroll
                 for (int d = 1; d < 32; d <<= 1) {
@@ -531,15 +544,18 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             __syncthreads();
             {
                 const unsigned lt = (1u << lane) - 1u;
+                for (int m = 1 + wid; m <= 2 * B; m += kThreads / 32) {
+                    int pos0 = sRowOff[m - 1];
 #pragma unroll
-                for (int t = 0; t < 4; ++t) {
-                    const int m = 1 + wid + 8 * t;
-                    const unsigned mk0 = sMask[m * 2], mk1 = sMask[m * 2 + 1];
-                    const bool k0 = (mk0 >> lane) & 1u, k1 = (mk1 >> lane) & 1u;
-                    const int pos = sRowOff[m - 1] + __popc(mk0 & lt) + __popc(mk1 & lt);
-                    const unsigned c0 = 2 * lane;
-                    if (k0) sList[pos] = ((unsigned)m << 8) | c0;
-                    if (k1) sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
+                    for (int h = 0; h < kHalves; ++h) {
+                        const unsigned mk0 = sMask[(m * 2) * kHalves + h], mk1 = sMask[(m * 2 + 1) * kHalves + h];
+                        const bool k0 = (mk0 >> lane) & 1u, k1 = (mk1 >> lane) & 1u;
+                        const int pos = pos0 + __popc(mk0 & lt) + __popc(mk1 & lt);
+                        const unsigned c0 = 2 * (32 * h + lane);
+                        if (k0) sList[pos] = ((unsigned)m << 8) | c0;
+                        if (k1) sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
+                        pos0 += __popc(mk0) + __popc(mk1);
+                    }
                 }
             }
             __syncthreads();
@@ -558,7 +574,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr).cand;
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
-                int* wc = sWarp + 8 * rd;
+                int* wc = sWarp + (kThreads / 32) * rd;
                 if (lane == 0) wc[wid] = __popc(bal);
                 __syncthreads();
                 int off = 0, tot = 0;
