@@ -161,6 +161,9 @@ typedef struct toed_subpix_params {
     float nbr_radius;  /* drop edgels with no other edgel within this distance; <= 0 keeps all (default 2) */
     int out_dtype;     /* TOED_F32 or TOED_F64 */
     int precision;     /* TOED_HYBRID: FP64 peak fit and orientation correction per edgel */
+    int interp_n;      /* 0..4: work on the 2^n grid ((h-1) 2^n + 1 rows), the map (and theta)
+                          bilinearly resized onto it; positions in original pixels
+                          (the reference's interp_n, subpix_to_correction.cpp:95-105, :224-244) */
 } toed_subpix_params;
 
 toed_status toed_subpix_to_correct_batch(toed_ctx* ctx, const toed_edgemap* maps, int n_maps,
@@ -191,11 +194,13 @@ toed_status toed_detect_noalloc(const toed_image* image, const toed_params* para
  * image in, detect, copy the edgel list back, gpu_toed.hpp:141-231 and
  * :415-441) for a whole batch, pipelined: the batch is cut into `chunks`
  * groups of consecutive images with similar pixel counts; the copy of group
- * k+1 to the device overlaps the detection of group k and the copy back of
- * group k-1 (three streams of the context, ordered by events).  Synchronous:
- * returns when every count and list is in host memory.  Device staging for
- * the images and lists is kept in the context and grows on demand.  Host
- * buffers should be page-locked for full copy speed.  Returns
+ * k+1 to the device overlaps the detection of group k (streams of the
+ * context, ordered by events).  Page-locked output buffers (edgels, count,
+ * grid_index) are written by the detection's ordering pass directly through
+ * their device mapping; pageable ones are filled by copies per group once its
+ * counts are read back.  Synchronous: returns when every count and list is in
+ * host memory.  Device staging is kept in the context and grows on demand.
+ * Page-locked image buffers give full copy speed.  Returns
  * TOED_ERR_TIMEOUT if a bounded device wait gave up; more edgels than
  * `capacity` show as count > capacity (the list holds the first capacity). */
 typedef struct toed_host_image {

@@ -63,6 +63,10 @@ def lib():
             _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double, _dp,
             ctypes.c_int, _dp, ctypes.c_long, _dp, _dp, _dp, _dp, _dp]
         L.subpix_oracle_run.restype = ctypes.c_long
+        L.subpix_oracle_run_n.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_double,
+            _dp, ctypes.c_int, _dp, ctypes.c_long, _dp, _dp, _dp, _dp, _dp]
+        L.subpix_oracle_run_n.restype = ctypes.c_long
         L.subpix_oracle_kernels.argtypes = [ctypes.c_double, _dp]
         L.subpix_oracle_kernels.restype = ctypes.c_int
         _LIB = L
@@ -122,22 +126,26 @@ def planes9(img, sigma: float = 2.0, r: int | None = None, nthreads: int = 0):
 
 
 def subpix_to_correct(E, thresh: float = 0.1, sigma: float = 2.0, nbr_radius: float = 2.0,
-                      theta=None, nthreads: int = 0, dense: bool = False, debug: bool = False):
-    """FP64 subpixel TO correction (interp_n = 0).  Returns dict(edges=(N,4)
-    [, TO_E, TO_O] [, nms=(4,h,w), theta=(h,w), planes10=(10,h,w)])."""
+                      theta=None, nthreads: int = 0, dense: bool = False, debug: bool = False,
+                      interp_n: int = 0):
+    """FP64 subpixel TO correction on the 2^interp_n work grid.  Returns
+    dict(edges=(N,4) [, TO_E, TO_O (original size)] [, nms=(4,hw,ww),
+    theta=(hw,ww), planes10=(10,hw,ww) on the work grid])."""
     E = np.ascontiguousarray(E, dtype=np.float64)
     h, w = E.shape
+    sc = 1 << max(int(interp_n), 0)
+    hw, ww = (h - 1) * sc + 1, (w - 1) * sc + 1
     th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
-    cap = h * w
+    cap = hw * ww
     edges = np.zeros((cap, 4), np.float64)
     TE = np.zeros((h, w)) if dense else None
     TO = np.zeros((h, w)) if dense else None
-    nms = np.zeros((4, h, w)) if debug else None
-    tho = np.zeros((h, w)) if debug else None
-    p10 = np.zeros((10, h, w)) if debug else None
-    n = lib().subpix_oracle_run(_ptr(E), h, w, float(thresh), float(sigma), float(nbr_radius),
-                                _ptr(th), int(nthreads), _ptr(edges), cap, _ptr(TE), _ptr(TO),
-                                _ptr(nms), _ptr(tho), _ptr(p10))
+    nms = np.zeros((4, hw, ww)) if debug else None
+    tho = np.zeros((hw, ww)) if debug else None
+    p10 = np.zeros((10, hw, ww)) if debug else None
+    n = lib().subpix_oracle_run_n(_ptr(E), h, w, int(interp_n), float(thresh), float(sigma), float(nbr_radius),
+                                  _ptr(th), int(nthreads), _ptr(edges), cap, _ptr(TE), _ptr(TO),
+                                  _ptr(nms), _ptr(tho), _ptr(p10))
     out = {"edges": edges[:n].copy()}
     if dense:
         out["TO_E"], out["TO_O"] = TE, TO
@@ -165,6 +173,10 @@ def ref_lib():
             _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
             ctypes.c_double, _dp, ctypes.c_char_p, _dp, ctypes.c_long, _dp, _dp, _dp, _dp]
         L.ref_subpix_to_correct.restype = ctypes.c_long
+        L.ref_subpix_to_correct_n.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+            ctypes.c_double, _dp, ctypes.c_char_p, _dp, ctypes.c_long, _dp, _dp]
+        L.ref_subpix_to_correct_n.restype = ctypes.c_long
         _REF = L
     return _REF
 
@@ -210,3 +222,20 @@ def ref_subpix_to_correct(E, thresh=0.1, sigma=2.0, nbr_radius=2.0, theta=None, 
     if dense:
         out["TO_E"], out["TO_O"] = TE, TO
     return out
+
+
+def ref_subpix_to_correct_n(E, interp_n, thresh=0.1, sigma=2.0, nbr_radius=2.0, theta=None, nthreads=0):
+    """The reference's SubpixelTOCorrectionCPU<double> at interp_n (dense maps included)."""
+    E = np.ascontiguousarray(E, dtype=np.float64)
+    h, w = E.shape
+    sc = 1 << int(interp_n)
+    cap = ((h - 1) * sc + 1) * ((w - 1) * sc + 1)
+    th = None if theta is None else np.ascontiguousarray(theta, dtype=np.float64)
+    edges = np.zeros((cap, 4))
+    TE, TO = np.zeros((h, w)), np.zeros((h, w))
+    nt = nthreads if nthreads > 0 else os.cpu_count()
+    with tempfile.TemporaryDirectory() as d:
+        n = ref_lib().ref_subpix_to_correct_n(_ptr(E), h, w, int(interp_n), float(thresh), float(sigma), nt,
+                                              float(nbr_radius), _ptr(th), d.encode(), _ptr(edges), cap,
+                                              _ptr(TE), _ptr(TO))
+    return {"edges": edges[:n].copy(), "TO_E": TE, "TO_O": TO}

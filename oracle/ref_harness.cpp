@@ -116,4 +116,27 @@ long ref_subpix_to_correct(const double* E, int h, int w, double thresh, double 
     return N;
 }
 
+// The same at interp_n >= 0 (the map resized onto the 2^n work grid by the
+// class itself, set_edgemap :224-233).  TO_E / TO_O: optional, h*w.
+long ref_subpix_to_correct_n(const double* E, int h, int w, int interp_n, double thresh, double sigma,
+                             int nthreads, double nbr_radius, const double* theta, const char* scratch_dir,
+                             double* edges, long capacity, double* TO_E, double* TO_O)
+{
+    SubpixelTOCorrectionCPU<double> tc(h, w, thresh, sigma, nthreads, interp_n);
+    tc.set_output_dir(scratch_dir ? scratch_dir : ".");
+    tc.set_neighbor_radius(nbr_radius);
+    tc.set_edgemap(E);
+    if (theta)
+        tc.set_orientation(theta);
+    else
+        tc.estimate_orientation();
+    std::vector<double> buf((size_t)tc.work_height * tc.work_width * 4, 0.0);
+    int N = tc.run(buf.data());
+    long nw = N < capacity ? N : capacity;
+    if (nw > 0) std::memcpy(edges, buf.data(), sizeof(double) * 4 * nw);
+    if (TO_E) std::memcpy(TO_E, tc.TO_edgemap, sizeof(double) * (size_t)h * w);
+    if (TO_O) std::memcpy(TO_O, tc.TO_orientation, sizeof(double) * (size_t)h * w);
+    return N;
+}
+
 }  // extern "C"

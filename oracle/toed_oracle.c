@@ -500,6 +500,26 @@ static double interp2_cubic(const double *src, int h, int w, double x, double y)
     return acc;
 }
 
+/* bilinear_resize :69-90 -- corner-aligned resize to the 2^n work grid */
+static void bilinear_resize(const double *src, int sh, int sw, double *dst, int dh, int dw)
+{
+    for (int i = 0; i < dh; i++) {
+        const double y = (dh == 1) ? 0 : (double)i * (sh - 1) / (double)(dh - 1);
+        const int y0 = (int)floor(y);
+        const int y1 = (y0 + 1 < sh - 1) ? y0 + 1 : sh - 1;
+        const double fy = y - y0;
+        for (int j = 0; j < dw; j++) {
+            const double x = (dw == 1) ? 0 : (double)j * (sw - 1) / (double)(dw - 1);
+            const int x0 = (int)floor(x);
+            const int x1 = (x0 + 1 < sw - 1) ? x0 + 1 : sw - 1;
+            const double fx = x - x0;
+            const double v00 = src[(size_t)y0 * sw + x0], v01 = src[(size_t)y0 * sw + x1];
+            const double v10 = src[(size_t)y1 * sw + x0], v11 = src[(size_t)y1 * sw + x1];
+            dst[(size_t)i * dw + j] = (1 - fy) * ((1 - fx) * v00 + fx * v01) + fy * ((1 - fx) * v10 + fx * v11);
+        }
+    }
+}
+
 /*
  * Whole TO-correction pipeline (run :623-736 after set_edgemap / optional
  * set_orientation or estimate_orientation).
@@ -509,13 +529,32 @@ static double interp2_cubic(const double *src, int h, int w, double x, double y)
  *   (nms_x, nms_y, nms_mag, valid) for plane-level tests; theta_out: optional.
  * Returns N after isolated-edgel removal.
  */
-long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigma,
-                       double nbr_radius, const double *theta_in, int nthreads, double *edges,
-                       long capacity, double *TO_E, double *TO_O, double *nms_out,
-                       double *theta_out, double *planes10)
+long subpix_oracle_run_n(const double *E_in, int h0, int w0, int interp_n, double thresh, double sigma,
+                         double nbr_radius, const double *theta_in0, int nthreads, double *edges,
+                         long capacity, double *TO_E, double *TO_O, double *nms_out,
+                         double *theta_out, double *planes10)
 {
     if (nthreads > 0) omp_set_num_threads(nthreads);
-    const size_t n = (size_t)h * w;
+    /* interp_n > 0: the work grid is (h0-1) 2^n + 1 by (w0-1) 2^n + 1, the
+     * map (and a given orientation) bilinearly resized onto it
+     * (set_edgemap / set_orientation :224-244), the NMS margin 3 * 2^n
+     * (:628-630), positions divided by 2^n (:657, :696-697) and the dense
+     * maps kept at the original size (:707-715). */
+    const int sc = 1 << (interp_n > 0 ? interp_n : 0);
+    const int h = (h0 - 1) * sc + 1, w = (w0 - 1) * sc + 1;
+    const size_t n = (size_t)h * w, n0 = (size_t)h0 * w0;
+    double *E_work = NULL, *th_work = NULL;
+    const double *E = E_in, *theta_in = theta_in0;
+    if (sc > 1) {
+        E_work = (double *)malloc(n * sizeof(double));
+        bilinear_resize(E_in, h0, w0, E_work, h, w);
+        E = E_work;
+        if (theta_in0) {
+            th_work = (double *)malloc(n * sizeof(double));
+            bilinear_resize(theta_in0, h0, w0, th_work, h, w);
+            theta_in = th_work;
+        }
+    }
     const int rad = (int)ceil(sigma * 4);
     const int ksz = 2 * rad + 1;
     double *k3 = (double *)malloc(sizeof(double) * 3 * ksz);
@@ -537,8 +576,8 @@ long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigm
         diry[k] = sin(a);
     }
 
-    /* nms_token(margin = 3) :413-519 */
-    const int margin = 3;
+    /* nms_token(margin = 3 * 2^n) :413-519 */
+    const int margin = 3 * sc;
     double *nx_ = (double *)calloc(n, sizeof(double));
     double *ny_ = (double *)calloc(n, sizeof(double));
     double *nm_ = (double *)calloc(n, sizeof(double));
@@ -636,8 +675,8 @@ long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigm
                 Fy /= Fm;
                 ori = atan2(Fx, -Fy);
             }
-            L[4 * m + 0] = sx; /* coord_scale = 1 for interp_n = 0 */
-            L[4 * m + 1] = sy;
+            L[4 * m + 0] = sx / (double)sc; /* coord_scale :696-697 */
+            L[4 * m + 1] = sy / (double)sc;
             L[4 * m + 2] = ori;
             L[4 * m + 3] = mag_e;
             m++;
@@ -707,15 +746,15 @@ long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigm
     }
 
     /* dense TO maps :708-715 (later edgels overwrite earlier ones) */
-    if (TO_E) memset(TO_E, 0, n * sizeof(double));
-    if (TO_O) memset(TO_O, 0, n * sizeof(double));
+    if (TO_E) memset(TO_E, 0, n0 * sizeof(double));
+    if (TO_O) memset(TO_O, 0, n0 * sizeof(double));
     for (long k = 0; k < kept; k++) {
         int X = (int)round(L[4 * k + 0]);
         int Y = (int)round(L[4 * k + 1]);
-        X = X < 0 ? 0 : (X > w - 1 ? w - 1 : X);
-        Y = Y < 0 ? 0 : (Y > h - 1 ? h - 1 : Y);
-        if (TO_E) TO_E[(size_t)Y * w + X] = L[4 * k + 3];
-        if (TO_O) TO_O[(size_t)Y * w + X] = L[4 * k + 2];
+        X = X < 0 ? 0 : (X > w0 - 1 ? w0 - 1 : X);
+        Y = Y < 0 ? 0 : (Y > h0 - 1 ? h0 - 1 : Y);
+        if (TO_E) TO_E[(size_t)Y * w0 + X] = L[4 * k + 3];
+        if (TO_O) TO_O[(size_t)Y * w0 + X] = L[4 * k + 2];
     }
     for (long k = 0; k < kept && k < capacity; k++) memcpy(&edges[4 * k], &L[4 * k], 4 * sizeof(double));
 
@@ -732,5 +771,16 @@ long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigm
     free(tmp);
     free(P);
     free(L);
+    free(E_work);
+    free(th_work);
     return kept;
+}
+
+long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigma,
+                       double nbr_radius, const double *theta_in, int nthreads, double *edges,
+                       long capacity, double *TO_E, double *TO_O, double *nms_out,
+                       double *theta_out, double *planes10)
+{
+    return subpix_oracle_run_n(E, h, w, 0, thresh, sigma, nbr_radius, theta_in, nthreads, edges, capacity,
+                               TO_E, TO_O, nms_out, theta_out, planes10);
 }

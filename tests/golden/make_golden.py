@@ -14,7 +14,11 @@ Fixtures (all .npz):
   (FP64, N x 4) from ThirdOrderEdgeDetectionCPU<double> at sigma 2 / kernel 17,
   and for small cases its Ix / Iy / |grad| / orientation planes.
 * ``subpix_<case>``    -- edge map, optional orientation, the reference's
-  SubpixelTOCorrectionCPU<double> edgel list and dense TO maps.
+  SubpixelTOCorrectionCPU<double> edgel list and dense TO maps; the
+  ``_n1`` / ``_n2`` cases run it on the 2^n work grid (interp_n = 1, 2) and
+  store interp_n as the fourth parameter.
+
+``--only PREFIX`` regenerates just the fixtures whose name starts with PREFIX.
 """
 from __future__ import annotations
 
@@ -71,13 +75,18 @@ def kat_images():
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--only", default="", help="regenerate only fixtures whose name starts with this")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={args.ref_dir}"],
                    check=True)
     import oracle
     synth = _synth()
 
-    np.savez_compressed(os.path.join(HERE, "ref_taps_sigma2.npz"), taps=literal_taps(args.ref_dir))
+    def want(name):
+        return name.startswith(args.only)
+
+    if want("ref_taps_sigma2"):
+        np.savez_compressed(os.path.join(HERE, "ref_taps_sigma2.npz"), taps=literal_taps(args.ref_dir))
 
     cases = dict(kat_images())
     cases["shapes_37x53"] = synth.shapes_image(37, 53, seed=11).image
@@ -86,6 +95,8 @@ def main():
     cases["shapes_150x97"] = synth.shapes_image(150, 97, seed=14, noise_std=6.0).image
     cases["shapes_752x480"] = synth.shapes_image(480, 752, seed=1).image
     for name, img in cases.items():
+        if not want(f"toed_{name}"):
+            continue
         small = img.size <= 64 * 64
         r = oracle.ref_detect_u8(img, planes=small)
         d = {"image": img, "edges": r["edges"]}
@@ -102,6 +113,8 @@ def main():
         "ridges_80x90_s15_r0": (synth.ridge_map(80, 90, seed=24, n_curves=4), None, 0.15, 1.5, 0.0),
     }
     for name, (E, th, thresh, sigma, rad) in sub.items():
+        if not want(f"subpix_{name}"):
+            continue
         E = E.astype(np.float64)
         r = oracle.ref_subpix_to_correct(E, thresh, sigma, rad, theta=th, dense=True)
         d = {"E": E, "edges": r["edges"], "TO_E": r["TO_E"], "TO_O": r["TO_O"], "theta": r["theta"],
@@ -110,6 +123,25 @@ def main():
             d["theta_in"] = th
         np.savez_compressed(os.path.join(HERE, f"subpix_{name}.npz"), **d)
         print(f"subpix_{name}: {E.shape} -> {len(r['edges'])} edgels")
+
+    # the 2^n work grid (interp_n > 0): bilinear resize, scaled margin, positions / 2^n
+    sub_n = {
+        "ridges_60x72_est_n1": (synth.ridge_map(60, 72, seed=25, n_curves=4), None, 0.1, 2.0, 2.0, 1),
+        "ridges_48x56_theta_n2": (synth.ridge_map(48, 56, seed=26, n_curves=3),
+                                  np.random.Generator(np.random.PCG64(27)).uniform(0, 3, (48, 56)),
+                                  0.1, 1.5, 2.0, 2),
+    }
+    for name, (E, th, thresh, sigma, rad, n) in sub_n.items():
+        if not want(f"subpix_{name}"):
+            continue
+        E = E.astype(np.float64)
+        r = oracle.ref_subpix_to_correct_n(E, n, thresh, sigma, rad, theta=th)
+        d = {"E": E, "edges": r["edges"], "TO_E": r["TO_E"], "TO_O": r["TO_O"],
+             "params": np.array([thresh, sigma, rad, n])}
+        if th is not None:
+            d["theta_in"] = th
+        np.savez_compressed(os.path.join(HERE, f"subpix_{name}.npz"), **d)
+        print(f"subpix_{name}: {E.shape} (interp_n {n}) -> {len(r['edges'])} edgels")
 
 
 if __name__ == "__main__":

@@ -273,11 +273,13 @@ def test_autotune_and_launch_shapes_agree(toed, synth):
         assert int(o["count"].item()) == n0 and t.equal(o["edgels"][:n0].cpu(), e0)
 
 
-@pytest.mark.parametrize("chunks", [1, 3])
-def test_host_batch_matches_device_batch(toed, synth, chunks):
+@pytest.mark.parametrize("chunks,pin", [(1, True), (3, True), (3, False)])
+def test_host_batch_matches_device_batch(toed, synth, chunks, pin):
     """toed_detect_host_batch (host buffers, pipelined copies) returns the same
     lists as the device-buffer batch, for uint8 / float32, a host pitch wider
-    than the image, and a capacity smaller than the edgel count."""
+    than the image, and a capacity smaller than the edgel count -- with
+    page-locked outputs (written through their device mapping) and pageable
+    ones (copied back)."""
     t = _torch()
     det = toed.Detector(0)
     sizes = [(200, 300), (97, 1000), (333, 129), (64, 64), (450, 211)]
@@ -290,7 +292,7 @@ def test_host_batch_matches_device_batch(toed, synth, chunks):
     host[0] = wide[:, :sizes[0][1]]  # pitch > width in host memory
     prm = toed.make_params(1.5)
     ref = det.detect_batch([im.contiguous().cuda() for im in host], sigma=1.5)
-    outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True)
+    outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True, pin=pin)
     small = 3  # image 3: capacity below its edgel count
     outs[small]["capacity"] = max(1, ref[small]["count"] // 2)
     det.detect_host(host, outs, prm, chunks=chunks)

@@ -53,9 +53,11 @@ def _run(detector, E, thresh, sigma, rad, theta=None, **kw):
 @pytest.mark.parametrize("dt", [np.float64, np.float32])
 def test_golden(detector, toed, case, dt):
     g = golden("subpix_" + case)
-    thresh, sigma, rad = g["params"]
+    thresh, sigma, rad = g["params"][:3]
+    interp_n = int(g["params"][3]) if len(g["params"]) > 3 else 0
     th = g["theta_in"].astype(dt) if "theta_in" in g else None
-    r = _run(detector, g["E"].astype(dt), thresh, sigma, rad, theta=th, out_dtype=toed.TOED_F64)
+    r = _run(detector, g["E"].astype(dt), thresh, sigma, rad, theta=th, out_dtype=toed.TOED_F64,
+             interp_n=interp_n)
     got = r["edgels"].cpu().numpy()
     assert r["count"] == len(got)
     _check(g["edges"], got)
@@ -87,3 +89,19 @@ def test_batch_and_fp32_mode(detector, oracle, synth, toed):
                                            nbr_radius=2.0, precision=toed.TOED_FP32)[0]
     ref = oracle.subpix_to_correct(maps[0].astype(np.float64), 0.1, 2.0, 2.0)
     _check(ref["edges"], r32["edgels"].double().cpu().numpy(), ori=2e-3, mag=1e-3)
+
+
+@pytest.mark.parametrize("interp_n,est", [(1, True), (2, False)])
+def test_work_grid_vs_oracle(detector, oracle, synth, toed, interp_n, est):
+    """interp_n > 0: the map (and orientation) resized onto the 2^n work grid."""
+    E = synth.ridge_map(90, 110, seed=60 + interp_n, n_curves=5).astype(np.float32)
+    th = None if est else np.random.default_rng(61).uniform(0, 3, E.shape).astype(np.float32)
+    ref = oracle.subpix_to_correct(E.astype(np.float64), 0.1, 2.0, 2.0,
+                                   theta=None if th is None else th.astype(np.float64), dense=True,
+                                   interp_n=interp_n)
+    r = _run(detector, E, 0.1, 2.0, 2.0, theta=th, out_dtype=toed.TOED_F64, interp_n=interp_n)
+    assert len(ref["edges"]) > 100
+    _check(ref["edges"], r["edgels"].cpu().numpy())
+    TE = r["TO_E"].cpu().numpy()
+    assert TE.shape == E.shape
+    assert ((TE != 0) != (ref["TO_E"] != 0)).sum() <= max(2, 0.002 * (ref["TO_E"] != 0).sum())

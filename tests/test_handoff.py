@@ -52,10 +52,12 @@ def test_text_writer_gpu_format(toed, tmp_path):
 @pytest.mark.parametrize("dt", ["float32", "float64"])
 def test_curvelet_columns(toed, synth, dt):
     import torch
-    img = torch.as_tensor(synth.shapes_image(120, 160, seed=5, dtype=np.float32).image).cuda()
+    img = torch.as_tensor(synth.shapes_image(120, 160, seed=5, n_shapes=6, radius_range=(10, 40),
+                                             scale_to_base=False, dtype=np.float32).image).cuda()
     out_dtype = toed.TOED_F64 if dt == "float64" else toed.TOED_F32
     r = toed.detect(img, sigma=1.5, out_dtype=out_dtype)
     e = r["edgels"].contiguous()
+    assert e.shape[0] > 50
     cm = toed.edgels_to_columns(e)
     torch.cuda.synchronize()
     ref = e.double().t().contiguous()  # column j of the list = row j of the (4, n) array

@@ -72,9 +72,10 @@ def test_toed_known_answers(oracle):
 @pytest.mark.parametrize("case", SUBPIX_CASES)
 def test_subpix_bit_exact(oracle, case):
     g = golden("subpix_" + case)
-    thresh, sigma, rad = g["params"]
+    thresh, sigma, rad = g["params"][:3]
+    interp_n = int(g["params"][3]) if len(g["params"]) > 3 else 0
     th = g["theta_in"] if "theta_in" in g else None
-    o = oracle.subpix_to_correct(g["E"], thresh, sigma, rad, theta=th, dense=True)
+    o = oracle.subpix_to_correct(g["E"], thresh, sigma, rad, theta=th, dense=True, interp_n=interp_n)
     assert np.array_equal(o["edges"], g["edges"], equal_nan=True)
     assert np.array_equal(o["TO_E"], g["TO_E"])
     assert np.array_equal(o["TO_O"], g["TO_O"])
@@ -110,3 +111,15 @@ def test_subpix_live_reference(oracle, synth, seed, est):
     assert np.array_equal(r["edges"], o["edges"], equal_nan=True)
     assert np.array_equal(r["TO_E"], o["TO_E"]) and np.array_equal(r["TO_O"], o["TO_O"])
     assert np.array_equal(r["theta"], o["theta"])
+
+
+@pytest.mark.parametrize("interp_n", [1, 2])
+def test_subpix_live_reference_interp(oracle, synth, interp_n):
+    """interp_n > 0: the reference resizes the map onto the 2^n work grid."""
+    _ref_or_skip(oracle)
+    E = synth.ridge_map(44, 52, seed=300 + interp_n, n_curves=3).astype(np.float64)
+    r = oracle.ref_subpix_to_correct_n(E, interp_n, 0.1, 2.0, 2.0)
+    o = oracle.subpix_to_correct(E, 0.1, 2.0, 2.0, dense=True, interp_n=interp_n)
+    assert len(r["edges"]) > 20
+    assert np.array_equal(r["edges"], o["edges"], equal_nan=True)
+    assert np.array_equal(r["TO_E"], o["TO_E"]) and np.array_equal(r["TO_O"], o["TO_O"])

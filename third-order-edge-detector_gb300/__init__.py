@@ -84,7 +84,7 @@ class toed_edgemap(ctypes.Structure):
 class toed_subpix_params(ctypes.Structure):
     _fields_ = [
         ("thresh", ctypes.c_float), ("sigma", ctypes.c_float), ("nbr_radius", ctypes.c_float),
-        ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
+        ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int), ("interp_n", ctypes.c_int),
     ]
 
 
@@ -421,11 +421,12 @@ class Detector:
 
     def subpix_to_correct_batch(self, maps, thresh=0.2, sigma=2.0, nbr_radius=2.0, thetas=None,
                                 out_dtype=TOED_F32, precision=TOED_HYBRID, capacity=None, dense=True,
-                                stream=None):
+                                stream=None, interp_n=0):
         """Subpixel TO correction of dense edge maps (2-D CUDA float32 /
-        float64 tensors), the reference's SubpixelTOCorrectionCPU<T>.
-        Returns dicts with ``edgels`` (N x 4: x, y, orientation, strength)
-        and, with ``dense``, ``TO_E`` / ``TO_O``."""
+        float64 tensors), the reference's SubpixelTOCorrectionCPU<T>; with
+        ``interp_n`` > 0 on its 2^n work grid.  Returns dicts with ``edgels``
+        (N x 4: x, y, orientation, strength) and, with ``dense``, ``TO_E`` /
+        ``TO_O`` (original size)."""
         t = self.torch
         dt = t.float64 if out_dtype == TOED_F64 else t.float32
         dev = f"cuda:{self.device}"
@@ -437,7 +438,7 @@ class Detector:
             if th is not None and (th.dtype != E.dtype or th.stride() != E.stride() or th.shape != E.shape):
                 raise ValueError("orientation map must match the edge map's dtype, shape and strides")
             h, w = E.shape
-            cap = int(capacity) if capacity is not None else h * w
+            cap = int(capacity) if capacity is not None else ((h - 1) * (1 << interp_n) + 1) * ((w - 1) * (1 << interp_n) + 1)
             o = {"edgels": t.empty((max(cap, 1), 4), dtype=dt, device=dev),
                  "count": t.zeros(1, dtype=t.int32, device=dev), "capacity": cap}
             if dense:
@@ -450,7 +451,8 @@ class Detector:
                                     o["TO_E"].data_ptr() if dense else None,
                                     o["TO_O"].data_ptr() if dense else None))
         a = (toed_edgemap * len(arr))(*arr)
-        prm = toed_subpix_params(float(thresh), float(sigma), float(nbr_radius), int(out_dtype), int(precision))
+        prm = toed_subpix_params(float(thresh), float(sigma), float(nbr_radius), int(out_dtype), int(precision),
+                                 int(interp_n))
         s = stream if stream is not None else t.cuda.current_stream(self.device)
         _check(lib().toed_subpix_to_correct_batch(self._ctx, a, len(arr), ctypes.byref(prm),
                                                   ctypes.c_void_p(s.cuda_stream)), "toed_subpix_to_correct_batch")

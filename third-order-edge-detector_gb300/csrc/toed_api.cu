@@ -83,6 +83,23 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
+// cuStreamWriteValue32 through the runtime's driver entry point (null when
+// unavailable): lets the copy stream mark each image as landed.
+static PFN_cuStreamWriteValue32_v11070 write_value_fn()
+{
+    static PFN_cuStreamWriteValue32_v11070 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* ptr = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &ptr, 11070, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuStreamWriteValue32_v11070>(ptr);
+    });
+    return fn;
+}
+
 void encode_rows_map(CUtensorMap* m, DetImage& d, int r)
 {
     d.tma = 0;
@@ -146,6 +163,8 @@ struct toed_ctx {
     long long img_count_cap = 0;
     unsigned char* keep = nullptr;
     long long keep_cap = 0;
+    double* sp_work = nullptr;  // TO correction at interp_n > 0: maps resized onto the work grid
+    long long sp_work_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
     // launch shape chosen by toed_autotune per (radius, precision); strip_rows 0 = heuristic
     toed_tuning tune[TOED_MAX_RADIUS + 1][2] = {};
@@ -164,6 +183,9 @@ struct toed_ctx {
     int* hb_cnt_host = nullptr;
     long long hb_cnt_host_cap = 0;
     cudaStream_t s_in = nullptr, s_out = nullptr;
+    unsigned* hb_ready = nullptr;  // per image: the copy stream writes the call's epoch after its copy
+    long long hb_ready_cap = 0;
+    unsigned hb_epoch = 0;
     std::mutex mu;
 };
 
@@ -238,10 +260,12 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->win);
     cudaFree(c->img_count);
     cudaFree(c->keep);
+    cudaFree(c->sp_work);
     cudaFree(c->hb_in);
     cudaFree(c->hb_out);
     cudaFree(c->hb_idx);
     cudaFree(c->hb_cnt);
+    cudaFree(c->hb_ready);
     if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
     if (c->s_in) cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamDestroy(c->s_out);
@@ -337,7 +361,8 @@ static int plan_strip_rows(const toed_image* images, int n, long long resident)
 }
 
 static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr)
+                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr,
+                                const unsigned* ready = nullptr, unsigned epoch = 0)
 {
     const bool hyb = prm->precision != TOED_FP32;
     DetectEntry ent = detect_entry(r, hyb);
@@ -361,6 +386,8 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->n_img = n;
     p->out_f64 = (prm->out_dtype == TOED_F64) ? 1 : 0;
     p->radius = r;
+    p->ready = ready;
+    p->ready_epoch = epoch;
     long long units = 0, tiles = 0, staging = 0;
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
@@ -437,12 +464,14 @@ static toed_status check_batch(const toed_ctx* c, const toed_image* images, int 
 
 // The batch in chunks of kBatchMax images (caller holds c->mu, device set).
 static toed_status detect_all(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                              cudaStream_t stream, const toed_tuning* force = nullptr)
+                              cudaStream_t stream, const toed_tuning* force = nullptr,
+                              const unsigned* ready = nullptr, unsigned epoch = 0)
 {
     const int r = radius_of(prm);
     toed_status st = TOED_OK;
     for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
-        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force);
+        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force,
+                          ready ? ready + i0 : nullptr, epoch);
     return st;
 }
 
@@ -546,8 +575,7 @@ extern "C" toed_status toed_detect(toed_ctx* c, const toed_image* image, const t
 
 // Host-memory batch, pipelined over `chunks` groups of images (see the
 // header).  Streams: s_in (H2D), the caller's stream (detection), s_out
-// (D2H); events order them per group.  The counts of group k are read on
-// the host before its lists are copied, while later groups still run.
+// (D2H, pageable outputs only); events order them per group.
 extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image* images, int n,
                                               const toed_params* prm, int chunks, cudaStream_t stream)
 {
@@ -617,18 +645,64 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     }
     if (!c->s_in) TOED_HB(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));
     if (!c->s_out) TOED_HB(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
+    // Page-locked host outputs are written by the ordering pass itself
+    // (mapped into the device's address space; coherent over the C2C link):
+    // no count read-back and no list copies.  Otherwise lists go through
+    // device staging and are copied back per group once its counts are known.
+    auto mapped = [](void* hp) -> void* {
+        cudaPointerAttributes a;
+        if (!hp || cudaPointerGetAttributes(&a, hp) != cudaSuccess) {
+            cudaGetLastError();
+            return nullptr;
+        }
+        return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    };
+    bool direct = true;
+    for (int i = 0; i < n && direct; ++i) {
+        void* e = mapped(images[i].edgels);
+        void* cn = mapped(images[i].count);
+        void* gi = images[i].grid_index ? mapped(images[i].grid_index) : nullptr;
+        direct = e && cn && (!images[i].grid_index || gi);
+        dev[i].edgels = e;
+        dev[i].count = static_cast<int*>(cn);
+        dev[i].grid_index = static_cast<int*>(gi);
+    }
     for (int i = 0; i < n; ++i) {
         dev[i].pixels = c->hb_in + in_off[i];
-        dev[i].edgels = c->hb_out + out_off[i];
-        dev[i].count = c->hb_cnt + i;
-        dev[i].grid_index = images[i].grid_index ? c->hb_idx + idx_off[i] : nullptr;
+        if (!direct) {
+            dev[i].edgels = c->hb_out + out_off[i];
+            dev[i].count = c->hb_cnt + i;
+            dev[i].grid_index = images[i].grid_index ? c->hb_idx + idx_off[i] : nullptr;
+        }
     }
     for (int i = 0; i < n; ++i) {
         st = check_image(dev[i]);
         if (st != TOED_OK) return fail(st);
     }
-    // groups of consecutive images with similar pixel counts
-    {
+    // With per-image ready flags (written by the copy stream after each
+    // image) one persistent launch takes the whole batch and starts on each
+    // image as soon as it has landed; otherwise groups of consecutive images
+    // with similar pixel counts are detected one after another.
+    auto wv = write_value_fn();
+    const bool concurrent = wv != nullptr;
+    unsigned epoch = 0;
+    if (concurrent) {
+        if (c->hb_ready_cap < n) {
+            // fresh flags start at zero before any kernel or copy of this call can see them
+            if ((st = grow(&c->hb_ready, &c->hb_ready_cap, (long long)n, stream)) != TOED_OK) return fail(st);
+            TOED_HB(cudaMemset(c->hb_ready, 0, sizeof(unsigned) * (size_t)c->hb_ready_cap));
+            c->hb_epoch = 0;
+        }
+        epoch = ++c->hb_epoch;
+        if (epoch == 0) {  // wrapped: clear and restart
+            TOED_HB(cudaMemset(c->hb_ready, 0, sizeof(unsigned) * (size_t)c->hb_ready_cap));
+            epoch = c->hb_epoch = 1;
+        }
+        chunks = 1;
+        first[0] = 0;
+        first[1] = n;
+    }
+    if (!concurrent) {
         long long acc = 0;
         int k = 0;
         first[0] = 0;
@@ -651,13 +725,19 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
             TOED_HB(cudaMemcpy2DAsync(const_cast<void*>(dev[i].pixels), (size_t)dev[i].pitch * esz, h.pixels,
                                       (size_t)h.pitch * esz, (size_t)h.width * esz, (size_t)h.height,
                                       cudaMemcpyHostToDevice, c->s_in));
+            if (concurrent &&
+                wv(c->s_in, (CUdeviceptr)(c->hb_ready + i), epoch, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS) {
+                g_last_cuda_error = "cuStreamWriteValue32 failed";
+                return fail(TOED_ERR_CUDA);
+            }
         }
         TOED_HB(cudaEventRecord(ev_in[k], c->s_in));
     }
     // 2. detection of each group once its images are in
     for (int k = 0; k < chunks; ++k) {
-        TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
-        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream);
+        if (!concurrent) TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
+        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream, nullptr,
+                        concurrent ? c->hb_ready + first[k] : nullptr, epoch);
         if (st != TOED_OK) return fail(st);
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n + k, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
         TOED_HB(cudaEventRecord(ev_det[k], stream));
@@ -665,7 +745,13 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     // 3. per group: counts (and the group's device flags) to the host, then
     // the lists, while later groups are still being copied in or detected
     int flags = 0;
-    for (int k = 0; k < chunks; ++k) {
+    if (direct) {
+        TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + n, c->hb_cnt + n, sizeof(int) * chunks, cudaMemcpyDeviceToHost,
+                                stream));
+        TOED_HB(cudaStreamSynchronize(stream));
+        for (int k = 0; k < chunks; ++k) flags |= c->hb_cnt_host[n + k];
+    }
+    for (int k = 0; k < chunks && !direct; ++k) {
         TOED_HB(cudaStreamWaitEvent(c->s_out, ev_det[k], 0));
         const int i0 = first[k], nk = first[k + 1] - first[k];
         TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + i0, c->hb_cnt + i0, sizeof(int) * nk, cudaMemcpyDeviceToHost,
@@ -747,6 +833,8 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
         return TOED_ERR_INVALID_ARG;
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
+    if (prm->interp_n < 0 || prm->interp_n > 4) return TOED_ERR_INVALID_ARG;
+    const int sc = 1 << prm->interp_n;  // work grid (h-1) sc + 1 by (w-1) sc + 1
     const int r = (int)std::ceil((double)prm->sigma * 4.0);  // build_gaussian_kernels radius
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
     for (int i = 0; i < n; ++i) {
@@ -754,7 +842,8 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
         if (!m.E || !m.edgels || !m.count || m.height < 2 || m.width < 2 || m.pitch < m.width || m.capacity < 0)
             return TOED_ERR_INVALID_ARG;
         if (m.dtype != TOED_F32 && m.dtype != TOED_F64) return TOED_ERR_UNSUPPORTED;
-        if ((long long)m.height * m.width >= (1LL << 31)) return TOED_ERR_UNSUPPORTED;
+        if ((long long)((m.height - 1) * (long long)sc + 1) * ((m.width - 1) * (long long)sc + 1) >= (1LL << 31))
+            return TOED_ERR_UNSUPPORTED;
         if ((reinterpret_cast<uintptr_t>(m.edgels) & 15u) != 0) return TOED_ERR_INVALID_ARG;
     }
     int prev = 0;
@@ -766,15 +855,17 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
         for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax) {
             const int cn = std::min(kBatchMax, n - i0);
             const toed_edgemap* mp = maps + i0;
-            long long px = 0, stag = 0, segs = 0, segtiles = 0;
+            long long px = 0, stag = 0, segs = 0, segtiles = 0, work = 0;
             for (int i = 0; i < cn; ++i) {
-                const long long hw = (long long)mp[i].height * mp[i].width;
+                const long long wh = (long long)(mp[i].height - 1) * sc + 1, ww = (long long)(mp[i].width - 1) * sc + 1;
+                const long long hw = wh * ww;  // work-grid pixels
                 px += hw;
                 // every NMS edgel is staged before isolated ones are removed:
                 // at most one per pixel, in practice far fewer than half
                 stag += std::max<long long>(mp[i].capacity, hw / 2 + 1024);
-                const long long nseg = (long long)mp[i].height * ((mp[i].width + 31) / 32);
+                const long long nseg = wh * ((ww + 31) / 32);
                 segtiles += (nseg + kSegTile - 1) / kSegTile;
+                if (sc > 1) work += hw * (mp[i].theta ? 2 : 1);
             }
             segs = segtiles * kSegTile;
             if ((st = ensure_scratch(c, stag, segs, segtiles, cn, stream)) != TOED_OK) break;
@@ -783,6 +874,7 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
             if ((st = grow(&c->win, &c->px_cap3, px, stream)) != TOED_OK) break;
             if ((st = grow(&c->img_count, &c->img_count_cap, (long long)cn, stream)) != TOED_OK) break;
             if ((st = grow(&c->keep, &c->keep_cap, c->staging_cap, stream)) != TOED_OK) break;
+            if (work > 0 && (st = grow(&c->sp_work, &c->sp_work_cap, work, stream)) != TOED_OK) break;
             SubScratch s;
             s.sc.words = c->words;
             s.sc.staging = c->staging;
@@ -796,6 +888,7 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
             s.win = c->win;
             s.img_count = c->img_count;
             s.keep = c->keep;
+            s.work = c->sp_work;
             cudaError_t e = subpix_launch(mp, cn, prm, r, s, stream);
             if (e != cudaSuccess) {
                 g_last_cuda_error = std::string("subpix_launch: ") + cudaGetErrorString(e);

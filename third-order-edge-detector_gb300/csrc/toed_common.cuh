@@ -78,6 +78,8 @@ struct BatchParams {
     int out_f64;
     int radius;
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
+    const unsigned* ready;  // optional per image: == ready_epoch once its copy to the device landed
+    unsigned ready_epoch;
     Scratch sc;
     DetImage img[kBatchMax];
 };

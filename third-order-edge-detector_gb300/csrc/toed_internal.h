@@ -38,6 +38,7 @@ struct SubScratch {
     int* win;             // per pixel (dense maps)
     int* img_count;       // per map
     unsigned char* keep;  // per staged edgel
+    double* work;         // interp_n > 0: resized maps (and orientations), per work pixel
 };
 
 // Enqueue the TO-correction kernels for up to kBatchMax maps (toed_subpix.cu).

@@ -1,7 +1,10 @@
 // toed_subpix.cu -- subpixel third-order correction of dense edge maps on
 // GB300: the reference's SubpixelTOCorrectionCPU<T>::estimate_orientation()
-// + run() (subpix_TO_correction/subpix_to_correction.cpp:307-736, interp_n=0)
-// as five short kernels over a batch of maps:
+// + run() (subpix_TO_correction/subpix_to_correction.cpp:307-736) as five
+// short kernels over a batch of maps.  At interp_n > 0 the maps are first
+// bilinearly resized onto the 2^n work grid (tc_resize, :69-90) and the
+// kernels below run on that grid; positions come out in original pixels.
+//
 //
 //   tc_orient_nms   one CTA per 32x32 tile: triangle smoothing (r = 4,
 //                   symmetric padding), gradient2 with one-sided borders and
@@ -38,13 +41,15 @@ constexpr int kT = 32;   // tile side (pixels)
 constexpr int kTriR = 4; // triangle filter radius (:316)
 
 struct SubMap {
-    const void* E;
+    const void* E;       // the map the kernels read: the caller's, or its work-grid resize
     const void* theta;
     long long pitch;
     long long px_base;   // offset of this map in the per-pixel scratch planes
     void* TO_E;
     void* TO_O;
-    int h, w, dtype;
+    int h, w, dtype;     // work grid (the original grid at interp_n = 0)
+    int oh, ow;          // original grid (dense TO maps)
+    int scale, margin;   // 2^interp_n; NMS margin 3 * 2^interp_n (:628-630)
     int ntx, nty;
     int tile_base;       // first spatial tile of this map
     long long seg_base;  // first (row, tile column) segment, kSegTile aligned
@@ -191,7 +196,7 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
     }
     __syncthreads();
 
-    // NMS along dir on E (:424-514), margin 3: i, j in [4, dim - 5)
+    // NMS along dir on E (:424-514), margin mg: i, j in [mg + 1, dim - mg - 2)
     unsigned bal[4];
     double rx[4], ry[4], rm[4];
 #pragma unroll
@@ -200,7 +205,7 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
         const int i = i0 + a, j = j0 + b;
         bool acc = false;
         rx[u] = ry[u] = rm[u] = 0.0;
-        if (i >= 4 && i < h - 5 && j >= 4 && j < w - 5) {
+        if (i >= M.margin + 1 && i < h - M.margin - 2 && j >= M.margin + 1 && j < w - M.margin - 2) {
             const float f = sE[a + HE][b + HE];
             const float2 g = sDir[a][b];
             if (f > p.thresh && !(fabsf(g.x) < 1e-5f && fabsf(g.y) < 1e-5f)) {
@@ -487,6 +492,9 @@ __global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubPar
             ori = atan2f((float)Fx, (float)(-Fy));
         }
         rec.z = (double)ori;
+        // coord_scale (:657, :696-697): positions in original pixels
+        rec.x /= (double)M.scale;
+        rec.y /= (double)M.scale;
         p.sc.staging[sidx] = rec;
     }
 }
@@ -508,7 +516,9 @@ __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubPar
     const long long nseg = (long long)M.h * M.ntx;
     const bool all = !(p.nbr > 0.0) || p.img_count[k] < 2;  // :567-568
     const double r2 = p.nbr * p.nbr, inv = 1.0 / p.nbr;
-    const int reach = (int)ceil(p.nbr + 1.5);  // an edgel lies within sqrt(2) of its pixel
+    // an edgel lies within sqrt(2) work pixels of its own; search the id map
+    // (work grid) around it, compare in original pixels as the reference does
+    const int reach = (int)ceil(p.nbr * M.scale + 1.5);
     for (int q = threadIdx.x; q < kSegTile; q += blockDim.x) {
         const long long local = (long long)(t - M.seg_tile_base) * kSegTile + q;
         if (local >= nseg) break;
@@ -522,7 +532,7 @@ __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubPar
             }
             const double4_32a me = p.sc.staging[r];
             const long long cx = (long long)floor(me.x * inv), cy = (long long)floor(me.y * inv);
-            const int pi = (int)floor(me.y), pj = (int)floor(me.x);
+            const int pi = (int)floor(me.y * M.scale), pj = (int)floor(me.x * M.scale);
             bool found = false;
             for (int ii = max(0, pi - reach); ii <= min(M.h - 1, pi + reach) && !found; ++ii) {
                 for (int jj = max(0, pj - reach); jj <= min(M.w - 1, pj + reach); ++jj) {
@@ -610,9 +620,9 @@ __global__ void __launch_bounds__(kSegTile) tc_dense(const __grid_constant__ Sub
         if (r >= p.sc.staging_cap) break;
         const double4_32a rec = p.sc.staging[r];
         int X = (int)round(rec.x), Y = (int)round(rec.y);
-        X = max(0, min(X, M.w - 1));
-        Y = max(0, min(Y, M.h - 1));
-        const long long o = (long long)Y * M.w + X;
+        X = max(0, min(X, M.ow - 1));
+        Y = max(0, min(Y, M.oh - 1));
+        const long long o = (long long)Y * M.ow + X;  // original grid (also indexes the winner map)
         const int li = (int)(dest + e);
         if (PASS == 0) {
             atomicMax(&p.win[M.px_base + o], li);
@@ -626,6 +636,26 @@ __global__ void __launch_bounds__(kSegTile) tc_dense(const __grid_constant__ Sub
             }
         }
     }
+}
+
+// bilinear_resize (:69-90) of one map onto the work grid, in FP64.
+__global__ void __launch_bounds__(256) tc_resize(const void* __restrict__ src, int dtype, long long pitch, int sh,
+                                                 int sw, double* __restrict__ dst, int dh, int dw)
+{
+    const int j = blockIdx.x * blockDim.x + threadIdx.x, i = blockIdx.y;
+    if (j >= dw || i >= dh) return;
+    auto at = [&](int y, int x) -> double {
+        const long long o = (long long)y * pitch + x;
+        return dtype == TOED_F64 ? __ldg((const double*)src + o) : (double)__ldg((const float*)src + o);
+    };
+    const double y = (dh == 1) ? 0.0 : (double)i * (sh - 1) / (double)(dh - 1);
+    const int y0 = (int)floor(y), y1 = min(y0 + 1, sh - 1);
+    const double fy = y - y0;
+    const double x = (dw == 1) ? 0.0 : (double)j * (sw - 1) / (double)(dw - 1);
+    const int x0 = (int)floor(x), x1 = min(x0 + 1, sw - 1);
+    const double fx = x - x0;
+    const double v00 = at(y0, x0), v01 = at(y0, x1), v10 = at(y1, x0), v11 = at(y1, x1);
+    dst[(long long)i * dw + j] = (1 - fy) * ((1 - fx) * v00 + fx * v01) + fy * ((1 - fx) * v10 + fx * v11);
 }
 
 template <int R>
@@ -663,29 +693,54 @@ cudaError_t subpix_launch(const toed_edgemap* maps, int n, const toed_subpix_par
     p->hyb = prm->precision != TOED_FP32;
     p->out_f64 = prm->out_dtype == TOED_F64;
     p->n_maps = n;
-    long long px = 0, segtiles = 0;
+    const int sc = 1 << prm->interp_n;
+    long long px = 0, segtiles = 0, work = 0;
     int tiles = 0;
+    cudaError_t e = cudaSuccess;
     for (int i = 0; i < n; ++i) {
         const toed_edgemap& m = maps[i];
         SubMap& d = p->m[i];
-        d.E = m.E;
-        d.theta = m.theta;
-        d.pitch = m.pitch;
+        d.oh = m.height;
+        d.ow = m.width;
+        d.scale = sc;
+        d.margin = 3 * sc;
+        d.h = (m.height - 1) * sc + 1;
+        d.w = (m.width - 1) * sc + 1;
+        if (sc == 1) {
+            d.E = m.E;
+            d.theta = m.theta;
+            d.pitch = m.pitch;
+            d.dtype = m.dtype;
+        } else {  // set_edgemap / set_orientation (:224-244): resize onto the work grid
+            const long long hw = (long long)d.h * d.w;
+            double* wE = s.work + work;
+            work += hw;
+            const dim3 g((d.w + 255) / 256, d.h);
+            tc_resize<<<g, 256, 0, stream>>>(m.E, m.dtype, m.pitch, m.height, m.width, wE, d.h, d.w);
+            d.E = wE;
+            d.theta = nullptr;
+            if (m.theta) {
+                double* wT = s.work + work;
+                work += hw;
+                tc_resize<<<g, 256, 0, stream>>>(m.theta, m.dtype, m.pitch, m.height, m.width, wT, d.h, d.w);
+                d.theta = wT;
+            }
+            d.pitch = d.w;
+            d.dtype = TOED_F64;
+            if (e == cudaSuccess) e = cudaGetLastError();
+        }
         d.px_base = px;
         d.TO_E = m.TO_E;
         d.TO_O = m.TO_O;
-        d.h = m.height;
-        d.w = m.width;
-        d.dtype = m.dtype;
-        d.ntx = (m.width + kT - 1) / kT;
-        d.nty = (m.height + kT - 1) / kT;
+        d.ntx = (d.w + kT - 1) / kT;
+        d.nty = (d.h + kT - 1) / kT;
         d.tile_base = tiles;
         d.seg_tile_base = (int)segtiles;
         d.seg_base = segtiles * kSegTile;
-        const long long nseg = (long long)m.height * d.ntx;
+        const long long nseg = (long long)d.h * d.ntx;
         tiles += d.ntx * d.nty;
         segtiles += (nseg + kSegTile - 1) / kSegTile;
-        px += (long long)m.height * m.width;
+        px += (long long)d.h * d.w;
     }
     p->n_tiles = tiles;
     p->n_seg_tiles = (int)segtiles;
@@ -697,7 +752,7 @@ cudaError_t subpix_launch(const toed_edgemap* maps, int n, const toed_subpix_par
     p->keep = s.keep;
     std::unique_ptr<SubParams> guard(p);
 
-    cudaError_t e = cudaMemsetAsync(s.sc.words, 0, 3 * sizeof(int), stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(s.sc.words, 0, 3 * sizeof(int), stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(s.img_count, 0, sizeof(int) * n, stream);
     void* args[] = {p};
     if (e == cudaSuccess) e = cudaLaunchKernel((const void*)tc_orient_nms, dim3(tiles), dim3(256), args, 0, stream);
@@ -722,11 +777,11 @@ cudaError_t subpix_launch(const toed_edgemap* maps, int n, const toed_subpix_par
         d.count = maps[i].count;
         d.index = nullptr;
         d.seg_base = p->m[i].seg_base;
-        d.nseg = (long long)maps[i].height * p->m[i].ntx;
+        d.nseg = (long long)p->m[i].h * p->m[i].ntx;
         d.tile_base = p->m[i].seg_tile_base;
         d.cap = maps[i].capacity;
-        d.H = maps[i].height;
-        d.W = maps[i].width;
+        d.H = p->m[i].h;
+        d.W = p->m[i].w;
     }
     if (e == cudaSuccess) e = launch_finalize(*b, stream);
     bool dense = false;
