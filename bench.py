@@ -42,7 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SIGMA, THRESH, N_IMAGES, SEED0 = 1.5, 2.0, 64, 3000
-E2E_CHUNKS = 8  # image groups the host-buffer path pipelines over
+E2E_CHUNKS = 4  # image groups the host-buffer path pipelines over
 METRIC = "Mpixel/s (TOED fused forward, uneven batch of 64 float32 images, sigma 1.5)"
 
 

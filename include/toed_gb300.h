@@ -193,7 +193,7 @@ toed_status toed_detect_noalloc(const toed_image* image, const toed_params* para
 /* Detection of images held in host memory -- the reference's flow (copy the
  * image in, detect, copy the edgel list back, gpu_toed.hpp:141-231 and
  * :415-441) for a whole batch, pipelined: the batch is cut into `chunks`
- * groups of consecutive images with similar pixel counts; the copy of group
+ * groups of consecutive images, growing in pixel count; the copy of group
  * k+1 to the device overlaps the detection of group k (streams of the
  * context, ordered by events).  Page-locked output buffers (edgels, count,
  * grid_index) are written by the detection's ordering pass directly through

@@ -302,3 +302,27 @@ def test_host_batch_matches_device_batch(toed, synth, chunks, pin):
         m = min(n, o["capacity"])
         assert t.equal(o["edgels"][:m], r["edgels"][:m].cpu()), k
         assert t.equal(o["index"][:m], r["index"][:m].cpu()), k
+
+
+@pytest.mark.parametrize("pin", [True, False])
+def test_host_batch_flat_images(toed, synth, pin):
+    """Contiguous images whose rows are whole 16-byte multiples are copied
+    with whole-image 1-D copies; the result equals the device-buffer batch
+    bit for bit, on repeated calls."""
+    t = _torch()
+    det = toed.Detector(0)
+    sizes = [(200, 300, np.float32), (128, 256, np.float32), (96, 64, np.uint8), (301, 120, np.float32),
+             (257, 400, np.float32), (64, 48, np.uint8)]
+    host = [t.as_tensor(synth.shapes_image(h, w, seed=1500 + k, dtype=dt).image)
+            for k, (h, w, dt) in enumerate(sizes)]
+    ref = det.detect_batch([im.cuda() for im in host], sigma=1.5)
+    prm = toed.make_params(1.5)
+    hp = [im.pin_memory() for im in host] if pin else host
+    outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True, pin=pin)
+    for _ in range(2):
+        det.detect_host(hp, outs, prm, chunks=2)
+        for k, (r, o) in enumerate(zip(ref, outs)):
+            n = int(o["count"].item())
+            assert n == r["count"], k
+            assert t.equal(o["edgels"][:n], r["edgels"].cpu()), k
+            assert t.equal(o["index"][:n], r["index"].cpu()), k

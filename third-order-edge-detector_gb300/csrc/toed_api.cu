@@ -83,23 +83,6 @@ static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
     return fn;
 }
 
-// cuStreamWriteValue32 through the runtime's driver entry point (null when
-// unavailable): lets the copy stream mark each image as landed.
-static PFN_cuStreamWriteValue32_v11070 write_value_fn()
-{
-    static PFN_cuStreamWriteValue32_v11070 fn = nullptr;
-    static std::once_flag once;
-    std::call_once(once, [] {
-        void* ptr = nullptr;
-        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
-        if (cudaGetDriverEntryPointByVersion("cuStreamWriteValue32", &ptr, 11070, cudaEnableDefault, &q) ==
-                cudaSuccess &&
-            q == cudaDriverEntryPointSuccess)
-            fn = reinterpret_cast<PFN_cuStreamWriteValue32_v11070>(ptr);
-    });
-    return fn;
-}
-
 void encode_rows_map(CUtensorMap* m, DetImage& d, int r)
 {
     d.tma = 0;
@@ -183,9 +166,6 @@ struct toed_ctx {
     int* hb_cnt_host = nullptr;
     long long hb_cnt_host_cap = 0;
     cudaStream_t s_in = nullptr, s_out = nullptr;
-    unsigned* hb_ready = nullptr;  // per image: the copy stream writes the call's epoch after its copy
-    long long hb_ready_cap = 0;
-    unsigned hb_epoch = 0;
     std::mutex mu;
 };
 
@@ -265,7 +245,6 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->hb_out);
     cudaFree(c->hb_idx);
     cudaFree(c->hb_cnt);
-    cudaFree(c->hb_ready);
     if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
     if (c->s_in) cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamDestroy(c->s_out);
@@ -361,8 +340,7 @@ static int plan_strip_rows(const toed_image* images, int n, long long resident)
 }
 
 static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr,
-                                const unsigned* ready = nullptr, unsigned epoch = 0)
+                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr)
 {
     const bool hyb = prm->precision != TOED_FP32;
     DetectEntry ent = detect_entry(r, hyb);
@@ -386,8 +364,6 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->n_img = n;
     p->out_f64 = (prm->out_dtype == TOED_F64) ? 1 : 0;
     p->radius = r;
-    p->ready = ready;
-    p->ready_epoch = epoch;
     long long units = 0, tiles = 0, staging = 0;
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
@@ -464,14 +440,12 @@ static toed_status check_batch(const toed_ctx* c, const toed_image* images, int 
 
 // The batch in chunks of kBatchMax images (caller holds c->mu, device set).
 static toed_status detect_all(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                              cudaStream_t stream, const toed_tuning* force = nullptr,
-                              const unsigned* ready = nullptr, unsigned epoch = 0)
+                              cudaStream_t stream, const toed_tuning* force = nullptr)
 {
     const int r = radius_of(prm);
     toed_status st = TOED_OK;
     for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
-        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force,
-                          ready ? ready + i0 : nullptr, epoch);
+        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force);
     return st;
 }
 
@@ -679,36 +653,18 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         st = check_image(dev[i]);
         if (st != TOED_OK) return fail(st);
     }
-    // With per-image ready flags (written by the copy stream after each
-    // image) one persistent launch takes the whole batch and starts on each
-    // image as soon as it has landed; otherwise groups of consecutive images
-    // with similar pixel counts are detected one after another.
-    auto wv = write_value_fn();
-    const bool concurrent = wv != nullptr;
-    unsigned epoch = 0;
-    if (concurrent) {
-        if (c->hb_ready_cap < n) {
-            // fresh flags start at zero before any kernel or copy of this call can see them
-            if ((st = grow(&c->hb_ready, &c->hb_ready_cap, (long long)n, stream)) != TOED_OK) return fail(st);
-            TOED_HB(cudaMemset(c->hb_ready, 0, sizeof(unsigned) * (size_t)c->hb_ready_cap));
-            c->hb_epoch = 0;
-        }
-        epoch = ++c->hb_epoch;
-        if (epoch == 0) {  // wrapped: clear and restart
-            TOED_HB(cudaMemset(c->hb_ready, 0, sizeof(unsigned) * (size_t)c->hb_ready_cap));
-            epoch = c->hb_epoch = 1;
-        }
-        chunks = 1;
-        first[0] = 0;
-        first[1] = n;
-    }
-    if (!concurrent) {
+    // groups of consecutive images whose pixel counts grow geometrically
+    // (ratio 1.6, about detection time / copy time per pixel): the first
+    // group is small so detection starts early, and each later copy still
+    // finishes before the detection in front of it
+    {
+        const double g = 1.6, gn = std::pow(g, chunks) - 1.0;
         long long acc = 0;
         int k = 0;
         first[0] = 0;
         for (int i = 0; i < n && k + 1 < chunks; ++i) {
             acc += (long long)images[i].height * images[i].width;
-            if (acc * chunks >= total_px * (k + 1) && i + 1 < n) first[++k] = i + 1;
+            if ((double)acc >= (double)total_px * (std::pow(g, k + 1) - 1.0) / gn && i + 1 < n) first[++k] = i + 1;
         }
         chunks = k + 1;
         first[chunks] = n;
@@ -717,27 +673,26 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         TOED_HB(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
         TOED_HB(cudaEventCreateWithFlags(&ev_det[k], cudaEventDisableTiming));
     }
-    // 1. every group's images to the device, in order
+    // 1. every group's images to the device, in order (whole-image 1-D
+    // copies where the rows are contiguous: those run on the copy engines)
     for (int k = 0; k < chunks; ++k) {
         for (int i = first[k]; i < first[k + 1]; ++i) {
             const toed_host_image& h = images[i];
             const int esz = h.dtype == TOED_U8 ? 1 : 4;
-            TOED_HB(cudaMemcpy2DAsync(const_cast<void*>(dev[i].pixels), (size_t)dev[i].pitch * esz, h.pixels,
-                                      (size_t)h.pitch * esz, (size_t)h.width * esz, (size_t)h.height,
-                                      cudaMemcpyHostToDevice, c->s_in));
-            if (concurrent &&
-                wv(c->s_in, (CUdeviceptr)(c->hb_ready + i), epoch, CU_STREAM_WRITE_VALUE_DEFAULT) != CUDA_SUCCESS) {
-                g_last_cuda_error = "cuStreamWriteValue32 failed";
-                return fail(TOED_ERR_CUDA);
-            }
+            if (h.pitch == h.width && dev[i].pitch == h.width)
+                TOED_HB(cudaMemcpyAsync(const_cast<void*>(dev[i].pixels), h.pixels, (size_t)h.width * h.height * esz,
+                                        cudaMemcpyHostToDevice, c->s_in));
+            else
+                TOED_HB(cudaMemcpy2DAsync(const_cast<void*>(dev[i].pixels), (size_t)dev[i].pitch * esz, h.pixels,
+                                          (size_t)h.pitch * esz, (size_t)h.width * esz, (size_t)h.height,
+                                          cudaMemcpyHostToDevice, c->s_in));
         }
         TOED_HB(cudaEventRecord(ev_in[k], c->s_in));
     }
     // 2. detection of each group once its images are in
     for (int k = 0; k < chunks; ++k) {
-        if (!concurrent) TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
-        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream, nullptr,
-                        concurrent ? c->hb_ready + first[k] : nullptr, epoch);
+        TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
+        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream);
         if (st != TOED_OK) return fail(st);
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n + k, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
         TOED_HB(cudaEventRecord(ev_det[k], stream));

@@ -78,11 +78,42 @@ struct BatchParams {
     int out_f64;
     int radius;
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
-    const unsigned* ready;  // optional per image: == ready_epoch once its copy to the device landed
-    unsigned ready_epoch;
     Scratch sc;
     DetImage img[kBatchMax];
 };
+
+// Block-wide exclusive scan of one int per thread (NT threads); leaves the
+// block total in *total.  s_warp: 33 ints of shared memory.
+template <int NT>
+__device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total)
+{
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    int incl = v;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= d) incl += y;
+    }
+    if (lane == 31) s_warp[wid] = incl;
+    __syncthreads();
+    if (wid == 0) {
+        constexpr int NW = NT / 32;
+        int w = (lane < NW) ? s_warp[lane] : 0;
+        int wi = w;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, wi, d);
+            if (lane >= d) wi += y;
+        }
+        if (lane < NW) s_warp[lane] = wi - w;
+        if (lane == NW - 1) s_warp[32] = wi;
+    }
+    __syncthreads();
+    const int r = incl - v + s_warp[wid];
+    *total = s_warp[32];
+    __syncthreads();
+    return r;
+}
 
 // Index of the image whose [base, next base) range holds `u` (bases ascending).
 template <typename GetBase>

@@ -88,25 +88,6 @@ __device__ __forceinline__ float fetch_px(const void* src, long long pitch, int 
     return __ldg((const float*)src + o);
 }
 
-// Bounded wait for an image whose copy to the device runs concurrently with
-// the kernel (the copy stream writes `epoch` after the copy): acquire load at
-// system scope, about 2 s of polling at most.
-__device__ __forceinline__ bool wait_ready(const unsigned* f, unsigned epoch)
-{
-    const long long t0 = clock64();
-    for (int it = 0; it < (1 << 24); ++it) {
-        unsigned v;
-        asm volatile("ld.acquire.sys.global.u32 %0, [%1];" : "=r"(v) : "l"(f) : "memory");
-        if (v == epoch) {
-            asm volatile("fence.proxy.async;" ::: "memory");  // the TMA reads that follow see the copy
-            return true;
-        }
-        if (clock64() - t0 > 4000000000LL) break;
-        __nanosleep(256);
-    }
-    return false;
-}
-
 // ---------------------------------------------------------------------------
 // TMA staging of input rows (cp.async.bulk.tensor + mbarrier)
 // ---------------------------------------------------------------------------
@@ -386,7 +367,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
     int* sRowOff = sMisc + 32;   // [32]
     int* sAccCnt = sMisc + 64;   // [32] accepted edgels per NMS row
     int* sWarp = sMisc + 96;     // [2][16] warp counts of the NMS compaction
-    int* sScal = sMisc + 128;    // [0] unit [1] staging refill [2] list length [3] input wait gave up
+    int* sScal = sMisc + 128;    // [0] unit [1] staging refill [2] list length
     unsigned char* sRaw = smem + C::off_raw;  // TMA destination: one box of input rows
     const uint32_t bar = smem_addr(smem + C::off_mbar);
     uint32_t phase = 0;
@@ -408,22 +389,9 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
 
     for (;;) {
         __syncthreads();
-        if (tid == 0) {
-            const int u0 = atomicAdd(&p.sc.words[0], 1);
-            sScal[0] = u0;
-            sScal[3] = 0;
-            if (p.ready && u0 < p.n_units) {
-                // the unit's image is being copied in while the kernel runs
-                const int k0 = find_image(p.n_img, u0, [&](int i) { return p.img[i].unit_base; });
-                if (!wait_ready(p.ready + k0, p.ready_epoch)) {
-                    atomicOr(&p.sc.words[2], TOED_FLAG_TIMEOUT);
-                    sScal[3] = 1;
-                }
-            }
-        }
+        if (tid == 0) sScal[0] = atomicAdd(&p.sc.words[0], 1);
         __syncthreads();
         const int u = sScal[0];
-        if (sScal[3]) break;  // gave up waiting for the input: flush the ring and leave
         if (u >= p.n_units) break;
         const int k = find_image(p.n_img, u, [&](int i) { return p.img[i].unit_base; });
         const DetImage& im = p.img[k];

@@ -16,37 +16,6 @@
 
 namespace toed {
 
-template <int NT>
-__device__ __forceinline__ int block_excl_scan(int v, int* s_warp, int* total)
-{
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    int incl = v;
-#pragma unroll
-    for (int d = 1; d < 32; d <<= 1) {
-        const int y = __shfl_up_sync(0xffffffffu, incl, d);
-        if (lane >= d) incl += y;
-    }
-    if (lane == 31) s_warp[wid] = incl;
-    __syncthreads();
-    if (wid == 0) {
-        constexpr int NW = NT / 32;
-        int w = (lane < NW) ? s_warp[lane] : 0;
-        int wi = w;
-#pragma unroll
-        for (int d = 1; d < 32; d <<= 1) {
-            const int y = __shfl_up_sync(0xffffffffu, wi, d);
-            if (lane >= d) wi += y;
-        }
-        if (lane < NW) s_warp[lane] = wi - w;
-        if (lane == NW - 1) s_warp[32] = wi;
-    }
-    __syncthreads();
-    const int r = incl - v + s_warp[wid];
-    *total = s_warp[32];
-    __syncthreads();
-    return r;
-}
-
 __global__ void __launch_bounds__(256) fin_tile_sums(const __grid_constant__ BatchParams p)
 {
     __shared__ int s_warp[33];

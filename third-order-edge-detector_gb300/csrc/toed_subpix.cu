@@ -508,34 +508,66 @@ __device__ __forceinline__ int seg_map(const SubParams& p, int t)
     return find_image(p.n_maps, t, [&](int i) { return p.m[i].seg_tile_base; });
 }
 
+// One CTA per tile of kSegTile segments, a thread per staged edgel of the
+// tile (owning segment by binary search over the scanned counts): an edgel
+// survives if another lies within the radius and in its 3x3 cell
+// neighbourhood (:563-621).  Candidates come from the per-pixel id map,
+// searched ring by ring from the edgel's own pixel outwards and stopping at
+// the first hit (the result does not depend on the order).
 __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubParams p)
 {
+    constexpr int PER = kSegTile / 256;
+    __shared__ int s_warp[33];
+    __shared__ int s_dst[kSegTile];  // exclusive prefix of segment counts within the tile
+    __shared__ int s_src[kSegTile];  // staging offset of each segment
     const int t = blockIdx.x;
     const int k = seg_map(p, t);
     const SubMap& M = p.m[k];
     const long long nseg = (long long)M.h * M.ntx;
+    const long long q0 = (long long)(t - M.seg_tile_base) * kSegTile + threadIdx.x * PER;
+    int cnt[PER], sum = 0;
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        const int2 sg = (q0 + u < nseg) ? p.sc.seg[M.seg_base + q0 + u] : make_int2(0, 0);
+        cnt[u] = sg.y;
+        s_src[threadIdx.x * PER + u] = sg.x;
+        sum += sg.y;
+    }
+    int total;
+    int run = block_excl_scan<256>(sum, s_warp, &total);
+#pragma unroll
+    for (int u = 0; u < PER; ++u) {
+        s_dst[threadIdx.x * PER + u] = run;
+        run += cnt[u];
+    }
+    __syncthreads();
     const bool all = !(p.nbr > 0.0) || p.img_count[k] < 2;  // :567-568
     const double r2 = p.nbr * p.nbr, inv = 1.0 / p.nbr;
     // an edgel lies within sqrt(2) work pixels of its own; search the id map
     // (work grid) around it, compare in original pixels as the reference does
     const int reach = (int)ceil(p.nbr * M.scale + 1.5);
-    for (int q = threadIdx.x; q < kSegTile; q += blockDim.x) {
-        const long long local = (long long)(t - M.seg_tile_base) * kSegTile + q;
-        if (local >= nseg) break;
-        const int2 sg = p.sc.seg[M.seg_base + local];
-        for (int e = 0; e < sg.y; ++e) {
-            const long long r = (long long)sg.x + e;
-            if (r >= p.sc.staging_cap) break;
-            if (all) {
-                p.keep[r] = 1;
-                continue;
-            }
-            const double4_32a me = p.sc.staging[r];
-            const long long cx = (long long)floor(me.x * inv), cy = (long long)floor(me.y * inv);
-            const int pi = (int)floor(me.y * M.scale), pj = (int)floor(me.x * M.scale);
-            bool found = false;
-            for (int ii = max(0, pi - reach); ii <= min(M.h - 1, pi + reach) && !found; ++ii) {
-                for (int jj = max(0, pj - reach); jj <= min(M.w - 1, pj + reach); ++jj) {
+    for (int e = threadIdx.x; e < total; e += blockDim.x) {
+        int lo = 0, hi = kSegTile - 1;  // last segment with s_dst <= e
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (s_dst[mid] <= e) lo = mid; else hi = mid - 1;
+        }
+        const long long r = (long long)s_src[lo] + (e - s_dst[lo]);
+        if (r >= p.sc.staging_cap) continue;
+        if (all) {
+            p.keep[r] = 1;
+            continue;
+        }
+        const double4_32a me = p.sc.staging[r];
+        const long long cx = (long long)floor(me.x * inv), cy = (long long)floor(me.y * inv);
+        const int pi = (int)floor(me.y * M.scale), pj = (int)floor(me.x * M.scale);
+        bool found = false;
+        for (int d = 0; d <= reach && !found; ++d) {
+            for (int ii = pi - d; ii <= pi + d && !found; ++ii) {
+                if (ii < 0 || ii >= M.h) continue;
+                const int step = (ii == pi - d || ii == pi + d) ? 1 : 2 * d;  // ring: full edge rows, end columns
+                for (int jj = pj - d; jj <= pj + d; jj += step) {
+                    if (jj < 0 || jj >= M.w) continue;
                     const int o = p.eid[M.px_base + (long long)ii * M.w + jj];
                     if (o < 0 || o == r) continue;
                     const double4_32a ot = p.sc.staging[o];
@@ -548,8 +580,8 @@ __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubPar
                     }
                 }
             }
-            p.keep[r] = found ? 1 : 0;
         }
+        p.keep[r] = found ? 1 : 0;
     }
 }
 
