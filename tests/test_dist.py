@@ -48,3 +48,17 @@ def test_two_ranks_gloo():
     res = sorted(q.get(timeout=10) for _ in range(2))
     assert [m for _, m, _ in res] == [20.0, 20.0]
     assert res[0][2] != res[1][2]
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """bench.py --impl reference prints one JSON line with the contract's keys
+    (a short CPU budget here)."""
+    import json
+    import types
+    import bench
+    monkeypatch.setattr(bench, "REF_SECONDS", 2.0)
+    bench.run_reference(types.SimpleNamespace(steps=1, warmup=1), 1, 0)
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "Mpixel/s"
+    assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
