@@ -234,11 +234,14 @@ toed_status toed_write_edgels_txt(const char* path, const void* edgels, int dtyp
  * height 14, 30, 62, 126, 254, 510 or 1022 rows, input rows staged by TMA or
  * by plain loads -- on the caller's batch with CUDA events, `reps` timed runs
  * after one untimed run each, keeps the fastest in the context for this
- * radius and precision (later toed_detect_batch calls use it) and returns it.
+ * radius, precision and launch size class -- floor(log2(pixels)) of each
+ * launch of the batch (64 images at most per launch) -- and returns it; later
+ * launches of the same class use it, launches of other classes keep the
+ * built-in heuristic.
  * It is synchronous, runs the detection 14 * (reps + 1) times (the outputs hold
  * the last run; every candidate gives the same result bit for bit) and is
- * refused under stream capture.  toed_set_tuning installs a shape (NULL
- * restores the built-in heuristic). */
+ * refused under stream capture.  toed_set_tuning installs a shape for every
+ * size class (NULL restores the built-in heuristic). */
 typedef struct toed_tuning {
     int strip_rows;  /* 16k - 2 for k in 1, 2, 4, ..., 64 */
     int staging;     /* 1: TMA (when the image allows it), 0: plain loads */

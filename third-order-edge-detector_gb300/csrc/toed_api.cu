@@ -149,8 +149,9 @@ struct toed_ctx {
     double* sp_work = nullptr;  // TO correction at interp_n > 0: maps resized onto the work grid
     long long sp_work_cap = 0;
     int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
-    // launch shape chosen by toed_autotune per (radius, precision); strip_rows 0 = heuristic
-    toed_tuning tune[TOED_MAX_RADIUS + 1][2] = {};
+    // launch shape chosen by toed_autotune per (radius, precision, size class of
+    // the launch: floor(log2(pixels))); strip_rows 0 = heuristic
+    toed_tuning tune[TOED_MAX_RADIUS + 1][2][kSizeClasses] = {};
     bool profiling = false;
     std::vector<std::pair<cudaEvent_t, cudaEvent_t>> prof;
     // toed_detect_host_batch: device staging of images / lists / counts, a
@@ -324,6 +325,18 @@ static int radius_of(const toed_params* p)
     return (int)std::ceil(4.0 * (double)p->sigma);
 }
 
+// Size class of one launch: floor(log2(pixels)).  A launch shape that wins
+// on a 64-image batch is a poor one for a single small image, so tuned shapes
+// are kept per class.
+static int size_class(const toed_image* images, int n)
+{
+    long long px = 1;
+    for (int i = 0; i < n; ++i) px += (long long)images[i].width * images[i].height;
+    int k = 0;
+    while (k + 1 < kSizeClasses && (px >> (k + 1)) > 0) ++k;
+    return k;
+}
+
 // Strip height: the tallest multiple of the step (minus the 2-row ring) that
 // still gives every resident CTA several units to balance the queue.
 static int plan_strip_rows(const toed_image* images, int n, long long resident)
@@ -358,7 +371,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     make_taps((double)prm->sigma, r, &p->taps);
     p->thr = prm->threshold;
     p->border = prm->border;
-    const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0];
+    const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0][size_class(images, n)];
     const toed_tuning* use = force ? force : (tuned.strip_rows > 0 ? &tuned : nullptr);
     p->S = use ? use->strip_rows : plan_strip_rows(images, n, resident);
     p->n_img = n;
@@ -515,7 +528,9 @@ extern "C" toed_status toed_autotune(toed_ctx* c, const toed_image* images, int 
                 cand.ms = ms / (float)reps;
                 if (st == TOED_OK && (win.ms < 0.f || cand.ms < win.ms)) win = cand;
             }
-        if (st == TOED_OK) c->tune[r][hyb] = win;
+        if (st == TOED_OK)
+            for (int i0 = 0; i0 < n; i0 += kBatchMax)
+                c->tune[r][hyb][size_class(images + i0, std::min(kBatchMax, n - i0))] = win;
     }
     if (e0) cudaEventDestroy(e0);
     if (e1) cudaEventDestroy(e1);
@@ -537,7 +552,7 @@ extern "C" toed_status toed_set_tuning(toed_ctx* c, const toed_params* prm, cons
         v = *t;
     }
     std::lock_guard<std::mutex> lk(c->mu);
-    c->tune[r][prm->precision != TOED_FP32 ? 1 : 0] = v;
+    for (int k = 0; k < kSizeClasses; ++k) c->tune[r][prm->precision != TOED_FP32 ? 1 : 0][k] = v;
     return TOED_OK;
 }
 

@@ -19,6 +19,7 @@ namespace toed {
 
 constexpr int kMaxTaps = 2 * TOED_MAX_RADIUS + 3;  // taps of the widest (shifted/full) filter
 constexpr int kBatchMax = 64;                      // images per launch (larger batches are chunked)
+constexpr int kSizeClasses = 48;                   // launch size classes floor(log2(pixels)) of tuned shapes
 constexpr int kThreads = 256;                      // threads per detection CTA
 constexpr int kExt = 32;                           // strip width incl. a 1-pixel ring each side
 constexpr int kInner = kExt - 2;                   // 30 output columns per strip

@@ -162,35 +162,44 @@ __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int p0, 
         float o_[2][12];
 #pragma unroll
         for (int o = 0; o < 2; ++o) {
-            // The taps are exactly symmetric (G, Gxx) or antisymmetric (Gx,
-            // Gxxx) about 0, and about -1/2 for the shifted set, so each
-            // mirrored pair of inputs is summed / differenced once and shared
-            // by the even / odd filters.
+            // The odd filters (Gx, Gxxx) are exactly antisymmetric about 0 (about
+            // -1/2 for the shifted set): each mirrored pair of inputs is
+            // differenced once -- fewer operations and a smaller rounding
+            // error, since neighbouring inputs nearly cancel.  The even filters
+            // (G, Gxx) are summed tap by tap: folding them would round the sum
+            // of two full-scale inputs and double the error of Gxx.
             const int c = o + R + 1;  // centre: out(x) = sum_q in(x-q) X(q), in(x-q) = v[c-q]
-            float tG = v[c] * tp.v[0][R + 1], tGxx = v[c] * tp.v[2][R + 1], tGx = 0.f, tGxxx = 0.f;
+            float tG = 0.f, tGxx = 0.f, tGx = 0.f, tGxxx = 0.f;
+#pragma unroll
+            for (int q = -R; q <= R; ++q) {
+                tG = fmaf(v[c - q], tp.v[0][q + R + 1], tG);
+                tGxx = fmaf(v[c - q], tp.v[2][q + R + 1], tGxx);
+            }
 #pragma unroll
             for (int q = 1; q <= R; ++q) {
-                const float sm = v[c - q] + v[c + q], df = v[c - q] - v[c + q];
-                tG = fmaf(sm, tp.v[0][q + R + 1], tG);
-                tGxx = fmaf(sm, tp.v[2][q + R + 1], tGxx);
+                const float df = v[c - q] - v[c + q];
                 tGx = fmaf(df, tp.v[1][q + R + 1], tGx);
                 tGxxx = fmaf(df, tp.v[3][q + R + 1], tGxxx);
             }
-            // full 2r+3-tap responses add the pair q = +-(r+1)
-            const float smo = v[c - R - 1] + v[c + R + 1], dfo = v[c - R - 1] - v[c + R + 1];
-            const float fG = fmaf(smo, tp.v[0][2 * R + 2], tG);
+            // full 2r+3-tap responses add the taps q = +-(r+1)
+            const float fG = fmaf(v[c + R + 1], tp.v[0][0], fmaf(v[c - R - 1], tp.v[0][2 * R + 2], tG));
+            const float fGxx = fmaf(v[c + R + 1], tp.v[2][0], fmaf(v[c - R - 1], tp.v[2][2 * R + 2], tGxx));
+            const float dfo = v[c - R - 1] - v[c + R + 1];
             const float fGx = fmaf(dfo, tp.v[1][2 * R + 2], tGx);
-            const float fGxx = fmaf(smo, tp.v[2][2 * R + 2], tGxx);
             const float fGxxx = fmaf(dfo, tp.v[3][2 * R + 2], tGxxx);
-            // shifted taps X(q + 1/2): pairs (q, -1-q) for q = 0..r, then q = r+1 alone
+            // shifted taps X(q + 1/2), q = -(r+1)..r+1: even filters tap by tap,
+            // odd ones over the pairs (q, -1-q) for q = 0..r plus q = r+1 alone
+            float sG = 0.f, sGxx = 0.f;
+#pragma unroll
+            for (int q = -(R + 1); q <= R + 1; ++q) {
+                sG = fmaf(v[c - q], tp.v[4][q + R + 1], sG);
+                sGxx = fmaf(v[c - q], tp.v[6][q + R + 1], sGxx);
+            }
             const float vl = v[c - R - 1];
-            float sG = vl * tp.v[4][2 * R + 2], sGx = vl * tp.v[5][2 * R + 2];
-            float sGxx = vl * tp.v[6][2 * R + 2], sGxxx = vl * tp.v[7][2 * R + 2];
+            float sGx = vl * tp.v[5][2 * R + 2], sGxxx = vl * tp.v[7][2 * R + 2];
 #pragma unroll
             for (int q = 0; q <= R; ++q) {
-                const float sm = v[c - q] + v[c + 1 + q], df = v[c - q] - v[c + 1 + q];
-                sG = fmaf(sm, tp.v[4][q + R + 1], sG);
-                sGxx = fmaf(sm, tp.v[6][q + R + 1], sGxx);
+                const float df = v[c - q] - v[c + 1 + q];
                 sGx = fmaf(df, tp.v[5][q + R + 1], sGx);
                 sGxxx = fmaf(df, tp.v[7][q + R + 1], sGxxx);
             }
