@@ -291,6 +291,12 @@ def side_measurements(toed, det, images, side, stream):
     dms = _time_ms(dense_form, 2, stream)
     out["dense_two_kernel_form_mpx_s"] = round(npx / (dms * 1e-3) / 1e6, 1)
     del planes
+    # -- the MATLAB quick-and-dirty orientation mode on the same batch ------
+    pq = toed.make_params(SIGMA, 0, THRESH, orientation=toed.TOED_ORI_QAD)
+    qms = _time_ms(lambda: det.detect_into(d_imgs, outs, pq, stream), 3, stream)
+    gms = _time_ms(lambda: det.detect_into(d_imgs, outs, prm, stream), 3, stream)
+    out["qad_orientation_batch"] = {"ms": round(qms, 3), "grid_mode_ms": round(gms, 3),
+                                    "mpx_s": round(npx / (qms * 1e-3) / 1e6, 1)}
     # -- config 4: forward vs forward + backward (16 x 512^2, sigma learnable)
     c4 = [torch.as_tensor(im).to(dev) for im in side["c4"]]
     o4 = det.alloc_outputs([im.shape for im in c4], None)
@@ -331,6 +337,17 @@ def side_measurements(toed, det, images, side, stream):
                              "pos_err_max_px": float(f"{pe.max():.3g}"), "pos_err_p99_px": float(f"{np.quantile(pe, .99):.3g}"),
                              "ori_err_max_rad": float(f"{np.nanmax(oe):.3g}"),
                              "ori_err_p99_rad": float(f"{np.nanquantile(oe, .99):.3g}")}
+            if name == "c2_1080":
+                # the quick-and-dirty orientation mode against its own FP64 oracle
+                refq = oracle.detect(im.astype(np.float64), sg, nthreads=os.cpu_count(), orientation="qad")
+                r = det.detect(torch.as_tensor(im).to(dev), sigma=sg, out_dtype=toed.TOED_F64,
+                               orientation=toed.TOED_ORI_QAD)
+                gi = r["index"].cpu().numpy().astype(np.int64)
+                common, ia, ib = np.intersect1d(refq["index"], gi, return_indices=True)
+                oe = np.abs(np.angle(np.exp(1j * (refq["edges"][ia, 2] - r["edgels"].cpu().numpy()[ib, 2]))))
+                row["qad_orientation"] = {"agreement": round(len(common) / max(len(gi), len(refq["index"])), 6),
+                                          "ori_err_max_rad": float(f"{np.nanmax(oe):.3g}"),
+                                          "ori_err_p99_rad": float(f"{np.nanquantile(oe, .99):.3g}")}
             row["n_ref"] = int(len(ref["index"]))
             prec[f"{name[3:]}_sigma{sg:g}"] = row
     out["precision_vs_fp64_oracle"] = prec

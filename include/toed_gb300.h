@@ -63,6 +63,14 @@ typedef enum toed_precision {
     TOED_FP32 = 1    /* everything FP32 (precision-study mode) */
 } toed_precision;
 
+/* Where the emitted third-order orientation is evaluated. */
+typedef enum toed_orientation {
+    TOED_ORI_GRID = 0, /* at the edgel's 2x-grid point (the C++ detector, cpu_toed.cpp:227-232) */
+    TOED_ORI_QAD = 1   /* MATLAB "quick and dirty" mode (third_order_edge_detector.m:91-141): the nine
+                          derivatives cubic-interpolated (interp2 'cubic', Keys a = -1/2) at the
+                          subpixel point; positions and strengths unchanged */
+} toed_orientation;
+
 /* Device flags (toed_device_flags) */
 #define TOED_FLAG_OVER_CAPACITY 0x1 /* some image found more edgels than its capacity */
 #define TOED_FLAG_STAGING_FULL 0x2  /* the context staging buffer overflowed */
@@ -90,6 +98,7 @@ typedef struct toed_params {
     int border;        /* NMS skips a border of this many 2x-grid points; reference 10 (cpu_toed.cpp:400) */
     int out_dtype;     /* TOED_F32 (16-byte edgels) or TOED_F64 (32-byte edgels) */
     int precision;     /* toed_precision */
+    int orientation;   /* toed_orientation (TOED_ORI_GRID: the reference C++ detector) */
 } toed_params;
 
 /* Fill `p` with the reference's configuration for a given sigma. */
@@ -134,6 +143,7 @@ typedef struct toed_grad_image {
     float* grad_pixels;       /* height x width float32 (device, row pitch = width): overwritten */
 } toed_grad_image;
 
+/* params->orientation must be TOED_ORI_GRID (TOED_ERR_UNSUPPORTED otherwise). */
 toed_status toed_backward_batch(toed_ctx* ctx, const toed_grad_image* items, int n_images,
                                 const toed_params* params, double* grad_sigma, cudaStream_t stream);
 

@@ -57,6 +57,10 @@ def lib():
             _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, ctypes.c_double,
             ctypes.c_int, _dp, ctypes.c_long, _dp, _dp, _i64p]
         L.toed_oracle_detect.restype = ctypes.c_long
+        L.toed_oracle_detect_qad.argtypes = [
+            _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, ctypes.c_double,
+            ctypes.c_int, _dp, ctypes.c_long, _i64p]
+        L.toed_oracle_detect_qad.restype = ctypes.c_long
         L.toed_oracle_planes.argtypes = [
             _dp, ctypes.c_int, ctypes.c_int, ctypes.c_int, _dp, ctypes.c_int, _dp, _dp, _dp, _dp, _dp]
         L.subpix_oracle_run.argtypes = [
@@ -87,9 +91,14 @@ def taps(sigma: float, r: int | None = None) -> np.ndarray:
 
 
 def detect(img, sigma: float = 2.0, r: int | None = None, tap_block=None, threshold: float = 2.0,
-           nthreads: int = 0, planes: bool = False):
+           nthreads: int = 0, planes: bool = False, orientation: str = "grid"):
     """FP64 TOED.  Returns dict(edges=(N,4), index=(N,) 2x-grid linear index
-    [, planes=(4,2H,2W) Ix/Iy/mag/ori, posmaps=(3,2H,2W)])."""
+    [, planes=(4,2H,2W) Ix/Iy/mag/ori, posmaps=(3,2H,2W)]).
+    orientation="qad": the MATLAB quick-and-dirty mode
+    (third_order_edge_detector.m:91-141), derivatives cubic-interpolated at
+    the subpixel point (no plane outputs)."""
+    if orientation not in ("grid", "qad"):
+        raise ValueError(orientation)
     img = np.ascontiguousarray(img, dtype=np.float64)
     H, W = img.shape
     r = default_radius(sigma) if r is None else r
@@ -100,6 +109,12 @@ def detect(img, sigma: float = 2.0, r: int | None = None, tap_block=None, thresh
     cap = 4 * H * W
     edges = np.zeros((cap, 4), np.float64)
     index = np.zeros(cap, np.int64)
+    if orientation == "qad":
+        if planes:
+            raise ValueError("orientation='qad' has no plane outputs")
+        n = lib().toed_oracle_detect_qad(_ptr(img), H, W, float(sigma), int(r), _ptr(tb), float(threshold),
+                                         int(nthreads), _ptr(edges), cap, index.ctypes.data_as(_i64p))
+        return {"edges": edges[:n].copy(), "index": index[:n].copy()}
     pl = np.zeros((4, 2 * H, 2 * W), np.float64) if planes else None
     pm = np.zeros((3, 2 * H, 2 * W), np.float64) if planes else None
     n = lib().toed_oracle_detect(_ptr(img), H, W, float(sigma), int(r), _ptr(tb), float(threshold),

@@ -16,6 +16,9 @@
  *     - NMS + fit       cpu_toed.cpp:379-506
  *     - compaction      cpu_toed.cpp:508-538 (row-major over the 2x grid,
  *                       x_out = (pos_x-1)/2, y_out = (pos_y-1)/2)
+ *     - MATLAB QaD orientation (third_order_edge_detector.m:91-141):
+ *                       toed_oracle_detect_qad, derivatives cubic-interpolated
+ *                       at the subpixel point
  *     Extensions over the reference (which hard-codes sigma = 2 through literal
  *     taps, kernel 17 and threshold 2): any sigma with taps from the
  *     reference's own commented formula, any half-width r, any threshold,
@@ -783,4 +786,53 @@ long subpix_oracle_run(const double *E, int h, int w, double thresh, double sigm
 {
     return subpix_oracle_run_n(E, h, w, 0, thresh, sigma, nbr_radius, theta_in, nthreads, edges, capacity,
                                TO_E, TO_O, nms_out, theta_out, planes10);
+}
+
+
+/* ------------------------------------------------------------------------ */
+/* TOED, MATLAB "quick and dirty" orientation mode                           */
+/* ------------------------------------------------------------------------ */
+/*
+ * third_order_edge_detector.m:91-141 with QaD_flag set: the nine derivatives
+ * are interpolated with MATLAB's interp2 'cubic' (cubic convolution, Keys
+ * a = -1/2, the same kernel the reference restates as cubic_kernel /
+ * interp2_cubic, subpix_to_correction.cpp:57-67, :521-556) at each edgel's
+ * subpixel point, and the orientation is atan2(Fx, -Fy) of the third-order
+ * vector built from them (:127-141) instead of the vector at the grid point
+ * (cpu_toed.cpp:227-232).  Here the derivatives are the C++ detector's own
+ * (the 2x grid of cpu_toed.cpp:204-344, zero padding) and the subpixel
+ * point is its NMS position in 2x-grid units (cpu_toed.cpp:488-489);
+ * positions and strengths are those of the grid mode.  Same arguments as
+ * toed_oracle_detect without the plane outputs; index_out is required.
+ */
+long toed_oracle_detect_qad(const double *img, int H, int W, double sigma, int r,
+                            const double *taps_in, double threshold, int nthreads, double *edges,
+                            long capacity, int64_t *index_out)
+{
+    const int n = 2 * r + 3;
+    double *taps = (double *)malloc(sizeof(double) * 8 * n);
+    if (taps_in)
+        memcpy(taps, taps_in, sizeof(double) * 8 * n);
+    else
+        toed_oracle_taps(sigma, r, taps);
+    const int H2 = 2 * H, W2 = 2 * W;
+    const size_t P2 = (size_t)H2 * W2;
+    double *pm = (double *)malloc(sizeof(double) * 3 * P2);
+    double *d9 = (double *)malloc(sizeof(double) * 9 * P2);
+    const long N = toed_oracle_detect(img, H, W, sigma, r, taps, threshold, nthreads, edges, capacity,
+                                      NULL, pm, index_out);
+    toed_oracle_planes(img, H, W, r, taps, nthreads, NULL, NULL, NULL, NULL, d9);
+    const long m = N < capacity ? N : capacity;
+#pragma omp parallel for schedule(static)
+    for (long e = 0; e < m; e++) {
+        const size_t o = (size_t)index_out[e];
+        const double px = pm[o], py = pm[P2 + o];
+        double d[9];
+        for (int k = 0; k < 9; k++) d[k] = interp2_cubic(d9 + (size_t)k * P2, H2, W2, px, py);
+        to_orientation(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8], &edges[4 * e + 2]);
+    }
+    free(d9);
+    free(pm);
+    free(taps);
+    return N;
 }

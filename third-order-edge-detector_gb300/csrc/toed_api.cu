@@ -181,6 +181,7 @@ void toed_params_default(toed_params* p, float sigma)
     p->border = 10;
     p->out_dtype = TOED_F32;
     p->precision = TOED_HYBRID;
+    p->orientation = TOED_ORI_GRID;
 }
 
 const char* toed_status_string(toed_status s)
@@ -377,6 +378,8 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->n_img = n;
     p->out_f64 = (prm->out_dtype == TOED_F64) ? 1 : 0;
     p->radius = r;
+    p->hyb = hyb ? 1 : 0;
+    p->qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
     long long units = 0, tiles = 0, staging = 0;
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
@@ -442,6 +445,7 @@ static toed_status check_batch(const toed_ctx* c, const toed_image* images, int 
     if (prm->border < 1) return TOED_ERR_INVALID_ARG;
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
+    if (prm->orientation != TOED_ORI_GRID && prm->orientation != TOED_ORI_QAD) return TOED_ERR_INVALID_ARG;
     const int r = radius_of(prm);
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
     for (int i = 0; i < n; ++i) {
@@ -875,6 +879,8 @@ extern "C" toed_status toed_backward_batch(toed_ctx* c, const toed_grad_image* i
 {
     if (!c || !items || n <= 0 || !prm || !grad_sigma) return TOED_ERR_INVALID_ARG;
     if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma)) return TOED_ERR_INVALID_ARG;
+    // the adjoint is that of the grid-point orientation (cpu_toed.cpp:227-232)
+    if (prm->orientation != TOED_ORI_GRID) return TOED_ERR_UNSUPPORTED;
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     const int r = radius_of(prm);
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;

@@ -79,6 +79,8 @@ struct BatchParams {
     int out_f64;
     int radius;
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
+    int hyb;             // 1: FP64 third-order vector and peak fit (TOED_HYBRID)
+    int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
     Scratch sc;
     DetImage img[kBatchMax];
 };

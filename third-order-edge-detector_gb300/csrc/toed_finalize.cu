@@ -120,6 +120,7 @@ cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream)
     if (e != cudaSuccess) return e;
     e = cudaLaunchKernel((const void*)fin_tile_scan, dim3(1), dim3(1024), args, 0, stream);
     if (e != cudaSuccess) return e;
+    if (p.qad) return launch_scatter_qad(p, stream);
     return cudaLaunchKernel((const void*)fin_scatter, dim3(p.n_tiles), dim3(kFinThreads), args, 0, stream);
 }
 

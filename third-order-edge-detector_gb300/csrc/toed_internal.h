@@ -18,6 +18,8 @@ struct DetectEntry {
 DetectEntry detect_entry(int radius, bool hyb);
 
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
+// The ordering pass's last kernel in the TOED_ORI_QAD orientation mode (toed_qad.cu).
+cudaError_t launch_scatter_qad(const BatchParams& p, cudaStream_t stream);
 
 // Fill d.tma / d.tma_align / d.tma_boxw and encode the image's row map for
 // TMA staging (kStepRows-row boxes, zero fill outside the image).  Leaves

@@ -93,6 +93,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
         return TOED_ERR_INVALID_ARG;
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
+    if (prm->orientation != TOED_ORI_GRID && prm->orientation != TOED_ORI_QAD) return TOED_ERR_INVALID_ARG;
     // the fixed scratch bounds the image and the edgel capacity
     if (im->height > kNaMaxDim || im->width > kNaMaxDim || (long long)im->height * im->width > kNaMaxPixels ||
         im->capacity > kNaMaxEdgels)
@@ -120,6 +121,8 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     p.n_img = 1;
     p.out_f64 = prm->out_dtype == TOED_F64;
     p.radius = r;
+    p.hyb = prm->precision != TOED_FP32 ? 1 : 0;
+    p.qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
     p.stage_blk = 1;  // staging sized to the capacity exactly: reserve each step's edgels alone
     // strip height: the tallest of 254 / 126 / 62 / 30 / 14 rows that still
     // gives every resident CTA a few strips
