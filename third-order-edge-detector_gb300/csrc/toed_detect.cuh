@@ -373,10 +373,9 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
     float4* sTab = reinterpret_cast<float4*>(smem + C::off_tab);
     int* sMisc = reinterpret_cast<int*>(smem + C::off_misc);
     float* sRec = reinterpret_cast<float*>(smem + C::off_rec);
-    int* sRowOff = sMisc + 32;   // [32]
     int* sAccCnt = sMisc + 64;   // [32] accepted edgels per NMS row
     int* sWarp = sMisc + 96;     // [2][16] warp counts of the NMS compaction
-    int* sScal = sMisc + 128;    // [0] unit [1] staging refill [2] list length
+    int* sScal = sMisc + 128;    // [0] unit [1] staging refill
     unsigned char* sRaw = smem + C::off_raw;  // TMA destination: one box of input rows
     const uint32_t bar = smem_addr(smem + C::off_mbar);
     uint32_t phase = 0;
@@ -454,16 +453,28 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     const int nrows = min(B, C::HS - ((s == 0) ? ch * B : 0));
                     const int a0 = (s == 0) ? ch * B : rb + 2 * R + 3;  // ring row of box row 0 (before wrapping)
                     if (ok) {
+                        // a warp per staged row, lanes along it
                         if (dtype == TOED_U8) {
-                            for (int i = tid; i < nrows * C::NIN; i += kThreads) {
-                                const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                                sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = (float)sRaw[rr * rawpitch + shift + cc];
+                            for (int rr = wid; rr < nrows; rr += kThreads / 32) {
+                                float* dst = sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN;
+                                const unsigned char* srow = sRaw + rr * rawpitch + shift;
+                                for (int cc = lane; cc < C::NIN; cc += 32) dst[cc] = (float)srow[cc];
+                            }
+                        } else if ((R & 1) == 0) {
+                            // even r: the staged row starts 8-byte aligned (shift = xin mod 4 is even)
+                            const float* rf = reinterpret_cast<const float*>(sRaw);
+                            static_assert(C::NIN % 2 == 0 && C::NIN / 2 <= 32, "one float2 per lane");
+                            for (int rr = wid; rr < nrows; rr += kThreads / 32) {
+                                float2* dst = reinterpret_cast<float2*>(sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN);
+                                const float2* srow = reinterpret_cast<const float2*>(rf + rr * im.tma_boxw + shift);
+                                if (lane < C::NIN / 2) dst[lane] = srow[lane];
                             }
                         } else {
                             const float* rf = reinterpret_cast<const float*>(sRaw);
-                            for (int i = tid; i < nrows * C::NIN; i += kThreads) {
-                                const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                                sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = rf[rr * im.tma_boxw + shift + cc];
+                            for (int rr = wid; rr < nrows; rr += kThreads / 32) {
+                                float* dst = sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN;
+                                const float* srow = rf + rr * im.tma_boxw + shift;
+                                for (int cc = lane; cc < C::NIN; cc += 32) dst[cc] = srow[cc];
                             }
                         }
                     }
@@ -535,9 +546,11 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             __syncthreads();
             // ---- 4a. points above the threshold, listed in row-major order ---
             // NMS rows m = 1..2B; mask (m, parity, half): bit L <-> 2x column
-            // 2 (32 half + L) + parity.  Warp 0 counts and scans the rows
-            // (lane L <-> row L + 1).
-            if (wid == 0) {
+            // 2 (32 half + L) + parity.  Every warp counts and scans the rows
+            // itself (lane L <-> row L + 1): no barrier between the scan and
+            // the list writes.
+            int row_excl, LA;
+            {
                 int cnt = 0;
 #pragma unroll
                 for (int q = 0; q < 2 * kHalves; ++q) cnt += __popc(sMask[(lane + 1) * 2 * kHalves + q]);
@@ -547,14 +560,13 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     const int y = __shfl_up_sync(0xffffffffu, incl, d);
                     if (lane >= d) incl += y;
                 }
-                sRowOff[lane] = incl - cnt;
-                if (lane == 31) sScal[2] = incl;
+                row_excl = incl - cnt;
+                LA = __shfl_sync(0xffffffffu, incl, 31);
             }
-            __syncthreads();
             {
                 const unsigned lt = (1u << lane) - 1u;
                 for (int m = 1 + wid; m <= 2 * B; m += kThreads / 32) {
-                    int pos0 = sRowOff[m - 1];
+                    int pos0 = __shfl_sync(0xffffffffu, row_excl, m - 1);
 #pragma unroll
                     for (int h = 0; h < kHalves; ++h) {
                         const unsigned mk0 = sMask[(m * 2) * kHalves + h], mk1 = sMask[(m * 2 + 1) * kHalves + h];
@@ -572,7 +584,6 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             // place, order kept (their rank never exceeds their list position).
             // One barrier per round: the warp counts alternate between two
             // halves of sWarp.
-            const int LA = sScal[2];
             int nacc = 0;
             for (int r0 = 0, rd = 0; r0 < LA; r0 += kThreads, rd ^= 1) {
                 const int e = r0 + tid;
