@@ -358,13 +358,18 @@ def run_workload(args):
     """One secondary workload alone (for profiling its kernels): 'fwd_bwd' =
     the differentiable batch of 16 float32 512x512 ellipse images, sigma 1.5,
     forward then backward per step; 'subpix' = TO correction of 8 float32
-    2048x2048 ridge maps.  Prints one JSON line of timings."""
-    if args.workload == "fwd_bwd":
-        jobs = [(512, 512, 4000 + k, "f32", True) for k in range(16)]
+    2048x2048 ridge maps; 'qad' = the headline batch detected with the
+    quick-and-dirty orientation mode, then with the grid mode.  Prints one
+    JSON line of timings."""
+    if args.workload == "qad":
+        ims = make_batch(SEED0)
     else:
-        jobs = [(2048, 2048, 5000 + k, "ridge", False) for k in range(8)]
-    with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
-        ims = pool.map(_gen_shapes, jobs)
+        if args.workload == "fwd_bwd":
+            jobs = [(512, 512, 4000 + k, "f32", True) for k in range(16)]
+        else:
+            jobs = [(2048, 2048, 5000 + k, "ridge", False) for k in range(8)]
+        with mp.get_context("spawn").Pool(min(len(jobs), os.cpu_count() or 4)) as pool:
+            ims = pool.map(_gen_shapes, jobs)
     import torch
     toed = _pkg()
     if not os.path.exists(toed.LIB_PATH):
@@ -384,6 +389,14 @@ def run_workload(args):
         line = {"workload": "fwd_bwd 16 x 512^2 float32, sigma 1.5", "fwd_ms": round(fwd, 4),
                 "bwd_ms": round(bwd, 4), "fwd_plus_bwd_over_fwd": round((fwd + bwd) / fwd, 3),
                 "edgels": int(sum(r["count"] for r in res))}
+    elif args.workload == "qad":
+        o = det.alloc_outputs([im.shape for im in x], None)
+        pq = toed.make_params(SIGMA, 0, THRESH, orientation=toed.TOED_ORI_QAD)
+        prm = toed.make_params(SIGMA, 0, THRESH)
+        qms = _time_ms(lambda: det.detect_into(x, o, pq, stream), args.steps, stream)
+        gms = _time_ms(lambda: det.detect_into(x, o, prm, stream), args.steps, stream)
+        line = {"workload": "qad: uneven batch of 64 float32 images, sigma 1.5", "qad_ms": round(qms, 3),
+                "grid_ms": round(gms, 3), "qad_mpx_s": round(npx / (qms * 1e-3) / 1e6, 1)}
     else:
         tms = _time_ms(lambda: det.subpix_to_correct_batch(x, thresh=0.1, sigma=2.0, nbr_radius=2.0, dense=True),
                        args.steps, stream)
@@ -572,8 +585,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-side", action="store_true", help="skip the other configurations' measurements")
     ap.add_argument("--launch-shape", default="", help="ROWS:tma|plain instead of autotuning, e.g. 254:tma")
-    ap.add_argument("--workload", default="batch", choices=["batch", "fwd_bwd", "subpix"],
-                    help="batch: the headline line; fwd_bwd / subpix: that secondary workload alone")
+    ap.add_argument("--workload", default="batch", choices=["batch", "fwd_bwd", "subpix", "qad"],
+                    help="batch: the headline line; fwd_bwd / subpix / qad: that secondary workload alone")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3

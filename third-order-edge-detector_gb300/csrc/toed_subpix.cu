@@ -113,7 +113,10 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
     __shared__ float sSm[kT + 4][kT + 4];     // rows/cols -2 .. +33
     __shared__ float sOx[kT + 2][kT + 3], sOy[kT + 2][kT + 3];  // -1 .. +32
     __shared__ float2 sDir[kT][kT];
-    __shared__ int sRowCnt[kT], sRowOff[kT];
+    __shared__ int sRowCnt[kT], sRowOff[kT], sCandOff[kT + 1];
+    __shared__ unsigned sOk[kT];              // per row: candidates the fit accepted
+    __shared__ short sCand[kT * kT];          // max-test candidates, row-major (tile pixel a * 32 + b)
+    __shared__ float3 sRes[kT * kT];          // per candidate: subpixel offset (x, y) and |max_f|
 
     const int t = blockIdx.x;
     const int k = find_image(p.n_maps, t, [&](int i) { return p.m[i].tile_base; });
@@ -185,8 +188,9 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
                 const float sgn = (oxy < 0.f) ? 1.f : ((oxy > 0.f) ? -1.f : 0.f);
                 th = atanf(oyy * sgn / (oxx + 1e-5f));  // :370-371
             }
-            // wrap_mod_pi (:216-222), then compute_dir_from_theta (:296-305)
-            float a2 = fmodf(th, PI_F);
+            // wrap_mod_pi (:216-222), then compute_dir_from_theta (:296-305);
+            // the estimate is an atan, |th| < pi/2, where fmod(th, pi) = th
+            float a2 = M.theta ? fmodf(th, PI_F) : th;
             if (a2 < 0.f) a2 += PI_F;
             float sn, cs;
             sincosf(a2, &sn, &cs);
@@ -196,15 +200,18 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
     }
     __syncthreads();
 
-    // NMS along dir on E (:424-514), margin mg: i, j in [mg + 1, dim - mg - 2)
-    unsigned bal[4];
-    double rx[4], ry[4], rm[4];
+    // NMS along dir on E (:424-514), margin mg: i, j in [mg + 1, dim - mg - 2).
+    // 1. per pixel, the max test along the sector's interpolated neighbours.
+    //    HYBRID decides in FP64 without a division: with ga = |g| along the
+    //    major axis (> 0) and gb along the minor one, slope = gb / ga, so
+    //    f > fp  <=>  f ga > Map (ga - gb) + Mdp gb, whose products of FP32
+    //    values are exact or rounded once in FP64.
+    unsigned bal1[4];
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         const int a = wid + 8 * u, b = lane;
         const int i = i0 + a, j = j0 + b;
-        bool acc = false;
-        rx[u] = ry[u] = rm[u] = 0.0;
+        bool cand = false;
         if (i >= M.margin + 1 && i < h - M.margin - 2 && j >= M.margin + 1 && j < w - M.margin - 2) {
             const float f = sE[a + HE][b + HE];
             const float2 g = sDir[a][b];
@@ -216,53 +223,102 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
                 const float Map = sE[a + HE + ar][b + HE + ac], Mdp = sE[a + HE + sy][b + HE + sx];
                 const float Mam = sE[a + HE - ar][b + HE - ac], Mdm = sE[a + HE - sy][b + HE - sx];
                 if (p.hyb) {
-                    const double gx = g.x, gy = g.y, fd = f;
-                    const double md = sqrt(gx * gx + gy * gy);
-                    const double nx = gx / md, ny = gy / md;
-                    const double sl = xmaj ? fabs(ny) / fabs(nx) : fabs(nx) / fabs(ny);
-                    const double fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
-                    if ((fd > fm && fd >= fp) || (fd >= fm && fd > fp)) {
-                        const double s = sqrt(1 + sl * sl);
-                        const double A = (fm + fp - 2 * fd) / (2 * s * s), B = (fp - fm) / (2 * s);
-                        if (!(fabs(A) < 1e-16)) {
-                            const double ss = -B / (2 * A);
-                            const double mf = A * ss * ss + B * ss + fd;
-                            if (fabs(ss) <= 1.4142135623730951) {
-                                acc = true;
-                                rx[u] = (double)j + ss * nx;
-                                ry[u] = (double)i + ss * ny;
-                                rm[u] = fabs(mf);
-                            }
-                        }
-                    }
+                    const double ga = xmaj ? fabsf(g.x) : fabsf(g.y), gb = xmaj ? fabsf(g.y) : fabsf(g.x);
+                    const double d = ga - gb;
+                    const double fpS = fma((double)Map, d, (double)Mdp * gb);
+                    const double fmS = fma((double)Mam, d, (double)Mdm * gb);
+                    const double fS = (double)f * ga;
+                    cand = (fS > fmS && fS >= fpS) || (fS >= fmS && fS > fpS);
                 } else {
                     const float md = sqrtf(g.x * g.x + g.y * g.y);
                     const float nx = g.x / md, ny = g.y / md;
                     const float sl = xmaj ? fabsf(ny) / fabsf(nx) : fabsf(nx) / fabsf(ny);
                     const float fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
-                    if ((f > fm && f >= fp) || (f >= fm && f > fp)) {
-                        const float s = sqrtf(1 + sl * sl);
-                        const float A = (fm + fp - 2 * f) / (2 * s * s), B = (fp - fm) / (2 * s);
-                        if (!(fabsf(A) < 1e-16f)) {
-                            const float ss = -B / (2 * A);
-                            const float mf = A * ss * ss + B * ss + f;
-                            if (fabsf(ss) <= 1.41421356f) {
-                                acc = true;
-                                rx[u] = (double)((float)j + ss * nx);
-                                ry[u] = (double)((float)i + ss * ny);
-                                rm[u] = (double)fabsf(mf);
-                            }
-                        }
-                    }
+                    cand = (f > fm && f >= fp) || (f >= fm && f > fp);
                 }
             }
         }
-        bal[u] = __ballot_sync(0xffffffffu, acc);
-        if (lane == 0) sRowCnt[a] = __popc(bal[u]);
+        bal1[u] = __ballot_sync(0xffffffffu, cand);
+        if (lane == 0) sRowCnt[a] = __popc(bal1[u]);
     }
+    if (tid < kT) sOk[tid] = 0u;
     __syncthreads();
     if (wid == 0) {
         const int cnt = sRowCnt[lane];
+        int incl = cnt;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int y = __shfl_up_sync(0xffffffffu, incl, d);
+            if (lane >= d) incl += y;
+        }
+        sCandOff[lane] = incl - cnt;
+        if (lane == 31) sCandOff[kT] = incl;
+    }
+    __syncthreads();
+    const unsigned ltm = (1u << lane) - 1u;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+        const int a = wid + 8 * u;
+        if ((bal1[u] >> lane) & 1u) sCand[sCandOff[a] + __popc(bal1[u] & ltm)] = (short)(a * kT + lane);
+    }
+    __syncthreads();
+    // 2. the parabola fit of the candidates, a thread each (:466-512): FP64
+    //    in HYBRID; subpixel offsets and |max_f| kept per candidate slot
+    const int ncand = sCandOff[kT];
+    for (int c = tid; c < ncand; c += blockDim.x) {
+        const int a = sCand[c] / kT, b = sCand[c] - (sCand[c] / kT) * kT;
+        const float f = sE[a + HE][b + HE];
+        const float2 g = sDir[a][b];
+        const bool xmaj = fabsf(g.x) >= fabsf(g.y);
+        const int sx = g.x >= 0.f ? 1 : -1, sy = g.y >= 0.f ? 1 : -1;
+        const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+        const float Map = sE[a + HE + ar][b + HE + ac], Mdp = sE[a + HE + sy][b + HE + sx];
+        const float Mam = sE[a + HE - ar][b + HE - ac], Mdm = sE[a + HE - sy][b + HE - sx];
+        bool ok = false;
+        float dx = 0.f, dy = 0.f, mag = 0.f;
+        if (p.hyb) {
+            const double gx = g.x, gy = g.y, fd = f;
+            const double md = sqrt(gx * gx + gy * gy);
+            const double nx = gx / md, ny = gy / md;
+            const double sl = xmaj ? fabs(ny) / fabs(nx) : fabs(nx) / fabs(ny);
+            const double fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
+            const double s = sqrt(1 + sl * sl);
+            const double A = (fm + fp - 2 * fd) / (2 * s * s), B = (fp - fm) / (2 * s);
+            if (!(fabs(A) < 1e-16)) {
+                const double ss = -B / (2 * A);
+                const double mf = A * ss * ss + B * ss + fd;
+                if (fabs(ss) <= 1.4142135623730951) {
+                    ok = true;
+                    dx = (float)(ss * nx);
+                    dy = (float)(ss * ny);
+                    mag = (float)fabs(mf);
+                }
+            }
+        } else {
+            const float md = sqrtf(g.x * g.x + g.y * g.y);
+            const float nx = g.x / md, ny = g.y / md;
+            const float sl = xmaj ? fabsf(ny) / fabsf(nx) : fabsf(nx) / fabsf(ny);
+            const float fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
+            const float s = sqrtf(1 + sl * sl);
+            const float A = (fm + fp - 2 * f) / (2 * s * s), B = (fp - fm) / (2 * s);
+            if (!(fabsf(A) < 1e-16f)) {
+                const float ss = -B / (2 * A);
+                const float mf = A * ss * ss + B * ss + f;
+                if (fabsf(ss) <= 1.41421356f) {
+                    ok = true;
+                    dx = ss * nx;
+                    dy = ss * ny;
+                    mag = fabsf(mf);
+                }
+            }
+        }
+        sRes[c] = make_float3(dx, dy, mag);
+        if (ok) atomicOr(&sOk[a], 1u << b);
+    }
+    __syncthreads();
+    // 3. the edgels in row-major order: staging slots, segment table, id map
+    if (wid == 0) {
+        const int cnt = __popc(sOk[lane]);
         int incl = cnt;
 #pragma unroll
         for (int d = 1; d < 32; d <<= 1) {
@@ -283,17 +339,23 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
         if (i < h) p.sc.seg[M.seg_base + (long long)i * M.ntx + tx] = make_int2(base + incl - cnt, cnt);
     }
     __syncthreads();
-    const unsigned ltm = (1u << lane) - 1u;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
         const int a = wid + 8 * u, b = lane;
         const int i = i0 + a, j = j0 + b;
         if (i >= h || j >= w) continue;
+        const unsigned okm = sOk[a];
         int id = -1;
-        if ((bal[u] >> lane) & 1u) {
-            id = sRowOff[a] + __popc(bal[u] & ltm);
+        if ((okm >> lane) & 1u) {
+            id = sRowOff[a] + __popc(okm & ltm);
             if (id < p.sc.staging_cap) {
-                p.sc.staging[id] = make_double4_32a(rx[u], ry[u], 0.0, rm[u]);
+                const float3 r = sRes[sCandOff[a] + __popc(bal1[u] & ltm)];
+                if (p.hyb)
+                    p.sc.staging[id] = make_double4_32a((double)j + (double)r.x, (double)i + (double)r.y, 0.0,
+                                                        (double)r.z);
+                else
+                    p.sc.staging[id] = make_double4_32a((double)((float)j + r.x), (double)((float)i + r.y), 0.0,
+                                                        (double)r.z);
                 p.sc.staging_idx[id] = i * w + j;
             } else {
                 id = -1;
@@ -363,9 +425,10 @@ __global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubPar
 
     // inputs with circular wrap: E, Hx = E dirx, Hy = E diry (:634-638)
     const int ri = i0 - HB - R, rj = j0 - HB - R;
+    const bool inside = ri >= 0 && rj >= 0 && ri + NI <= h && rj + NI <= w;  // no wrap needed
     for (int q = tid; q < NI * NI; q += blockDim.x) {
         const int a = q / NI, b = q - a * NI;
-        const int ii = wrap_circ(ri + a, h), jj = wrap_circ(rj + b, w);
+        const int ii = inside ? ri + a : wrap_circ(ri + a, h), jj = inside ? rj + b : wrap_circ(rj + b, w);
         const float e = load_map(M.E, M.dtype, (long long)ii * M.pitch + jj);
         const float2 d = p.dir[M.px_base + (long long)ii * w + jj];
         sE[q] = e;
@@ -430,58 +493,76 @@ __global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubPar
         sCol[7 * NO * NO + q] = hxy;
     }
     __syncthreads();
-    // per edgel: Keys bicubic of ten planes at (sx, sy), clamp to the image (:521-556)
+    // per edgel: Keys bicubic of ten planes at (sx, sy), clamp to the image
+    // (:521-556).  The interpolation is a short weighted sum of FP32
+    // convolution outputs and runs in FP32; the F vector, whose four products
+    // can cancel, is formed in FP64 from the interpolated values (HYBRID).
     for (int e = tid; e < n_edg; e += blockDim.x) {
-        int row = 0;
-        while (sOff[row + 1] <= e) ++row;
+        int row = 0;  // last row with sOff[row] <= e
+#pragma unroll
+        for (int st = 16; st >= 1; st >>= 1)
+            if (row + st < kT && sOff[row + st] <= e) row += st;
         const long long sidx = (long long)sSegOff[row] + (e - sOff[row]);
         if (sidx >= p.sc.staging_cap) continue;
         double4_32a rec = p.sc.staging[sidx];
         const double sx = rec.x, sy = rec.y;
         const int x0 = (int)floor(sx), y0 = (int)floor(sy);
         const double fx = sx - x0, fy = sy - y0;
-        double wx[4], wy[4];
-        wx[0] = cubic_w(fx + 1); wx[1] = cubic_w(fx); wx[2] = cubic_w(fx - 1); wx[3] = cubic_w(fx - 2);
-        wy[0] = cubic_w(fy + 1); wy[1] = cubic_w(fy); wy[2] = cubic_w(fy - 1); wy[3] = cubic_w(fy - 2);
+        float wx[4], wy[4];
+        wx[0] = (float)cubic_w(fx + 1); wx[1] = (float)cubic_w(fx); wx[2] = (float)cubic_w(fx - 1);
+        wx[3] = (float)cubic_w(fx - 2);
+        wy[0] = (float)cubic_w(fy + 1); wy[1] = (float)cubic_w(fy); wy[2] = (float)cubic_w(fy - 1);
+        wy[3] = (float)cubic_w(fy - 2);
         // plane order for interpolation: Px Py Pxx Pyy Pxy Hx Hxx Hxy Hyy Hy
-        double v[10];
+        float v[10];
 #pragma unroll
-        for (int pl = 0; pl < 10; ++pl) v[pl] = 0.0;
+        for (int pl = 0; pl < 10; ++pl) v[pl] = 0.f;
+#pragma unroll
         for (int pp = 0; pp < 4; ++pp) {
             int ii = y0 - 1 + pp;
             ii = ii < 0 ? 0 : (ii >= h ? h - 1 : ii);
             const int ra = ii - (i0 - HB);           // row in the conv region
             const int rin = ii - ri;                 // row in the input region
-            double rowv[10];
+            float rowv[10];
 #pragma unroll
-            for (int pl = 0; pl < 10; ++pl) rowv[pl] = 0.0;
+            for (int pl = 0; pl < 10; ++pl) rowv[pl] = 0.f;
+#pragma unroll
             for (int qq = 0; qq < 4; ++qq) {
                 int jj = x0 - 1 + qq;
                 jj = jj < 0 ? 0 : (jj >= w ? w - 1 : jj);
                 const int ca = jj - (j0 - HB);
                 const int cin = jj - rj;
                 const int o = ra * NO + ca;
-                const double wq = wx[qq];
-                rowv[0] += (double)sCol[0 * NO * NO + o] * wq;
-                rowv[1] += (double)sCol[1 * NO * NO + o] * wq;
-                rowv[2] += (double)sCol[2 * NO * NO + o] * wq;
-                rowv[3] += (double)sCol[4 * NO * NO + o] * wq;
-                rowv[4] += (double)sCol[3 * NO * NO + o] * wq;
-                rowv[5] += (double)sHx[rin * NI + cin] * wq;
-                rowv[6] += (double)sCol[5 * NO * NO + o] * wq;
-                rowv[7] += (double)sCol[7 * NO * NO + o] * wq;
-                rowv[8] += (double)sCol[6 * NO * NO + o] * wq;
-                rowv[9] += (double)sHy[rin * NI + cin] * wq;
+                const float wq = wx[qq];
+                rowv[0] = fmaf(sCol[0 * NO * NO + o], wq, rowv[0]);
+                rowv[1] = fmaf(sCol[1 * NO * NO + o], wq, rowv[1]);
+                rowv[2] = fmaf(sCol[2 * NO * NO + o], wq, rowv[2]);
+                rowv[3] = fmaf(sCol[4 * NO * NO + o], wq, rowv[3]);
+                rowv[4] = fmaf(sCol[3 * NO * NO + o], wq, rowv[4]);
+                rowv[5] = fmaf(sHx[rin * NI + cin], wq, rowv[5]);
+                rowv[6] = fmaf(sCol[5 * NO * NO + o], wq, rowv[6]);
+                rowv[7] = fmaf(sCol[7 * NO * NO + o], wq, rowv[7]);
+                rowv[8] = fmaf(sCol[6 * NO * NO + o], wq, rowv[8]);
+                rowv[9] = fmaf(sHy[rin * NI + cin], wq, rowv[9]);
             }
 #pragma unroll
-            for (int pl = 0; pl < 10; ++pl) v[pl] += rowv[pl] * wy[pp];
+            for (int pl = 0; pl < 10; ++pl) v[pl] = fmaf(rowv[pl], wy[pp], v[pl]);
         }
-        const double Px = v[0], Py = v[1], Pxx = v[2], Pyy = v[3], Pxy = v[4];
-        const double Hx = v[5], Hxx = v[6], Hxy = v[7], Hyy = v[8], Hy = v[9];
-        double Fx = Px * Hxx + Pxx * Hx + Py * Hxy + Pxy * Hy;  // :683-684
-        double Fy = Px * Hxy + Pxy * Hx + Py * Hyy + Pyy * Hy;
-        const double Fm = sqrt(Fx * Fx + Fy * Fy);
         float ori;
+        double Fx, Fy, Fm;
+        if (p.hyb) {
+            const double Px = v[0], Py = v[1], Pxx = v[2], Pyy = v[3], Pxy = v[4];
+            const double Hx = v[5], Hxx = v[6], Hxy = v[7], Hyy = v[8], Hy = v[9];
+            Fx = Px * Hxx + Pxx * Hx + Py * Hxy + Pxy * Hy;  // :683-684
+            Fy = Px * Hxy + Pxy * Hx + Py * Hyy + Pyy * Hy;
+            Fm = sqrt(Fx * Fx + Fy * Fy);
+        } else {
+            const float fFx = v[0] * v[6] + v[2] * v[5] + v[1] * v[7] + v[4] * v[9];
+            const float fFy = v[0] * v[7] + v[4] * v[5] + v[1] * v[8] + v[3] * v[9];
+            Fx = fFx;
+            Fy = fFy;
+            Fm = sqrtf(fFx * fFx + fFy * fFy);
+        }
         if (Fm < 1e-12) {
             const int pi = p.sc.staging_idx[sidx];
             const float2 d = p.dir[M.px_base + pi];
