@@ -373,17 +373,24 @@ struct CorrCfg {
     static constexpr int HB = 3;                  // bicubic reach around a tile pixel
     static constexpr int NO = kT + 2 * HB;        // 38: conv output region side
     static constexpr int NI = NO + 2 * R;         // input region side
-    static constexpr size_t off_E = 0;                                   // [NI][NI]
-    static constexpr size_t off_Hx = off_E + sizeof(float) * NI * NI;    // [NI][NI]
-    static constexpr size_t off_Hy = off_Hx + sizeof(float) * NI * NI;   // [NI][NI]
-    static constexpr size_t off_row = off_Hy + sizeof(float) * NI * NI;  // 6 x [NI][NO]
-    static constexpr size_t off_col = off_row + sizeof(float) * 6 * NI * NO;  // 8 x [NO][NO]
-    static constexpr size_t off_misc = off_col + sizeof(float) * 8 * NO * NO;
+    // Hx, Hy live through the whole kernel; E only until the row pass, after
+    // which its space (grown to 5 planes) takes the column planes Px Py Pxx
+    // Pxy Pyy; the row-pass planes 0-2 are dead once those are done and take
+    // Hxx Hyy Hxy.  About 101 KB at r = 8: two CTAs per SM.
+    static constexpr int NA = (NI * NI > 5 * NO * NO) ? NI * NI : 5 * NO * NO;
+    static constexpr size_t off_Hx = 0;                                     // [NI][NI]
+    static constexpr size_t off_Hy = off_Hx + sizeof(float) * NI * NI;      // [NI][NI]
+    static constexpr size_t off_E = off_Hy + sizeof(float) * NI * NI;       // [NI][NI], then 5 x [NO][NO]
+    static constexpr size_t off_row = off_E + sizeof(float) * NA;           // 6 x [NI][NO], then 3 x [NO][NO]
+    static constexpr size_t off_colA = off_E;
+    static constexpr size_t off_colB = off_row;
+    static_assert(3 * NO * NO <= 3 * NI * NO, "Hxx Hyy Hxy fit in the dead row planes 0-2");
+    static constexpr size_t off_misc = off_row + sizeof(float) * 6 * NI * NO;
     static constexpr size_t smem = off_misc + sizeof(int) * 2 * (kT + 1);
 };
 
 template <int R>
-__global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubParams p)
+__global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ SubParams p)
 {
     using C = CorrCfg<R>;
     constexpr int NI = C::NI, NO = C::NO, HB = C::HB;
@@ -392,7 +399,8 @@ __global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubPar
     float* sHx = reinterpret_cast<float*>(smem + C::off_Hx);
     float* sHy = reinterpret_cast<float*>(smem + C::off_Hy);
     float* sRow = reinterpret_cast<float*>(smem + C::off_row);
-    float* sCol = reinterpret_cast<float*>(smem + C::off_col);
+    float* sColA = reinterpret_cast<float*>(smem + C::off_colA);  // Px Py Pxx Pxy Pyy
+    float* sColB = reinterpret_cast<float*>(smem + C::off_colB);  // Hxx Hyy Hxy
     int* sOff = reinterpret_cast<int*>(smem + C::off_misc);  // [kT+1] exclusive prefix of row counts
     int* sSegOff = sOff + kT + 1;                             // [kT] staging offsets
 
@@ -437,62 +445,108 @@ __global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubPar
     }
     __syncthreads();
     // row pass (along j): E -> G, dG, d2G ; Hx -> dG ; Hy -> G, dG
-    // out(x) = sum_q src(x - q) k(q)  (:392-396)
-    for (int q = tid; q < NI * NO; q += blockDim.x) {
-        const int a = q / NO, c = q - a * NO;
-        const float* e = sE + a * NI + c + R;
-        const float* hx = sHx + a * NI + c + R;
-        const float* hy = sHy + a * NI + c + R;
-        float eG = 0.f, edG = 0.f, ed2G = 0.f, xdG = 0.f, yG = 0.f, ydG = 0.f;
+    // out(x) = sum_q src(x - q) k(q)  (:392-396).  A thread takes 4
+    // consecutive outputs of a row and slides one window of 2r + 4 inputs.
+    constexpr int G = 4, NG = (NO + G - 1) / G, NW = 2 * R + G;
+    for (int q = tid; q < NI * NG; q += blockDim.x) {
+        const int a = q / NG, c0 = (q - a * NG) * G;
+        float acc[6][G];
 #pragma unroll
-        for (int qq = -R; qq <= R; ++qq) {
-            const float g0 = p.g[0][qq + R], g1 = p.g[1][qq + R], g2 = p.g[2][qq + R];
-            const float ve = e[-qq], vx = hx[-qq], vy = hy[-qq];
-            eG = fmaf(ve, g0, eG);
-            edG = fmaf(ve, g1, edG);
-            ed2G = fmaf(ve, g2, ed2G);
-            xdG = fmaf(vx, g1, xdG);
-            yG = fmaf(vy, g0, yG);
-            ydG = fmaf(vy, g1, ydG);
+        for (int f = 0; f < 6; ++f)
+#pragma unroll
+            for (int o = 0; o < G; ++o) acc[f][o] = 0.f;
+#pragma unroll
+        for (int src = 0; src < 3; ++src) {
+            const float* row = (src == 0 ? sE : (src == 1 ? sHx : sHy)) + a * NI + c0;
+            float win[NW];
+#pragma unroll
+            for (int t = 0; t < NW; ++t) win[t] = (c0 + t < NI) ? row[t] : 0.f;
+#pragma unroll
+            for (int qq = -R; qq <= R; ++qq) {
+                const float g0 = p.g[0][qq + R], g1 = p.g[1][qq + R], g2 = p.g[2][qq + R];
+#pragma unroll
+                for (int o = 0; o < G; ++o) {
+                    const float x = win[o + R - qq];  // src(c0 + o - qq), window index o + R - qq
+                    if (src == 0) {
+                        acc[0][o] = fmaf(x, g0, acc[0][o]);
+                        acc[1][o] = fmaf(x, g1, acc[1][o]);
+                        acc[2][o] = fmaf(x, g2, acc[2][o]);
+                    } else if (src == 1) {
+                        acc[3][o] = fmaf(x, g1, acc[3][o]);
+                    } else {
+                        acc[4][o] = fmaf(x, g0, acc[4][o]);
+                        acc[5][o] = fmaf(x, g1, acc[5][o]);
+                    }
+                }
+            }
         }
-        sRow[(0 * NI + a) * NO + c] = eG;
-        sRow[(1 * NI + a) * NO + c] = edG;
-        sRow[(2 * NI + a) * NO + c] = ed2G;
-        sRow[(3 * NI + a) * NO + c] = xdG;
-        sRow[(4 * NI + a) * NO + c] = yG;
-        sRow[(5 * NI + a) * NO + c] = ydG;
+#pragma unroll
+        for (int o = 0; o < G; ++o)
+            if (c0 + o < NO)
+#pragma unroll
+                for (int f = 0; f < 6; ++f) sRow[(f * NI + a) * NO + c0 + o] = acc[f][o];
     }
     __syncthreads();
-    // column pass (along i): planes 0 Px 1 Py 2 Pxx 3 Pxy 4 Pyy 5 Hxx 6 Hyy 7 Hxy (:641-648)
-    for (int q = tid; q < NO * NO; q += blockDim.x) {
-        const int a = q / NO, c = q - a * NO;
-        float px = 0.f, py = 0.f, pxx = 0.f, pxy = 0.f, pyy = 0.f, hxx = 0.f, hyy = 0.f, hxy = 0.f;
+    // column pass (along i) (:641-648): first Px Py Pxx Pxy Pyy from the E
+    // row planes 0-2, then Hxx Hyy Hxy from planes 3-5 into the space of
+    // planes 0-2; a thread takes 4 consecutive output rows of a column
 #pragma unroll
-        for (int pp = -R; pp <= R; ++pp) {
-            const int row = a + R - pp;
-            const float g0 = p.g[0][pp + R], g1 = p.g[1][pp + R], g2 = p.g[2][pp + R];
-            const float eG = sRow[(0 * NI + row) * NO + c], edG = sRow[(1 * NI + row) * NO + c];
-            const float ed2G = sRow[(2 * NI + row) * NO + c], xdG = sRow[(3 * NI + row) * NO + c];
-            const float yG = sRow[(4 * NI + row) * NO + c], ydG = sRow[(5 * NI + row) * NO + c];
-            px = fmaf(edG, g0, px);    // (dG, G)  E
-            py = fmaf(eG, g1, py);     // (G, dG)  E
-            pxx = fmaf(ed2G, g0, pxx); // (d2G, G) E
-            pxy = fmaf(edG, g1, pxy);  // (dG, dG) E
-            pyy = fmaf(eG, g2, pyy);   // (G, d2G) E
-            hxx = fmaf(xdG, g0, hxx);  // (dG, G)  Hx
-            hyy = fmaf(yG, g1, hyy);   // (G, dG)  Hy
-            hxy = fmaf(ydG, g0, hxy);  // (dG, G)  Hy
+    for (int half = 0; half < 2; ++half) {
+        for (int q = tid; q < NG * NO; q += blockDim.x) {
+            const int a0 = (q / NO) * G, c = q - (q / NO) * NO;
+            float o0[G], o1[G], o2[G], o3[G], o4[G];
+#pragma unroll
+            for (int o = 0; o < G; ++o) o0[o] = o1[o] = o2[o] = o3[o] = o4[o] = 0.f;
+#pragma unroll
+            for (int f = 3 * half; f < 3 * half + 3; ++f) {
+                // rows a0 .. a0 + 2r + 3 of row-pass plane f at column c (output row a uses row a + R - pp)
+                const float* col = sRow + (f * NI + a0) * NO + c;
+                float win[NW];
+#pragma unroll
+                for (int t = 0; t < NW; ++t) win[t] = (a0 + t < NI) ? col[t * NO] : 0.f;
+#pragma unroll
+                for (int pp = -R; pp <= R; ++pp) {
+                    const float g0 = p.g[0][pp + R], g1 = p.g[1][pp + R], g2 = p.g[2][pp + R];
+#pragma unroll
+                    for (int o = 0; o < G; ++o) {
+                        const float x = win[o + R - pp];
+                        if (f == 0) {          // eG
+                            o1[o] = fmaf(x, g1, o1[o]);  // Py  (G, dG)  E
+                            o4[o] = fmaf(x, g2, o4[o]);  // Pyy (G, d2G) E
+                        } else if (f == 1) {   // edG
+                            o0[o] = fmaf(x, g0, o0[o]);  // Px  (dG, G)  E
+                            o3[o] = fmaf(x, g1, o3[o]);  // Pxy (dG, dG) E
+                        } else if (f == 2) {   // ed2G
+                            o2[o] = fmaf(x, g0, o2[o]);  // Pxx (d2G, G) E
+                        } else if (f == 3) {   // xdG
+                            o0[o] = fmaf(x, g0, o0[o]);  // Hxx (dG, G)  Hx
+                        } else if (f == 4) {   // yG
+                            o1[o] = fmaf(x, g1, o1[o]);  // Hyy (G, dG)  Hy
+                        } else {               // ydG
+                            o2[o] = fmaf(x, g0, o2[o]);  // Hxy (dG, G)  Hy
+                        }
+                    }
+                }
+            }
+#pragma unroll
+            for (int o = 0; o < G; ++o) {
+                if (a0 + o >= NO) break;
+                const int qo = (a0 + o) * NO + c;
+                if (half == 0) {
+                    sColA[0 * NO * NO + qo] = o0[o];
+                    sColA[1 * NO * NO + qo] = o1[o];
+                    sColA[2 * NO * NO + qo] = o2[o];
+                    sColA[3 * NO * NO + qo] = o3[o];
+                    sColA[4 * NO * NO + qo] = o4[o];
+                } else {
+                    sColB[0 * NO * NO + qo] = o0[o];
+                    sColB[1 * NO * NO + qo] = o1[o];
+                    sColB[2 * NO * NO + qo] = o2[o];
+                }
+            }
         }
-        sCol[0 * NO * NO + q] = px;
-        sCol[1 * NO * NO + q] = py;
-        sCol[2 * NO * NO + q] = pxx;
-        sCol[3 * NO * NO + q] = pxy;
-        sCol[4 * NO * NO + q] = pyy;
-        sCol[5 * NO * NO + q] = hxx;
-        sCol[6 * NO * NO + q] = hyy;
-        sCol[7 * NO * NO + q] = hxy;
+        __syncthreads();
     }
-    __syncthreads();
     // per edgel: Keys bicubic of ten planes at (sx, sy), clamp to the image
     // (:521-556).  The interpolation is a short weighted sum of FP32
     // convolution outputs and runs in FP32; the F vector, whose four products
@@ -534,15 +588,15 @@ __global__ void __launch_bounds__(512) tc_correct(const __grid_constant__ SubPar
                 const int cin = jj - rj;
                 const int o = ra * NO + ca;
                 const float wq = wx[qq];
-                rowv[0] = fmaf(sCol[0 * NO * NO + o], wq, rowv[0]);
-                rowv[1] = fmaf(sCol[1 * NO * NO + o], wq, rowv[1]);
-                rowv[2] = fmaf(sCol[2 * NO * NO + o], wq, rowv[2]);
-                rowv[3] = fmaf(sCol[4 * NO * NO + o], wq, rowv[3]);
-                rowv[4] = fmaf(sCol[3 * NO * NO + o], wq, rowv[4]);
+                rowv[0] = fmaf(sColA[0 * NO * NO + o], wq, rowv[0]);
+                rowv[1] = fmaf(sColA[1 * NO * NO + o], wq, rowv[1]);
+                rowv[2] = fmaf(sColA[2 * NO * NO + o], wq, rowv[2]);
+                rowv[3] = fmaf(sColA[4 * NO * NO + o], wq, rowv[3]);
+                rowv[4] = fmaf(sColA[3 * NO * NO + o], wq, rowv[4]);
                 rowv[5] = fmaf(sHx[rin * NI + cin], wq, rowv[5]);
-                rowv[6] = fmaf(sCol[5 * NO * NO + o], wq, rowv[6]);
-                rowv[7] = fmaf(sCol[7 * NO * NO + o], wq, rowv[7]);
-                rowv[8] = fmaf(sCol[6 * NO * NO + o], wq, rowv[8]);
+                rowv[6] = fmaf(sColB[0 * NO * NO + o], wq, rowv[6]);
+                rowv[7] = fmaf(sColB[2 * NO * NO + o], wq, rowv[7]);
+                rowv[8] = fmaf(sColB[1 * NO * NO + o], wq, rowv[8]);
                 rowv[9] = fmaf(sHy[rin * NI + cin], wq, rowv[9]);
             }
 #pragma unroll
