@@ -102,6 +102,15 @@ __device__ __forceinline__ double cubic_w(double s)
     return 0.0;
 }
 
+__device__ __forceinline__ float cubic_wf(float s)
+{  // the same kernel in FP32, for interpolation weights of FP32 data
+    const float a = -0.5f;
+    const float x = fabsf(s);
+    if (x <= 1.f) return ((a + 2.f) * x - (a + 3.f)) * x * x + 1.f;
+    if (x < 2.f) return ((a * x - 5.f * a) * x + 8.f * a) * x - 4.f * a;
+    return 0.f;
+}
+
 // ---------------------------------------------------------------------------
 // Orientation + NMS
 // ---------------------------------------------------------------------------
@@ -127,9 +136,11 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
     const int i0 = ty * kT, j0 = tx * kT;
     const int tid = threadIdx.x, lane = tid & 31, wid = tid >> 5;
 
+    const bool inside = i0 - HE >= 0 && j0 - HE >= 0 && i0 - HE + NE <= h && j0 - HE + NE <= w;  // no padding
     for (int q = tid; q < NE * NE; q += blockDim.x) {
         const int a = q / NE, b = q - a * NE;
-        const int ii = wrap_sym(i0 - HE + a, h), jj = wrap_sym(j0 - HE + b, w);
+        const int ii = inside ? i0 - HE + a : wrap_sym(i0 - HE + a, h);
+        const int jj = inside ? j0 - HE + b : wrap_sym(j0 - HE + b, w);
         sE[a][b] = load_map(M.E, dtype, (long long)ii * M.pitch + jj);
     }
     __syncthreads();
@@ -223,12 +234,22 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
                 const float Map = sE[a + HE + ar][b + HE + ac], Mdp = sE[a + HE + sy][b + HE + sx];
                 const float Mam = sE[a + HE - ar][b + HE - ac], Mdm = sE[a + HE - sy][b + HE - sx];
                 if (p.hyb) {
-                    const double ga = xmaj ? fabsf(g.x) : fabsf(g.y), gb = xmaj ? fabsf(g.y) : fabsf(g.x);
-                    const double d = ga - gb;
-                    const double fpS = fma((double)Map, d, (double)Mdp * gb);
-                    const double fmS = fma((double)Mam, d, (double)Mdm * gb);
-                    const double fS = (double)f * ga;
-                    cand = (fS > fmS && fS >= fpS) || (fS >= fmS && fS > fpS);
+                    // FP32 first; the FP64 form only where f lies within the FP32
+                    // rounding bound of fp or fm (a few pixels per map)
+                    const float ga = xmaj ? fabsf(g.x) : fabsf(g.y), gb = xmaj ? fabsf(g.y) : fabsf(g.x);
+                    const float fpS = fmaf(Map, ga - gb, Mdp * gb), fmS = fmaf(Mam, ga - gb, Mdm * gb);
+                    const float fS = f * ga;
+                    // |FP32 - exact| <= ~3e-7 (|f| + |Map| + |Mdp| + |Mam| + |Mdm|) ga; 30x margin
+                    const float tol = 1e-5f * ga * (fabsf(f) + fabsf(Map) + fabsf(Mdp) + fabsf(Mam) + fabsf(Mdm));
+                    if (fabsf(fS - fpS) > tol && fabsf(fS - fmS) > tol) {
+                        cand = fS > fmS && fS > fpS;
+                    } else {
+                        const double gad = ga, gbd = gb, d = gad - gbd;
+                        const double fpD = fma((double)Map, d, (double)Mdp * gbd);
+                        const double fmD = fma((double)Mam, d, (double)Mdm * gbd);
+                        const double fD = (double)f * gad;
+                        cand = (fD > fmD && fD >= fpD) || (fD >= fmD && fD > fpD);
+                    }
                 } else {
                     const float md = sqrtf(g.x * g.x + g.y * g.y);
                     const float nx = g.x / md, ny = g.y / md;
@@ -562,11 +583,13 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
         const double sx = rec.x, sy = rec.y;
         const int x0 = (int)floor(sx), y0 = (int)floor(sy);
         const double fx = sx - x0, fy = sy - y0;
+        const float tfx = (float)fx, tfy = (float)fy;
         float wx[4], wy[4];
-        wx[0] = (float)cubic_w(fx + 1); wx[1] = (float)cubic_w(fx); wx[2] = (float)cubic_w(fx - 1);
-        wx[3] = (float)cubic_w(fx - 2);
-        wy[0] = (float)cubic_w(fy + 1); wy[1] = (float)cubic_w(fy); wy[2] = (float)cubic_w(fy - 1);
-        wy[3] = (float)cubic_w(fy - 2);
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+            wx[q] = cubic_wf(tfx + 1.f - (float)q);
+            wy[q] = cubic_wf(tfy + 1.f - (float)q);
+        }
         // plane order for interpolation: Px Py Pxx Pyy Pxy Hx Hxx Hxy Hyy Hy
         float v[10];
 #pragma unroll
