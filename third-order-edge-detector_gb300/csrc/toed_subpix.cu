@@ -298,21 +298,24 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
         bool ok = false;
         float dx = 0.f, dy = 0.f, mag = 0.f;
         if (p.hyb) {
-            const double gx = g.x, gy = g.y, fd = f;
-            const double md = sqrt(gx * gx + gy * gy);
-            const double nx = gx / md, ny = gy / md;
-            const double sl = xmaj ? fabs(ny) / fabs(nx) : fabs(nx) / fabs(ny);
-            const double fp = Map * (1 - sl) + Mdp * sl, fm = Mam * (1 - sl) + Mdm * sl;
-            const double s = sqrt(1 + sl * sl);
-            const double A = (fm + fp - 2 * fd) / (2 * s * s), B = (fp - fm) / (2 * s);
-            if (!(fabs(A) < 1e-16)) {
-                const double ss = -B / (2 * A);
-                const double mf = A * ss * ss + B * ss + fd;
-                if (fabs(ss) <= 1.4142135623730951) {
+            // fp - fm and fm + fp - 2f cancel: formed in FP64 from the FP32
+            // inputs; the well-conditioned rest in FP32.  s* = -B / (2A) with
+            // A = (fm + fp - 2f) / (2 s^2), B = (fp - fm) / (2 s) (:496-505)
+            const float md = sqrtf(g.x * g.x + g.y * g.y);
+            const float nx = g.x / md, ny = g.y / md;
+            const float sl = xmaj ? fabsf(ny) / fabsf(nx) : fabsf(nx) / fabsf(ny);
+            const double s1 = sl, c1 = 1.0 - s1;
+            const double fp = (double)Map * c1 + (double)Mdp * s1, fm = (double)Mam * c1 + (double)Mdm * s1;
+            const double num = fp - fm, den = fm + fp - 2.0 * (double)f;
+            const float s = sqrtf(1.f + sl * sl);
+            if (!(fabs(den) < 2e-16 * (double)(s * s))) {  // |A| < 1e-16 (:502)
+                const float ss = -0.5f * (float)num * s / (float)den;
+                const float mf = f - 0.125f * (float)num * (float)num / (float)den;  // A s*^2 + B s* + f
+                if (fabsf(ss) <= 1.41421356f) {
                     ok = true;
-                    dx = (float)(ss * nx);
-                    dy = (float)(ss * ny);
-                    mag = (float)fabs(mf);
+                    dx = ss * nx;
+                    dy = ss * ny;
+                    mag = fabsf(mf);
                 }
             }
         } else {
