@@ -197,11 +197,23 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
                 const float oyy = (i == 0) ? sOy[e + 1][f] - sOy[e][f]
                                            : (i == h - 1 ? sOy[e][f] - sOy[e - 1][f] : 0.5f * (sOy[e + 1][f] - sOy[e - 1][f]));
                 const float sgn = (oxy < 0.f) ? 1.f : ((oxy > 0.f) ? -1.f : 0.f);
-                th = atanf(oyy * sgn / (oxx + 1e-5f));  // :370-371
+                const float x = oxx + 1e-5f, y = oyy * sgn;
+                if (x != 0.f) {
+                    // th = atan(y / x) (:370-371) lies in (-pi/2, pi/2), so
+                    // wrap_mod_pi (:216-222) adds pi exactly when th < 0, and
+                    // compute_dir_from_theta (:296-305) is (cos, sin) of that:
+                    // (|x|, y sgn x) / |(x, y)|, negated when x y < 0
+                    const float rn = rsqrtf(fmaf(x, x, y * y));
+                    const float cx = fabsf(x) * rn, sy = copysignf(1.f, x) * y * rn;
+                    const float2 d = (x * y < 0.f) ? make_float2(-cx, -sy) : make_float2(cx, sy);
+                    sDir[a][b] = d;
+                    p.dir[M.px_base + (long long)i * w + j] = d;
+                    continue;
+                }
+                th = atanf(y / x);
             }
-            // wrap_mod_pi (:216-222), then compute_dir_from_theta (:296-305);
-            // the estimate is an atan, |th| < pi/2, where fmod(th, pi) = th
-            float a2 = M.theta ? fmodf(th, PI_F) : th;
+            // wrap_mod_pi (:216-222), then compute_dir_from_theta (:296-305)
+            float a2 = fmodf(th, PI_F);
             if (a2 < 0.f) a2 += PI_F;
             float sn, cs;
             sincosf(a2, &sn, &cs);
