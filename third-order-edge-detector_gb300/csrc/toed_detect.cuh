@@ -328,11 +328,14 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         x = (double)(0.5f * (float)(Gc - 1)) + (double)(0.5f * sst * nx);
         y = (double)(0.5f * (float)(Gr - 1)) + (double)(0.5f * sst * ny);
         str = sqrtf((maxf * nx) * (maxf * nx) + (maxf * ny) * (maxf * ny));
+        // cpu_toed.cpp:227-232 with the shared products factored out (FP64):
+        // TIx = 2 (fx (fxx^2 + fxy^2) + fy fxy (fxx + fyy) + fx fy fxxy) + fy^2 fxyy + fx^2 fxxx
+        // TIy = 2 (fx fxy (fxx + fyy) + fy (fyy^2 + fxy^2) + fx fy fxyy) + fx^2 fxxy + fy^2 fyyy
         const double dfx = gx, dfy = gy, dxx = fxx, dxy = fxy, dyy = fyy;
-        const double tix = dfx * (2.0 * dxx * dxx + 2.0 * dxy * dxy) + dfy * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
-                           2.0 * dfx * dfy * (double)fxxy + dfy * dfy * (double)fxyy + dfx * dfx * (double)fxxx;
-        const double tiy = dfx * (2.0 * dxx * dxy + 2.0 * dyy * dxy) + dfy * (2.0 * dyy * dyy + 2.0 * dxy * dxy) +
-                           2.0 * dfx * dfy * (double)fxyy + dfx * dfx * (double)fxxy + dfy * dfy * (double)fyyy;
+        const double a2 = dxx * dxx + dxy * dxy, c2 = dyy * dyy + dxy * dxy, bc = dxy * (dxx + dyy);
+        const double pxy = dfx * dfy, x2 = dfx * dfx, y2 = dfy * dfy;
+        const double tix = 2.0 * (dfx * a2 + dfy * bc + pxy * (double)fxxy) + y2 * (double)fxyy + x2 * (double)fxxx;
+        const double tiy = 2.0 * (dfx * bc + dfy * c2 + pxy * (double)fxyy) + x2 * (double)fxxy + y2 * (double)fyyy;
         ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000) : atan2f((float)tix, (float)(-tiy));
     } else {
         const float fp = Map * (1.f - sl) + Mdp * sl;
