@@ -16,34 +16,34 @@
 #include "toed_internal.h"
 
 namespace toed {
-DetectEntry detect_entry_r1(bool);
-DetectEntry detect_entry_r2(bool);
-DetectEntry detect_entry_r3(bool);
-DetectEntry detect_entry_r4(bool);
-DetectEntry detect_entry_r5(bool);
-DetectEntry detect_entry_r6(bool);
-DetectEntry detect_entry_r7(bool);
-DetectEntry detect_entry_r8(bool);
-DetectEntry detect_entry_r9(bool);
-DetectEntry detect_entry_r10(bool);
-DetectEntry detect_entry_r11(bool);
-DetectEntry detect_entry_r12(bool);
+DetectEntry detect_entry_r1(bool, bool);
+DetectEntry detect_entry_r2(bool, bool);
+DetectEntry detect_entry_r3(bool, bool);
+DetectEntry detect_entry_r4(bool, bool);
+DetectEntry detect_entry_r5(bool, bool);
+DetectEntry detect_entry_r6(bool, bool);
+DetectEntry detect_entry_r7(bool, bool);
+DetectEntry detect_entry_r8(bool, bool);
+DetectEntry detect_entry_r9(bool, bool);
+DetectEntry detect_entry_r10(bool, bool);
+DetectEntry detect_entry_r11(bool, bool);
+DetectEntry detect_entry_r12(bool, bool);
 
-DetectEntry detect_entry(int r, bool hyb)
+DetectEntry detect_entry(int r, bool hyb, bool async)
 {
     switch (r) {
-    case 1: return detect_entry_r1(hyb);
-    case 2: return detect_entry_r2(hyb);
-    case 3: return detect_entry_r3(hyb);
-    case 4: return detect_entry_r4(hyb);
-    case 5: return detect_entry_r5(hyb);
-    case 6: return detect_entry_r6(hyb);
-    case 7: return detect_entry_r7(hyb);
-    case 8: return detect_entry_r8(hyb);
-    case 9: return detect_entry_r9(hyb);
-    case 10: return detect_entry_r10(hyb);
-    case 11: return detect_entry_r11(hyb);
-    case 12: return detect_entry_r12(hyb);
+    case 1: return detect_entry_r1(hyb, async);
+    case 2: return detect_entry_r2(hyb, async);
+    case 3: return detect_entry_r3(hyb, async);
+    case 4: return detect_entry_r4(hyb, async);
+    case 5: return detect_entry_r5(hyb, async);
+    case 6: return detect_entry_r6(hyb, async);
+    case 7: return detect_entry_r7(hyb, async);
+    case 8: return detect_entry_r8(hyb, async);
+    case 9: return detect_entry_r9(hyb, async);
+    case 10: return detect_entry_r10(hyb, async);
+    case 11: return detect_entry_r11(hyb, async);
+    case 12: return detect_entry_r12(hyb, async);
     default: return DetectEntry{nullptr, 0};
     }
 }
@@ -148,7 +148,7 @@ struct toed_ctx {
     long long keep_cap = 0;
     double* sp_work = nullptr;  // TO correction at interp_n > 0: maps resized onto the work grid
     long long sp_work_cap = 0;
-    int blocks_per_sm[TOED_MAX_RADIUS + 1][2] = {};
+    int blocks_per_sm[TOED_MAX_RADIUS + 1][2][2] = {};  // [radius][hybrid][async row staging]
     // launch shape chosen by toed_autotune per (radius, precision, size class of
     // the launch: floor(log2(pixels))); strip_rows 0 = heuristic
     toed_tuning tune[TOED_MAX_RADIUS + 1][2][kSizeClasses] = {};
@@ -353,13 +353,17 @@ static int plan_strip_rows(const toed_image* images, int n, long long resident)
     return kStepRows - 2;
 }
 
+// plain_loads: never stage input rows by TMA (images read in place from
+// page-locked host memory through their device mapping): float32 rows by
+// per-thread async copies one step ahead, uint8 rows by plain loads
 static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr)
+                                int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr,
+                                bool plain_loads = false)
 {
     const bool hyb = prm->precision != TOED_FP32;
-    DetectEntry ent = detect_entry(r, hyb);
+    DetectEntry ent = detect_entry(r, hyb, plain_loads);
     if (!ent.func) return TOED_ERR_UNSUPPORTED;
-    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0];
+    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0][plain_loads ? 1 : 0];
     if (bps == 0) {
         TOED_CU(cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem));
         TOED_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ent.func, kThreads, ent.smem));
@@ -399,7 +403,10 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
         encode_rows_map(&p->tmap[i], d, r);
-        if (use && !use->staging) d.tma = 0;
+        if (plain_loads)
+            d.tma = (d.dtype == TOED_F32) ? 2 : 0;  // async row copies (float32) or plain loads, never TMA
+        else if (use && !use->staging)
+            d.tma = 0;
         const long long nseg = 2LL * im.height * d.nsc;
         d.nseg = nseg;
         units += (long long)d.nsc * d.nsr;
@@ -457,12 +464,12 @@ static toed_status check_batch(const toed_ctx* c, const toed_image* images, int 
 
 // The batch in chunks of kBatchMax images (caller holds c->mu, device set).
 static toed_status detect_all(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                              cudaStream_t stream, const toed_tuning* force = nullptr)
+                              cudaStream_t stream, const toed_tuning* force = nullptr, bool plain_loads = false)
 {
     const int r = radius_of(prm);
     toed_status st = TOED_OK;
     for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
-        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force);
+        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force, plain_loads);
     return st;
 }
 
@@ -625,19 +632,6 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
             return fail(TOED_ERR_CUDA);                                                   \
         }                                                                                 \
     } while (0)
-    if ((st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
-    if ((st = grow(&c->hb_out, &c->hb_out_cap, std::max(out_b, 1LL), stream)) != TOED_OK) return fail(st);
-    if ((st = grow(&c->hb_idx, &c->hb_idx_cap, std::max(idx_n, 1LL), stream)) != TOED_OK) return fail(st);
-    if ((st = grow(&c->hb_cnt, &c->hb_cnt_cap, (long long)n + chunks, stream)) != TOED_OK) return fail(st);
-    if (c->hb_cnt_host_cap < (long long)n + chunks) {
-        if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
-        c->hb_cnt_host = nullptr;
-        c->hb_cnt_host_cap = 0;
-        TOED_HB(cudaMallocHost((void**)&c->hb_cnt_host, sizeof(int) * (size_t)(n + chunks)));
-        c->hb_cnt_host_cap = n + chunks;
-    }
-    if (!c->s_in) TOED_HB(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));
-    if (!c->s_out) TOED_HB(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
     // Page-locked host outputs are written by the ordering pass itself
     // (mapped into the device's address space; coherent over the C2C link):
     // no count read-back and no list copies.  Otherwise lists go through
@@ -650,6 +644,29 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         }
         return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
     };
+    // Page-locked inputs are read in place by the detection kernel through
+    // their device mapping (zero copy over the C2C link, plain row loads):
+    // no staging copies, and the batch goes as one launch per 64 images.
+    bool zin = true;
+    std::vector<const void*> in_map(n, nullptr);
+    for (int i = 0; i < n && zin; ++i) {
+        in_map[i] = mapped(const_cast<void*>(images[i].pixels));
+        zin = in_map[i] != nullptr;
+    }
+    if (zin) chunks = 1;
+    if (!zin && (st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
+    if ((st = grow(&c->hb_out, &c->hb_out_cap, std::max(out_b, 1LL), stream)) != TOED_OK) return fail(st);
+    if ((st = grow(&c->hb_idx, &c->hb_idx_cap, std::max(idx_n, 1LL), stream)) != TOED_OK) return fail(st);
+    if ((st = grow(&c->hb_cnt, &c->hb_cnt_cap, (long long)n + chunks, stream)) != TOED_OK) return fail(st);
+    if (c->hb_cnt_host_cap < (long long)n + chunks) {
+        if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
+        c->hb_cnt_host = nullptr;
+        c->hb_cnt_host_cap = 0;
+        TOED_HB(cudaMallocHost((void**)&c->hb_cnt_host, sizeof(int) * (size_t)(n + chunks)));
+        c->hb_cnt_host_cap = n + chunks;
+    }
+    if (!c->s_in) TOED_HB(cudaStreamCreateWithFlags(&c->s_in, cudaStreamNonBlocking));
+    if (!c->s_out) TOED_HB(cudaStreamCreateWithFlags(&c->s_out, cudaStreamNonBlocking));
     bool direct = true;
     for (int i = 0; i < n && direct; ++i) {
         void* e = mapped(images[i].edgels);
@@ -661,7 +678,8 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         dev[i].grid_index = static_cast<int*>(gi);
     }
     for (int i = 0; i < n; ++i) {
-        dev[i].pixels = c->hb_in + in_off[i];
+        dev[i].pixels = zin ? in_map[i] : c->hb_in + in_off[i];
+        if (zin) dev[i].pitch = images[i].pitch;
         if (!direct) {
             dev[i].edgels = c->hb_out + out_off[i];
             dev[i].count = c->hb_cnt + i;
@@ -694,7 +712,7 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     }
     // 1. every group's images to the device, in order (whole-image 1-D
     // copies where the rows are contiguous: those run on the copy engines)
-    for (int k = 0; k < chunks; ++k) {
+    for (int k = 0; k < chunks && !zin; ++k) {
         for (int i = first[k]; i < first[k + 1]; ++i) {
             const toed_host_image& h = images[i];
             const int esz = h.dtype == TOED_U8 ? 1 : 4;
@@ -710,8 +728,8 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     }
     // 2. detection of each group once its images are in
     for (int k = 0; k < chunks; ++k) {
-        TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
-        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream);
+        if (!zin) TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
+        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream, nullptr, zin);
         if (st != TOED_OK) return fail(st);
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n + k, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
         TOED_HB(cudaEventRecord(ev_det[k], stream));

@@ -52,7 +52,8 @@ struct DetImage {
     int nsc, nsr;        // strip columns / strip rows
     int unit_base;       // first work unit
     int tile_base;       // first ordering tile
-    int tma;             // 1: rows arrive by TMA through BatchParams::tmap[k]; 0: plain loads
+    int tma;             // 1: rows arrive by TMA through BatchParams::tmap[k]; 2: by per-thread async
+                         // copies (float32, any address); 0: plain loads
     int tma_align;       // element alignment of a TMA box's x coordinate (16 bytes)
     int tma_boxw;        // box width in elements (the halo row plus the alignment shift)
 };

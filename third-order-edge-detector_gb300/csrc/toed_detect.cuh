@@ -52,7 +52,8 @@ struct Cfg {
     static constexpr int MAXC = NMS_ROWS * 2 * kInner;
     static constexpr int RECW = 21;                 // words per deferred edgel record (odd: no bank conflicts)
     static constexpr int FW = 2 * kExt;             // 2x-grid columns held per row
-    static constexpr size_t sz_raw = kStepRows * kRawRowBytes;  // one TMA box of input rows
+    // one TMA box of input rows, or two boxes of float32 rows for the async copies
+    static constexpr size_t sz_raw = 2 * kStepRows * kRawRowBytes;
     static constexpr size_t off_raw = 0;
     static constexpr size_t off_mbar = off_raw + sz_raw;
     static constexpr size_t off_in = align_up(off_mbar + 16, 16);
@@ -131,9 +132,105 @@ __device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t phase)
     return false;
 }
 
+// Per-thread asynchronous 4-byte copy global -> shared; src_bytes 0 writes
+// zero (the reference's zero padding outside the image).
+__device__ __forceinline__ void cp_async4(uint32_t dst, const void* src, int src_bytes)
+{
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4, %2;" ::"r"(dst), "l"(src), "r"(src_bytes) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
 // Ring row of x for 0 <= x < 2 * N (every ring index the kernel forms).
 template <int N>
 __device__ __forceinline__ int ring_wrap(int x) { return x >= N ? x - N : x; }
+
+// Input rows by per-thread async copies (float32 rows at any address, e.g.
+// page-locked host memory read through its device mapping), two boxes of B
+// rows ahead in a double buffer.  A box is B rows x BW columns starting at
+// the 16-byte-aligned column xa <= xin; thread t owns 16-byte chunk t of
+// every box: one 16-byte copy where the image allows it (aligned base and
+// rows, chunk inside the image), else four 4-byte copies with zero fill
+// outside the image.  Each thread converts the chunk it copied itself, so it
+// waits for its own copies only (cp.async.wait_group 1: the newest box may
+// still be in flight).  Boxes 0 .. Q0-1 are the first step's window, box
+// Q0 - 1 + s the new rows of step s >= 1.  Only the ASYNC instantiation of
+// the kernel carries this path.
+template <int R>
+struct AsyncBox {
+    using C = Cfg<R>;
+    static constexpr int B = C::B;
+    static constexpr int BW = (C::NIN + 3 + 3) / 4 * 4;          // box width (floats): NIN + the alignment shift
+    static constexpr int CH = BW / 4;                           // 16-byte chunks per row
+    static constexpr int Q0 = (C::HS + B - 1) / B;              // boxes of the first step
+    static_assert(B * CH <= kThreads, "one chunk per thread");
+    static_assert(2 * B * BW * 4 <= C::sz_raw, "two boxes fit the staging buffer");
+};
+
+template <int R>
+__device__ __forceinline__ void async_issue_box(float* rawf, const float* fsrc, long long pitch, int H, int W, int xa,
+                                                int ys, int nsteps, int q, bool al16)
+{
+    using A = AsyncBox<R>;
+    constexpr int B = A::B;
+    const int t = threadIdx.x;
+    const int last = A::Q0 + nsteps - 2;  // the last box of the unit
+    if (q <= last && t < B * A::CH) {
+        const int rr = t / A::CH, k = t - rr * A::CH;
+        const int row0 = (q < A::Q0) ? ys - R - 3 + q * B : ys + (q - A::Q0 + 1) * B + R;
+        const int y = row0 + rr, x = xa + 4 * k;
+        float* dst = rawf + (q & 1) * (B * A::BW) + rr * A::BW + 4 * k;
+        const bool rowin = (unsigned)y < (unsigned)H;
+        if (al16 && rowin && x >= 0 && x + 4 <= W) {
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(fsrc + (long long)y * pitch + x)
+                         : "memory");
+        } else {
+#pragma unroll
+            for (int e = 0; e < 4; ++e) {
+                const bool in = rowin && (unsigned)(x + e) < (unsigned)W;
+                cp_async4(smem_addr(dst + e), in ? fsrc + (long long)y * pitch + x + e : fsrc, in ? 4 : 0);
+            }
+        }
+    }
+    cp_async_commit();  // one group per box, empty past the last box, so that wait_group counts boxes
+}
+
+template <int R>
+__device__ __forceinline__ void stage_rows_async(float* __restrict__ sIn, unsigned char* sRaw, const float* fsrc,
+                                                 long long pitch, int H, int W, int xin, int ys, int s, int nsteps,
+                                                 int rb)
+{
+    using C = Cfg<R>;
+    using A = AsyncBox<R>;
+    constexpr int B = C::B;
+    const int t = threadIdx.x;
+    float* rawf = reinterpret_cast<float*>(sRaw);
+    const int xa = xin - (((xin % 4) + 4) % 4), shift = xin - xa;
+    const bool al16 = ((reinterpret_cast<uintptr_t>(fsrc) & 15u) == 0) && ((pitch & 3) == 0);
+    if (s == 0) {
+        async_issue_box<R>(rawf, fsrc, pitch, H, W, xa, ys, nsteps, 0, al16);
+        async_issue_box<R>(rawf, fsrc, pitch, H, W, xa, ys, nsteps, 1, al16);
+    }
+    const int q0 = (s == 0) ? 0 : A::Q0 - 1 + s, q1 = (s == 0) ? A::Q0 : q0 + 1;
+    for (int q = q0; q < q1; ++q) {
+        asm volatile("cp.async.wait_group 1;" ::: "memory");
+        const int nrows = (s == 0) ? min(B, C::HS - q * B) : B;
+        const int a0 = (s == 0) ? q * B : rb + 2 * R + 3;  // ring row of the box's row 0 (before wrapping)
+        if (t < B * A::CH) {
+            const int rr = t / A::CH, k = t - rr * A::CH;
+            const float* src = rawf + (q & 1) * (B * A::BW) + rr * A::BW + 4 * k;
+            if (rr < nrows) {
+                float* dst = sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN;
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int cc = 4 * k + e - shift;  // ring column
+                    if (cc >= 0 && cc < C::NIN) dst[cc] = src[e];
+                }
+            }
+        }
+        async_issue_box<R>(rawf, fsrc, pitch, H, W, xa, ys, nsteps, q + 2, al16);
+    }
+}
 
 // ---------------------------------------------------------------------------
 // Row pass: for ring rows p0, p0+1, ... (mod RING; nrows of them) of the
@@ -359,7 +456,9 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
     }
 }
 
-template <int R, bool HYB>
+// ASYNC: input rows by per-thread async copies (images with tma == 2) or
+// plain loads; otherwise by TMA (tma == 1) or plain loads.
+template <int R, bool HYB, bool ASYNC>
 __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(const __grid_constant__ BatchParams p)
 {
     using C = Cfg<R>;
@@ -420,7 +519,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         const long long seg0 = im.seg_base;
         const int xin = x0 - R - 2;  // image column of sIn column 0
         int x_al = xin, shift = 0;
-        if (im.tma) {
+        if (!ASYNC && im.tma == 1) {
             const int al = im.tma_align;
             x_al = (xin >= 0) ? (xin / al) * al : -(((-xin) + al - 1) / al) * al;  // floor to the alignment
             shift = xin - x_al;
@@ -437,7 +536,10 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             // logical slot h <-> ring row (rb + h) mod RING <-> ext row
             // s*B - R - 2 + h <-> image row ys - 1 + ext row
             // ---- 1. input rows -> input ring (FP32, zero padded) -----------
-            if (im.tma) {
+            if (ASYNC && im.tma == 2) {
+                stage_rows_async<R>(sIn, sRaw, static_cast<const float*>(src), pitch, H, W, xin, ys, s, nsteps, rb);
+                __syncthreads();  // every thread's rows are in before the row pass
+            } else if (!ASYNC && im.tma == 1) {
                 // rows arrive by TMA (out-of-image texels read as zero, the
                 // reference's zero padding); step s+1's box is requested as
                 // soon as step s has consumed the staging buffer
@@ -703,7 +805,5 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
     for (int r = tid; r < nrec; r += kThreads) finish_edgel<HYB>(sRec + r * C::RECW, p.sc);
 }
 
-template <int R, bool HYB>
-void launch_detect(const BatchParams& p, int grid, cudaStream_t stream);
 
 }  // namespace toed

@@ -6,12 +6,16 @@
 
 #define TOED_DETECT_INSTANCE(R)                                                    \
     namespace toed {                                                               \
-    DetectEntry detect_entry_r##R(bool hyb)                                        \
+    DetectEntry detect_entry_r##R(bool hyb, bool async)                            \
     {                                                                              \
         DetectEntry e;                                                             \
         e.smem = Cfg<R>::smem;                                                     \
-        e.func = hyb ? (const void*)toed_detect_kernel<R, true>                    \
-                     : (const void*)toed_detect_kernel<R, false>;                  \
+        if (async)                                                                 \
+            e.func = hyb ? (const void*)toed_detect_kernel<R, true, true>          \
+                         : (const void*)toed_detect_kernel<R, false, true>;        \
+        else                                                                       \
+            e.func = hyb ? (const void*)toed_detect_kernel<R, true, false>         \
+                         : (const void*)toed_detect_kernel<R, false, false>;       \
         return e;                                                                  \
     }                                                                              \
     }

@@ -14,8 +14,9 @@ struct DetectEntry {
     size_t smem;
 };
 
-// Per-radius instantiations (toed_detect_r<R>.cu); hyb selects the FP64 epilogue.
-DetectEntry detect_entry(int radius, bool hyb);
+// Per-radius instantiations (toed_detect_r<R>.cu); hyb selects the FP64
+// epilogue, async the variant that stages rows by per-thread async copies.
+DetectEntry detect_entry(int radius, bool hyb, bool async = false);
 
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
 // The ordering pass's last kernel in the TOED_ORI_QAD orientation mode (toed_qad.cu).
