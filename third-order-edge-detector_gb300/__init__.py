@@ -416,7 +416,7 @@ class Detector:
                                          gi.data_ptr() if gi.numel() else None,
                                          go.data_ptr() if go.numel() else None, gp.data_ptr()))
         arr = (toed_grad_image * len(items))(*items)
-        gs = t.zeros(1, dtype=t.float64, device=dev)
+        gs = t.empty(1, dtype=t.float64, device=dev)  # cleared by toed_backward_batch
         p = make_params(sigma, radius, 2.0, 10, out_dtype)
         s = stream if stream is not None else t.cuda.current_stream(self.device)
         _check(lib().toed_backward_batch(self._ctx, arr, len(items), ctypes.byref(p), ctypes.c_void_p(gs.data_ptr()),

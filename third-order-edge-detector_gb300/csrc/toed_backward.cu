@@ -13,7 +13,8 @@
 //      accumulates dL/dsigma;
 //   3. a warp per edgel adds the separable cotangent windows
 //      sum_f X_f(q) V_f(p) of its five points onto the pixel gradient with
-//      vector float reductions in global memory (the host clears it first).
+//      vector float reductions in global memory (cleared first by bw_clear,
+//      one launch for the whole batch).
 // Reductions from different edgels land in an unspecified order, so the
 // pixel gradient is reproducible to float rounding, not bit for bit.
 #include <cmath>
@@ -457,6 +458,23 @@ static cudaError_t launch_bw(const BwParams& p, cudaStream_t stream)
                             dim3(kBwAdjThreads), args, 0, stream);
 }
 
+// Clears dL/dI of image blockIdx.y (rows of width W, contiguous): 16-byte
+// stores from the first 16-byte boundary, scalar stores around them.
+__global__ void __launch_bounds__(256) bw_clear(const __grid_constant__ BwParams p)
+{
+    const BwImage& d = p.img[blockIdx.y];
+    float* g = d.gpix;
+    const long long npx = (long long)d.H * d.W;
+    const long long head = min(npx, (long long)(((16u - (reinterpret_cast<uintptr_t>(g) & 15u)) & 15u) / 4u));
+    const long long nv = (npx - head) / 4;
+    const long long t0 = (long long)blockIdx.x * blockDim.x + threadIdx.x, st = (long long)gridDim.x * blockDim.x;
+    float4* g4 = reinterpret_cast<float4*>(g + head);
+    for (long long i = t0; i < nv; i += st) g4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (t0 < head) g[t0] = 0.f;
+    const long long tail = head + 4 * nv;
+    if (t0 < npx - tail) g[tail + t0] = 0.f;
+}
+
 cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_params* prm, int r, double* gsig,
                             cudaStream_t stream)
 {
@@ -500,8 +518,10 @@ cudaError_t backward_launch(const toed_grad_image* items, int n, const toed_para
         edg += d.n;
     }
     p.n_edgels = edg;
-    for (int i = 0; i < n; ++i) {
-        const cudaError_t e = cudaMemsetAsync(p.img[i].gpix, 0, sizeof(float) * p.img[i].H * p.img[i].W, stream);
+    {
+        // dL/dI of every image cleared by one launch (the scatter adds into it)
+        void* args[] = {&p};
+        const cudaError_t e = cudaLaunchKernel((const void*)bw_clear, dim3(64, n), dim3(256), args, 0, stream);
         if (e != cudaSuccess) return e;
     }
     switch (r) {
