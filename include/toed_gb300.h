@@ -131,7 +131,8 @@ toed_status toed_device_flags(toed_ctx* ctx, cudaStream_t stream, int* flags);
 /* Adjoint of toed_detect with the selection frozen (no reference counterpart:
  * the reference has no gradients).  For every edgel the forward emitted
  * (identified by the grid_index it wrote), given dL/d[x, y, orientation,
- * strength], writes dL/dpixel for the whole image and accumulates dL/dsigma.
+ * strength], writes dL/dpixel for the whole image and dL/dsigma of the whole batch
+ * (*grad_sigma, a device double, is overwritten).
  * The NMS decisions (which 2x-grid points are edgels, and each one's sector)
  * are those of the forward and are not differentiated. */
 typedef struct toed_grad_image {
