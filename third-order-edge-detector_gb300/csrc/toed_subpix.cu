@@ -251,17 +251,24 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
                     const float ga = xmaj ? fabsf(g.x) : fabsf(g.y), gb = xmaj ? fabsf(g.y) : fabsf(g.x);
                     const float fpS = fmaf(Map, ga - gb, Mdp * gb), fmS = fmaf(Mam, ga - gb, Mdm * gb);
                     const float fS = f * ga;
-                    // |FP32 - exact| <= ~3e-7 (|f| + |Map| + |Mdp| + |Mam| + |Mdm|) ga; 30x margin
+                    // |FP32 - exact| <= ~3e-7 (|f| + |Map| + |Mdp| + |Mam| + |Mdm|) ga; 30x margin.
+                    // Neighbours equal to f (a plateau, e.g. a clipped ridge) tie
+                    // exactly in the FP64 form too: decided without it.
                     const float tol = 1e-5f * ga * (fabsf(f) + fabsf(Map) + fabsf(Mdp) + fabsf(Mam) + fabsf(Mdm));
-                    if (fabsf(fS - fpS) > tol && fabsf(fS - fmS) > tol) {
-                        cand = fS > fmS && fS > fpS;
-                    } else {
-                        const double gad = ga, gbd = gb, d = gad - gbd;
-                        const double fpD = fma((double)Map, d, (double)Mdp * gbd);
-                        const double fmD = fma((double)Mam, d, (double)Mdm * gbd);
-                        const double fD = (double)f * gad;
-                        cand = (fD > fmD && fD >= fpD) || (fD >= fmD && fD > fpD);
+                    int cp = (Map == f && Mdp == f) ? 0 : (fS - fpS > tol ? 1 : (fpS - fS > tol ? -1 : 2));
+                    int cm = (Mam == f && Mdm == f) ? 0 : (fS - fmS > tol ? 1 : (fmS - fS > tol ? -1 : 2));
+                    if (cp == 2 || cm == 2) {
+                        const double gad = ga, gbd = gb, d = gad - gbd, fD = (double)f * gad;
+                        if (cp == 2) {
+                            const double fpD = fma((double)Map, d, (double)Mdp * gbd);
+                            cp = fD > fpD ? 1 : (fD < fpD ? -1 : 0);
+                        }
+                        if (cm == 2) {
+                            const double fmD = fma((double)Mam, d, (double)Mdm * gbd);
+                            cm = fD > fmD ? 1 : (fD < fmD ? -1 : 0);
+                        }
                     }
+                    cand = (cm > 0 && cp >= 0) || (cm >= 0 && cp > 0);  // :466-468
                 } else {
                     const float md = sqrtf(g.x * g.x + g.y * g.y);
                     const float nx = g.x / md, ny = g.y / md;
@@ -385,13 +392,13 @@ __global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ Sub
         if ((okm >> lane) & 1u) {
             id = sRowOff[a] + __popc(okm & ltm);
             if (id < p.sc.staging_cap) {
+                // positions and strength packed as (pixel, FP32 offset) / FP32 bits:
+                // tc_correct, a thread per edgel, forms the doubles (no FP64
+                // instruction here, where every warp-row with an edgel would pay it)
                 const float3 r = sRes[sCandOff[a] + __popc(bal1[u] & ltm)];
-                if (p.hyb)
-                    p.sc.staging[id] = make_double4_32a((double)j + (double)r.x, (double)i + (double)r.y, 0.0,
-                                                        (double)r.z);
-                else
-                    p.sc.staging[id] = make_double4_32a((double)((float)j + r.x), (double)((float)i + r.y), 0.0,
-                                                        (double)r.z);
+                p.sc.staging[id] = make_double4_32a(__hiloint2double(j, __float_as_int(r.x)),
+                                                    __hiloint2double(i, __float_as_int(r.y)), 0.0,
+                                                    __hiloint2double(0, __float_as_int(r.z)));
                 p.sc.staging_idx[id] = i * w + j;
             } else {
                 id = -1;
@@ -595,7 +602,12 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
         const long long sidx = (long long)sSegOff[row] + (e - sOff[row]);
         if (sidx >= p.sc.staging_cap) continue;
         double4_32a rec = p.sc.staging[sidx];
-        const double sx = rec.x, sy = rec.y;
+        // unpack tc_orient_nms's (pixel, FP32 offset) positions and FP32 strength
+        const int cj = __double2hiint(rec.x), ci = __double2hiint(rec.y);
+        const float ox = __int_as_float(__double2loint(rec.x)), oy = __int_as_float(__double2loint(rec.y));
+        const double sx = p.hyb ? (double)cj + (double)ox : (double)((float)cj + ox);
+        const double sy = p.hyb ? (double)ci + (double)oy : (double)((float)ci + oy);
+        rec.w = (double)__int_as_float(__double2loint(rec.w));
         const int x0 = (int)floor(sx), y0 = (int)floor(sy);
         const double fx = sx - x0, fy = sy - y0;
         const float tfx = (float)fx, tfy = (float)fy;
@@ -666,8 +678,8 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
         }
         rec.z = (double)ori;
         // coord_scale (:657, :696-697): positions in original pixels
-        rec.x /= (double)M.scale;
-        rec.y /= (double)M.scale;
+        rec.x = sx / (double)M.scale;
+        rec.y = sy / (double)M.scale;
         p.sc.staging[sidx] = rec;
     }
 }
@@ -715,7 +727,7 @@ __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubPar
     }
     __syncthreads();
     const bool all = !(p.nbr > 0.0) || p.img_count[k] < 2;  // :567-568
-    const double r2 = p.nbr * p.nbr, inv = 1.0 / p.nbr;
+    const double r2 = p.nbr * p.nbr;
     // an edgel lies within sqrt(2) work pixels of its own; search the id map
     // (work grid) around it, compare in original pixels as the reference does
     const int reach = (int)ceil(p.nbr * M.scale + 1.5);
@@ -732,7 +744,6 @@ __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubPar
             continue;
         }
         const double4_32a me = p.sc.staging[r];
-        const long long cx = (long long)floor(me.x * inv), cy = (long long)floor(me.y * inv);
         const int pi = (int)floor(me.y * M.scale), pj = (int)floor(me.x * M.scale);
         bool found = false;
         for (int d = 0; d <= reach && !found; ++d) {
@@ -743,9 +754,10 @@ __global__ void __launch_bounds__(256) tc_isolate(const __grid_constant__ SubPar
                     if (jj < 0 || jj >= M.w) continue;
                     const int o = p.eid[M.px_base + (long long)ii * M.w + jj];
                     if (o < 0 || o == r) continue;
+                    // the reference looks only in the 3 x 3 cells of size radius
+                    // around the edgel's cell; every edgel within the radius
+                    // lies in one of them, so the distance test alone decides
                     const double4_32a ot = p.sc.staging[o];
-                    const long long ox = (long long)floor(ot.x * inv), oy = (long long)floor(ot.y * inv);
-                    if (ox < cx - 1 || ox > cx + 1 || oy < cy - 1 || oy > cy + 1) continue;  // 3x3 cells
                     const double ddx = me.x - ot.x, ddy = me.y - ot.y;
                     if (ddx * ddx + ddy * ddy <= r2) {
                         found = true;
