@@ -326,3 +326,27 @@ def test_host_batch_flat_images(toed, synth, pin):
             assert n == r["count"], k
             assert t.equal(o["edgels"][:n], r["edgels"].cpu()), k
             assert t.equal(o["index"][:n], r["index"].cpu()), k
+
+
+def test_host_batch_zero_copy_layouts(toed, synth):
+    """Page-locked images are read in place by the detection kernel (async
+    row staging): 16-byte copies where rows allow them, 4-byte copies for odd
+    widths, a host pitch wider than the image and uint8 rows (plain loads).
+    Every layout gives the device-buffer batch's lists bit for bit."""
+    t = _torch()
+    det = toed.Detector(0)
+    sizes = [(211, 301, np.float32), (97, 127, np.float32), (150, 333, np.uint8), (120, 200, np.float32)]
+    host = [t.as_tensor(synth.shapes_image(h, w, seed=1600 + k, dtype=dt).image)
+            for k, (h, w, dt) in enumerate(sizes)]
+    ref = det.detect_batch([im.contiguous().cuda() for im in host], sigma=1.5)
+    pinned = [im.pin_memory() for im in host]
+    wide = t.zeros((sizes[3][0], sizes[3][1] + 3), dtype=t.float32).pin_memory()
+    wide[:, :sizes[3][1]] = host[3]
+    pinned[3] = wide[:, :sizes[3][1]]  # pitch 203 floats: rows not 16-byte aligned
+    outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True, pin=True)
+    det.detect_host(pinned, outs, toed.make_params(1.5))
+    for k, (r, o) in enumerate(zip(ref, outs)):
+        n = int(o["count"].item())
+        assert n == r["count"] and n > 20, k
+        assert t.equal(o["edgels"][:n], r["edgels"].cpu()), k
+        assert t.equal(o["index"][:n], r["index"].cpu()), k

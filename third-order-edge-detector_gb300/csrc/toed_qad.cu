@@ -23,9 +23,9 @@
 //      per lane (interpolation is linear), contracts the window column with
 //      each point row's y taps (lane-local) and accumulates the nine
 //      interpolated derivatives;
-//   4. sums the nine values over the lanes (butterfly) and lane 0 forms the
-//      third-order vector (FP64 in HYBRID precision), the angle and the
-//      output record.
+//   4. sums the nine values over the lanes (butterfly) and parks them; after
+//      32 records lane e forms record e's third-order vector (FP64 in HYBRID
+//      precision, all lanes busy), the angle and the output record.
 #include "toed_common.cuh"
 #include "toed_internal.h"
 
