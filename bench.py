@@ -486,7 +486,9 @@ def run_ours(args, ws, rank, local):
 
     # ---- end to end through the public API with host buffers -----------
     # toed_detect_host_batch: page-locked host images in, host edgel lists
-    # out; the library pipelines H2D, detection and D2H over groups of images
+    # out; the detection kernel reads the page-locked images in place over the
+    # C2C link and the ordering pass writes the lists into host memory (with
+    # pageable buffers the library pipelines copies over E2E_CHUNKS groups)
     h_imgs = [torch.as_tensor(im).pin_memory() for im in images]
     h_outs = det.alloc_host_outputs([im.shape for im in images], None, toed.TOED_F32, index=False)
     for o, c in zip(h_outs, caps):
