@@ -350,3 +350,33 @@ def test_host_batch_zero_copy_layouts(toed, synth):
         assert n == r["count"] and n > 20, k
         assert t.equal(o["edgels"][:n], r["edgels"].cpu()), k
         assert t.equal(o["index"][:n], r["index"].cpu()), k
+
+
+@pytest.mark.parametrize("H,W", [(2, 65536), (65536, 2), (12, 20000), (20000, 12)])
+def test_extreme_aspect_ratios(detector, oracle, synth, H, W):
+    """Images one strip wide or a few rows high: strip and step boundaries
+    everywhere (at 2 pixels no edgel survives the 10-point border of the 2x
+    grid, as in the reference; at 12 pixels a 4-point band does)."""
+    rng = np.random.default_rng(H * 7 + W)
+    img = (128 + 60 * rng.standard_normal((H, W))).astype(np.float32)
+    ref = oracle.detect(img.astype(np.float64), 1.0)
+    n, e, i = _run(detector, img, 1.0)
+    # pure noise: every edgel is a noise edgel, whose third-order vector nearly
+    # cancels (as below the reference threshold in test_threshold_and_border)
+    m = _check(ref, e, i, exact_set=True, skip=_undecidable(img, 1.0), ori=1e-3)
+    assert m["ori_p99"] <= 1e-5, m
+    if min(H, W) >= 12:
+        assert m["n_ref"] > 100
+
+
+def test_large_image(detector, oracle, synth):
+    """A 6000 x 7000 float32 image (42 Mpixel, one launch of many strips;
+    a shapes image tiled 6 x 7 with fresh noise) against the FP64 oracle at
+    the parity tolerances."""
+    base = synth.shapes_image(1000, 1000, seed=4242, dtype=np.float32).image
+    rng = np.random.default_rng(4243)
+    img = (np.tile(base, (6, 7)) + rng.normal(0, 2, (6000, 7000))).astype(np.float32)
+    ref = oracle.detect(img.astype(np.float64), 1.5, nthreads=os.cpu_count())
+    n, e, i = _run(detector, img, 1.5, capacity=4_000_000)
+    m = _check(ref, e, i)
+    assert m["n_ref"] > 300_000
