@@ -434,12 +434,12 @@ def run_ours(args, ws, rank, local):
         o["capacity"] = c
     params = toed.make_params(SIGMA, 0, THRESH, 10, toed.TOED_F32, toed.TOED_HYBRID)
     det.reserve(npx, sum(caps), len(images))
-    # launch shape (strip height, TMA or plain row staging) picked by the
+    # launch shape (strip height, TMA / async-copy / plain row staging) picked by the
     # library's autotuner on this batch, before any timed work (or fixed by
     # --launch-shape, e.g. for a profiler run)
     if args.launch_shape:
         rows, stg = args.launch_shape.split(":")
-        det.set_tuning(params, int(rows), stg == "tma")
+        det.set_tuning(params, int(rows), stg)
         tuned = {"strip_rows": int(rows), "staging": stg}
     else:
         tuned = det.autotune(d_imgs, outs, params, reps=3)
@@ -586,7 +586,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-side", action="store_true", help="skip the other configurations' measurements")
-    ap.add_argument("--launch-shape", default="", help="ROWS:tma|plain instead of autotuning, e.g. 254:tma")
+    ap.add_argument("--launch-shape", default="", help="ROWS:tma|async|plain instead of autotuning, e.g. 254:tma")
     ap.add_argument("--workload", default="batch", choices=["batch", "fwd_bwd", "subpix", "qad"],
                     help="batch: the headline line; fwd_bwd / subpix / qad: that secondary workload alone")
     args = ap.parse_args()

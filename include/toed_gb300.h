@@ -242,20 +242,22 @@ toed_status toed_write_edgels_txt(const char* path, const void* edgels, int dtyp
 
 /* Launch-shape autotuning (no counterpart in the reference, whose GPU path
  * has one fixed launch shape).  toed_autotune times each candidate -- strip
- * height 14, 30, 62, 126, 254, 510 or 1022 rows, input rows staged by TMA or
- * by plain loads -- on the caller's batch with CUDA events, `reps` timed runs
+ * height 14, 30, 62, 126, 254, 510 or 1022 rows, input rows staged by TMA, by
+ * per-thread async copies or by plain loads -- on the caller's batch with CUDA
+ * events, `reps` timed runs
  * after one untimed run each, keeps the fastest in the context for this
  * radius, precision and launch size class -- floor(log2(pixels)) of each
  * launch of the batch (64 images at most per launch) -- and returns it; later
  * launches of the same class use it, launches of other classes keep the
  * built-in heuristic.
- * It is synchronous, runs the detection 14 * (reps + 1) times (the outputs hold
+ * It is synchronous, runs the detection 21 * (reps + 1) times (the outputs hold
  * the last run; every candidate gives the same result bit for bit) and is
  * refused under stream capture.  toed_set_tuning installs a shape for every
  * size class (NULL restores the built-in heuristic). */
 typedef struct toed_tuning {
     int strip_rows;  /* 16k - 2 for k in 1, 2, 4, ..., 64 */
-    int staging;     /* 1: TMA (when the image allows it), 0: plain loads */
+    int staging;     /* input row staging: 1 TMA (when the image allows it), 2 per-thread async
+                        copies two steps ahead (float32 images), 0 plain loads */
     float ms;        /* measured time of one detection of the batch (autotune output) */
 } toed_tuning;
 

@@ -253,7 +253,7 @@ def test_autotune_and_launch_shapes_agree(toed, synth):
     prm = toed.make_params(1.5)
     ref = None
     for rows in (14, 30, 62, 126, 254, 510, 1022):
-        for staging in (True, False):
+        for staging in ("tma", "async", "plain"):
             det.set_tuning(prm, rows, staging)
             outs = det.alloc_outputs([im.shape for im in imgs])
             det.detect_into(imgs, outs, prm)
@@ -268,6 +268,7 @@ def test_autotune_and_launch_shapes_agree(toed, synth):
     outs = det.alloc_outputs([im.shape for im in imgs])
     best = det.autotune(imgs, outs, prm, reps=2)
     assert best["strip_rows"] in (14, 30, 62, 126, 254, 510, 1022) and best["ms"] > 0
+    assert best["staging"] in ("tma", "async", "plain")
     t.cuda.synchronize()
     for (n0, e0, i0), o in zip(ref, outs):
         assert int(o["count"].item()) == n0 and t.equal(o["edgels"][:n0].cpu(), e0)

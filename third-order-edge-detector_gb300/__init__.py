@@ -98,6 +98,9 @@ class toed_host_image(ctypes.Structure):
     ]
 
 
+_STAGING_NAMES = ["plain", "tma", "async"]  # toed_tuning.staging 0, 1, 2
+
+
 class toed_tuning(ctypes.Structure):
     _fields_ = [("strip_rows", ctypes.c_int), ("staging", ctypes.c_int), ("ms", ctypes.c_float)]
 
@@ -305,11 +308,14 @@ class Detector:
         best = toed_tuning()
         _check(lib().toed_autotune(self._ctx, arr, n, ctypes.byref(params), int(reps),
                                    ctypes.c_void_p(s.cuda_stream), ctypes.byref(best)), "toed_autotune")
-        return {"strip_rows": best.strip_rows, "staging": "tma" if best.staging else "plain", "ms": best.ms}
+        return {"strip_rows": best.strip_rows, "staging": _STAGING_NAMES[best.staging], "ms": best.ms}
 
-    def set_tuning(self, params: toed_params, strip_rows=None, staging: bool = True):
-        """Install a launch shape (strip_rows None: the built-in heuristic)."""
-        t = toed_tuning(int(strip_rows), 1 if staging else 0, 0.0) if strip_rows is not None else None
+    def set_tuning(self, params: toed_params, strip_rows=None, staging="tma"):
+        """Install a launch shape (strip_rows None: the built-in heuristic);
+        staging: "tma", "async" or "plain" (True / False mean "tma" / "plain")."""
+        if isinstance(staging, bool):
+            staging = "tma" if staging else "plain"
+        t = toed_tuning(int(strip_rows), _STAGING_NAMES.index(staging), 0.0) if strip_rows is not None else None
         _check(lib().toed_set_tuning(self._ctx, ctypes.byref(params), ctypes.byref(t) if t is not None else None),
                "toed_set_tuning")
 

@@ -361,9 +361,13 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
                                 bool plain_loads = false)
 {
     const bool hyb = prm->precision != TOED_FP32;
-    DetectEntry ent = detect_entry(r, hyb, plain_loads);
+    const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0][size_class(images, n)];
+    const toed_tuning* use = force ? force : (tuned.strip_rows > 0 ? &tuned : nullptr);
+    // async row staging: images read in place from host memory, or the tuned shape asks for it
+    const bool async_rows = plain_loads || (use && use->staging == 2);
+    DetectEntry ent = detect_entry(r, hyb, async_rows);
     if (!ent.func) return TOED_ERR_UNSUPPORTED;
-    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0][plain_loads ? 1 : 0];
+    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0][async_rows ? 1 : 0];
     if (bps == 0) {
         TOED_CU(cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem));
         TOED_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ent.func, kThreads, ent.smem));
@@ -376,8 +380,6 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     make_taps((double)prm->sigma, r, &p->taps);
     p->thr = prm->threshold;
     p->border = prm->border;
-    const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0][size_class(images, n)];
-    const toed_tuning* use = force ? force : (tuned.strip_rows > 0 ? &tuned : nullptr);
     p->S = use ? use->strip_rows : plan_strip_rows(images, n, resident);
     p->n_img = n;
     p->out_f64 = (prm->out_dtype == TOED_F64) ? 1 : 0;
@@ -403,7 +405,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
         encode_rows_map(&p->tmap[i], d, r);
-        if (plain_loads)
+        if (async_rows)
             d.tma = (d.dtype == TOED_F32) ? 2 : 0;  // async row copies (float32) or plain loads, never TMA
         else if (use && !use->staging)
             d.tma = 0;
@@ -519,7 +521,7 @@ extern "C" toed_status toed_autotune(toed_ctx* c, const toed_image* images, int 
             st = TOED_ERR_CUDA;
         }
         static const int steps[] = {1, 2, 4, 8, 16, 32, 64};
-        for (int staging = 1; staging >= 0 && st == TOED_OK; --staging)
+        for (int staging = 2; staging >= 0 && st == TOED_OK; --staging)
             for (int k = 0; k < 7 && st == TOED_OK; ++k) {
                 toed_tuning cand = {steps[k] * kStepRows - 2, staging, 0.f};
                 st = detect_all(c, images, n, prm, stream, &cand);  // untimed: scratch, caches
@@ -558,7 +560,7 @@ extern "C" toed_status toed_set_tuning(toed_ctx* c, const toed_params* prm, cons
     toed_tuning v = {};
     if (t) {
         if (t->strip_rows < kStepRows - 2 || (t->strip_rows + 2) % kStepRows != 0 || t->strip_rows > 64 * kStepRows - 2 ||
-            (t->staging != 0 && t->staging != 1))
+            (t->staging < 0 || t->staging > 2))
             return TOED_ERR_INVALID_ARG;
         v = *t;
     }
