@@ -11,6 +11,13 @@
 //     public edge_pt_list_idx, num_of_edge_data, time_conv, time_nms, start, stop
 //   void gpu_convolve(...) float / double                       gpu_kernels.hpp:24-45
 //   void gpu_nms(...)      float / double                       gpu_kernels.hpp:48-63
+//   template<typename T> class SubpixelTOCorrectionGPU, the GPU twin of
+//     SubpixelTOCorrectionCPU<T>          subpix_TO_correction/subpix_to_correction.hpp:20-96
+//     ctor (H, W, threshold, g_sigma, cpu_nthreads, n = 0), set_edgemap,
+//     set_orientation, estimate_orientation, int run(T* edginfo_out),
+//     set_output_dir, set_neighbor_radius, write_array_to_file; public
+//     subpix_edge_pts_final, TO_edgemap, TO_orientation, edge_pt_list_idx,
+//     num_of_edge_data, time_nms, time_conv, time_correct
 //
 // Differences a caller can see: convolve_img() runs the whole fused
 // detection (convolution, NMS and ordering) and time_conv is its device time;
@@ -19,6 +26,7 @@
 // execution continues, as the reference's cudacheck does (gpu_kernels.hpp:10-17).
 #pragma once
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -269,3 +277,184 @@ inline void gpu_nms(int device_id, int interp_h, int interp_w, double* dev_Ix, d
                                       dev_subpix_pos_x_map, dev_subpix_pos_y_map, 0),
                       "gpu_nms");
 }
+
+// The subpixel third-order correction of a dense edge map, with the
+// reference's SubpixelTOCorrectionCPU<T> interface, forwarding to
+// toed_subpix_to_correct_batch.  Differences a caller can see: the orientation
+// is estimated on the device inside run() when estimate_orientation() was
+// called (or taken from set_orientation(), zeros until then, as the
+// reference's theta buffer starts); cpu_nthreads is not used; time_conv holds
+// the device time of the whole correction (NMS, convolutions and correction
+// run as one pipeline), time_correct the copies of the results to the host,
+// time_nms 0 (seconds, as the reference's omp_get_wtime differences).
+template <typename T>
+class SubpixelTOCorrectionGPU {
+    int img_height, img_width, interp_n, work_height, work_width;
+    T thresh, sigma, neighbor_radius;
+    std::string output_dir;
+    toed_ctx* ctx = nullptr;
+    T* dev_E = nullptr;
+    T* dev_theta = nullptr;
+    bool estimate = false;
+    T* dev_edges = nullptr;
+    int* dev_count = nullptr;
+    T* dev_TO_E = nullptr;
+    T* dev_TO_O = nullptr;
+    int capacity = 0;
+    std::vector<T> edges_h, TO_E_h, TO_O_h;
+    cudaEvent_t start, stop;
+
+  public:
+    T* subpix_edge_pts_final;
+    T* TO_edgemap;
+    T* TO_orientation;
+    int edge_pt_list_idx;
+    int num_of_edge_data;
+    double time_nms, time_conv, time_correct;
+
+    SubpixelTOCorrectionGPU(int H, int W, T threshold, T g_sigma, int cpu_nthreads, int n = 0)
+        : img_height(H), img_width(W), interp_n(n < 0 ? 0 : n), thresh(threshold), sigma(g_sigma)
+    {
+        (void)cpu_nthreads;
+        neighbor_radius = T(2);
+        output_dir = "./output_files";
+        num_of_edge_data = 4;
+        edge_pt_list_idx = 0;
+        time_nms = time_conv = time_correct = 0;
+        const int scale = 1 << interp_n;
+        work_height = (img_height - 1) * scale + 1;
+        work_width = (img_width - 1) * scale + 1;
+        capacity = work_height * work_width;  // the reference's subpix_edge_pts_final holds one edgel per work pixel
+        const size_t px = (size_t)H * W;
+        edges_h.assign((size_t)capacity * 4, T(0));
+        TO_E_h.assign(px, T(0));
+        TO_O_h.assign(px, T(0));
+        subpix_edge_pts_final = edges_h.data();
+        TO_edgemap = TO_E_h.data();
+        TO_orientation = TO_O_h.data();
+        int device = 0;
+        toed_shim::report_cuda(cudaGetDevice(&device), "cudaGetDevice");
+        toed_shim::report(toed_create(&ctx, device), "toed_create");
+        toed_shim::report_cuda(cudaMalloc((void**)&dev_E, sizeof(T) * px), "cudaMalloc");
+        toed_shim::report_cuda(cudaMalloc((void**)&dev_theta, sizeof(T) * px), "cudaMalloc");
+        toed_shim::report_cuda(cudaMemset(dev_E, 0, sizeof(T) * px), "cudaMemset");
+        toed_shim::report_cuda(cudaMemset(dev_theta, 0, sizeof(T) * px), "cudaMemset");
+        toed_shim::report_cuda(cudaMalloc((void**)&dev_edges, sizeof(T) * 4 * (size_t)capacity), "cudaMalloc");
+        toed_shim::report_cuda(cudaMalloc((void**)&dev_count, sizeof(int)), "cudaMalloc");
+        toed_shim::report_cuda(cudaMalloc((void**)&dev_TO_E, sizeof(T) * px), "cudaMalloc");
+        toed_shim::report_cuda(cudaMalloc((void**)&dev_TO_O, sizeof(T) * px), "cudaMalloc");
+        toed_shim::report_cuda(cudaEventCreate(&start), "cudaEventCreate");
+        toed_shim::report_cuda(cudaEventCreate(&stop), "cudaEventCreate");
+    }
+    ~SubpixelTOCorrectionGPU()
+    {
+        cudaFree(dev_E);
+        cudaFree(dev_theta);
+        cudaFree(dev_edges);
+        cudaFree(dev_count);
+        cudaFree(dev_TO_E);
+        cudaFree(dev_TO_O);
+        cudaEventDestroy(start);
+        cudaEventDestroy(stop);
+        if (ctx) toed_destroy(ctx);
+    }
+    SubpixelTOCorrectionGPU(const SubpixelTOCorrectionGPU&) = delete;
+    SubpixelTOCorrectionGPU& operator=(const SubpixelTOCorrectionGPU&) = delete;
+
+    void set_edgemap(const T* data)
+    {
+        toed_shim::report_cuda(cudaMemcpy(dev_E, data, sizeof(T) * (size_t)img_height * img_width,
+                                          cudaMemcpyHostToDevice),
+                               "cudaMemcpy");
+    }
+    void set_orientation(const T* data)
+    {
+        toed_shim::report_cuda(cudaMemcpy(dev_theta, data, sizeof(T) * (size_t)img_height * img_width,
+                                          cudaMemcpyHostToDevice),
+                               "cudaMemcpy");
+        estimate = false;
+    }
+    // subpix_to_correction.cpp:307-375, run on the device inside run()
+    void estimate_orientation() { estimate = true; }
+
+    // subpix_to_correction.cpp:623-736: NMS along the orientation, the eight
+    // Gaussian-derivative convolutions, the per-edgel correction, isolated
+    // edgels removed, dense TO_edgemap / TO_orientation; returns the count
+    int run(T* edginfo_out)
+    {
+        toed_edgemap m;
+        m.E = dev_E;
+        m.theta = estimate ? nullptr : dev_theta;
+        m.height = img_height;
+        m.width = img_width;
+        m.pitch = img_width;
+        m.dtype = sizeof(T) == 8 ? TOED_F64 : TOED_F32;
+        m.edgels = dev_edges;
+        m.capacity = capacity;
+        m.count = dev_count;
+        m.TO_E = dev_TO_E;
+        m.TO_O = dev_TO_O;
+        toed_subpix_params p;
+        p.thresh = (float)thresh;
+        p.sigma = (float)sigma;
+        p.nbr_radius = (float)neighbor_radius;
+        p.out_dtype = sizeof(T) == 8 ? TOED_F64 : TOED_F32;
+        p.precision = TOED_HYBRID;
+        p.interp_n = interp_n;
+        float ms = 0.f;
+        toed_shim::report_cuda(cudaEventRecord(start), "cudaEventRecord");
+        toed_shim::report(toed_subpix_to_correct_batch(ctx, &m, 1, &p, 0), "toed_subpix_to_correct_batch");
+        toed_shim::report_cuda(cudaEventRecord(stop), "cudaEventRecord");
+        toed_shim::report_cuda(cudaEventSynchronize(stop), "cudaEventSynchronize");
+        toed_shim::report_cuda(cudaEventElapsedTime(&ms, start, stop), "cudaEventElapsedTime");
+        time_conv = ms * 1e-3;
+        time_nms = 0;
+        std::cout << "- Time of TO correction (GPU): " << ms << " (ms)" << std::endl;
+        toed_shim::report_cuda(cudaEventRecord(start), "cudaEventRecord");
+        int n = 0;
+        toed_shim::report_cuda(cudaMemcpy(&n, dev_count, sizeof(int), cudaMemcpyDeviceToHost), "cudaMemcpy");
+        const int k = n < capacity ? n : capacity;
+        std::fill(edges_h.begin(), edges_h.end(), T(0));
+        if (k > 0)
+            toed_shim::report_cuda(cudaMemcpy(edges_h.data(), dev_edges, sizeof(T) * 4 * (size_t)k,
+                                              cudaMemcpyDeviceToHost),
+                                   "cudaMemcpy");
+        const size_t px = (size_t)img_height * img_width;
+        toed_shim::report_cuda(cudaMemcpy(TO_E_h.data(), dev_TO_E, sizeof(T) * px, cudaMemcpyDeviceToHost),
+                               "cudaMemcpy");
+        toed_shim::report_cuda(cudaMemcpy(TO_O_h.data(), dev_TO_O, sizeof(T) * px, cudaMemcpyDeviceToHost),
+                               "cudaMemcpy");
+        toed_shim::report_cuda(cudaEventRecord(stop), "cudaEventRecord");
+        toed_shim::report_cuda(cudaEventSynchronize(stop), "cudaEventSynchronize");
+        toed_shim::report_cuda(cudaEventElapsedTime(&ms, start, stop), "cudaEventElapsedTime");
+        time_correct = ms * 1e-3;
+        edge_pt_list_idx = k;
+        if (edginfo_out && k > 0) std::memcpy(edginfo_out, edges_h.data(), sizeof(T) * 4 * (size_t)k);
+        return k;
+    }
+
+    void set_output_dir(const std::string& dir) { output_dir = dir.empty() ? "./output_files" : dir; }
+    void set_neighbor_radius(T radius) { neighbor_radius = radius; }
+
+    // subpix_to_correction.cpp:750-776 (default stream precision, tab separated)
+    void write_array_to_file(std::string filename, T* wr_data, int first_dim, int second_dim)
+    {
+        std::cout << "writing data to a file " << filename << " ..." << std::endl;
+        if (wr_data == nullptr || first_dim <= 0 || second_dim <= 0) {
+            std::cout << "write data file skipped: invalid buffer or dimensions." << std::endl;
+            return;
+        }
+        std::string out_file_name = output_dir;
+        if (!out_file_name.empty() && out_file_name.back() != '/') out_file_name.push_back('/');
+        out_file_name.append(filename);
+        std::ofstream out_file(out_file_name);
+        if (!out_file.is_open()) {
+            std::cout << "write data file cannot be opened!" << std::endl;
+            return;
+        }
+        for (int i = 0; i < first_dim; i++) {
+            for (int j = 0; j < second_dim; j++) out_file << wr_data[(size_t)i * second_dim + j] << "\t";
+            out_file << "\n";
+        }
+    }
+};

@@ -41,3 +41,41 @@ def test_cpp_shim_matches_oracle(toed, oracle, synth, tmp_path):
     want = ref["posmaps"][0]
     assert np.array_equal(px != 0, want != 0)
     assert np.abs(px - want).max() < 1e-9
+
+
+def test_cpp_subpix_shim_matches_oracle(toed, oracle, synth, tmp_path):
+    """SubpixelTOCorrectionGPU<T> used as the reference's driver uses
+    SubpixelTOCorrectionCPU<T> (main_subpix_to_correction.cpp:279-293):
+    estimated orientation (double), a given orientation (float), edgels and
+    the dense TO maps against the FP64 oracle."""
+    import sys
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_gpu_subpix import _check
+    toed.build()
+    exe = tmp_path / "subpix_driver"
+    cuda = "/usr/local/cuda"
+    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
+           os.path.join(ROOT, "tests", "cpp", "subpix_driver.cpp"), "-o", str(exe),
+           toed.LIB_PATH, "-L" + cuda + "/lib64", "-lcudart", "-Wl,-rpath," + os.path.dirname(toed.LIB_PATH),
+           "-Wl,-rpath," + cuda + "/lib64"]
+    subprocess.run(cmd, check=True)
+    H, W = 160, 192
+    E = synth.ridge_map(H, W, seed=77, n_curves=6).astype(np.float64)
+    rng = np.random.default_rng(78)
+    theta = rng.uniform(-np.pi, np.pi, (H, W))
+    (tmp_path / "E.raw").write_bytes(E.tobytes())
+    (tmp_path / "theta.raw").write_bytes(theta.tobytes())
+    r = subprocess.run([str(exe), str(tmp_path / "E.raw"), str(H), str(W), str(tmp_path), str(tmp_path / "theta.raw")],
+                       capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0, (r.returncode, r.stderr)
+    ref = oracle.subpix_to_correct(E, 0.1, 2.0, 2.0, dense=True)
+    got = np.fromfile(tmp_path / "sp_edges.bin", dtype=np.float64).reshape(-1, 4)
+    assert len(ref["edges"]) > 50
+    _check(ref["edges"], got)
+    te = np.fromfile(tmp_path / "sp_TO_E.bin", dtype=np.float64).reshape(H, W)
+    assert np.array_equal(te != 0, ref["TO_E"] != 0)
+    assert (tmp_path / "subpix_edges.txt").exists()
+    ref2 = oracle.subpix_to_correct(E, 0.1, 2.0, 2.0, theta=theta)
+    got2 = np.fromfile(tmp_path / "sp_edges_f32.bin", dtype=np.float32).reshape(-1, 4).astype(np.float64)
+    # the float class reads the map rounded to float32: near-tie NMS decisions may differ
+    _check(ref2["edges"], got2, agree=0.99, pos=2e-3, ori=2e-3, mag=1e-4)
