@@ -80,7 +80,34 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
         os.replace(tmp, LIB)
+    build_driver(verbose)
     return LIB
+
+
+DRIVER_SRC = os.path.join(HERE, "driver", "toed_batch.cpp")
+DRIVER = os.path.join(HERE, "toed_batch")
+
+
+def build_driver(verbose: bool = False) -> str:
+    """The batch command-line driver (host C++ over the C ABI): g++, linked
+    against the library with an rpath to it."""
+    import platform
+    stamp = DRIVER + ".arch"  # the machine the binary was built for (the tree may move between hosts)
+    if (os.path.exists(DRIVER) and os.path.exists(stamp) and open(stamp).read() == platform.machine()
+            and os.path.getmtime(DRIVER) >= max(os.path.getmtime(DRIVER_SRC), os.path.getmtime(LIB))):
+        return DRIVER
+    cuda = os.path.dirname(os.path.dirname(nvcc()))
+    cmd = [shutil.which("g++") or "g++", "-std=c++17", "-O2", "-I" + INCLUDE, "-I" + os.path.join(cuda, "include"),
+           DRIVER_SRC, "-o", DRIVER, LIB, "-L" + os.path.join(cuda, "lib64"), "-lcudart", "-lpthread",
+           "-Wl,-rpath," + HERE, "-Wl,-rpath," + os.path.join(cuda, "lib64")]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("driver build failed:\n" + r.stderr)
+    with open(stamp, "w") as f:
+        f.write(platform.machine())
+    if verbose:
+        print("built", DRIVER)
+    return DRIVER
 
 
 if __name__ == "__main__":
