@@ -50,9 +50,11 @@ def test_struct_layout_matches_header(toed, tmp_path):
 #include <stddef.h>
 #include "toed_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(toed_image), offsetof(toed_image, dtype),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(toed_image), offsetof(toed_image, dtype),
          offsetof(toed_image, edgels), offsetof(toed_image, capacity), offsetof(toed_image, count),
-         offsetof(toed_image, grid_index), sizeof(toed_params), offsetof(toed_params, precision));
+         offsetof(toed_image, grid_index), sizeof(toed_params), offsetof(toed_params, precision),
+         offsetof(toed_params, orientation), sizeof(toed_tuning), sizeof(toed_host_image),
+         offsetof(toed_host_image, grid_index), sizeof(toed_edgemap), sizeof(toed_subpix_params));
   return 0;
 }
 """)
@@ -60,9 +62,11 @@ int main(void) {
     subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), "-I/usr/local/cuda/include", str(c), "-o",
                     str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True).stdout.split()]
-    T, P = toed.toed_image, toed.toed_params
+    T, P, HI = toed.toed_image, toed.toed_params, toed.toed_host_image
     want = [ctypes.sizeof(T), T.dtype.offset, T.edgels.offset, T.capacity.offset, T.count.offset,
-            T.grid_index.offset, ctypes.sizeof(P), P.precision.offset]
+            T.grid_index.offset, ctypes.sizeof(P), P.precision.offset, P.orientation.offset,
+            ctypes.sizeof(toed.toed_tuning), ctypes.sizeof(HI), HI.grid_index.offset,
+            ctypes.sizeof(toed.toed_edgemap), ctypes.sizeof(toed.toed_subpix_params)]
     assert got == want
 
 
@@ -94,3 +98,28 @@ def test_ellipse_distance(synth):
     by = e.cy + e.a * np.cos(t) * s + e.b * np.sin(t) * c
     assert np.abs(synth.ellipse_distance(bx, by, e)).max() < 1e-9
     assert abs(synth.ellipse_distance(np.array([10.0]), np.array([20.0]), e)[0] - 3.0) < 1e-9
+
+
+def test_cpp_dropin_header_and_drivers_compile(toed, tmp_path):
+    """The header-only C++ drop-in (both classes and the free functions) and
+    the reference-style drivers that exercise it compile and link here."""
+    toed.build()
+    for drv in ("shim_driver.cpp", "subpix_driver.cpp"):
+        exe = tmp_path / drv.replace(".cpp", "")
+        subprocess.run(["g++", "-O1", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
+                        "-I/usr/local/cuda/include", os.path.join(ROOT, "tests", "cpp", drv), "-o", str(exe),
+                        toed.LIB_PATH, "-L/usr/local/cuda/lib64", "-lcudart"], check=True)
+        assert exe.exists()
+
+
+def test_batch_driver_cli_without_gpu(toed, tmp_path):
+    """toed_batch is built by build(); its usage text and input checks need
+    no GPU."""
+    toed.build()
+    exe = os.path.join(os.path.dirname(toed.LIB_PATH), "toed_batch")
+    r = subprocess.run([exe, "--help"], capture_output=True, text=True)
+    assert r.returncode == 0 and "edges_gpu.txt" in r.stdout
+    r = subprocess.run([exe, str(tmp_path / "missing"), str(tmp_path / "out")], capture_output=True, text=True)
+    assert r.returncode == 1 and "not found" in r.stderr
+    r = subprocess.run([exe, str(tmp_path), str(tmp_path / "out"), "--bogus"], capture_output=True, text=True)
+    assert r.returncode == 1 and "Unknown option" in r.stderr
