@@ -114,18 +114,26 @@ __device__ __forceinline__ float cubic_wf(float s)
 // ---------------------------------------------------------------------------
 // Orientation + NMS
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) tc_orient_nms(const __grid_constant__ SubParams p)
+__global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ SubParams p)
 {
     constexpr int HE = 6, NE = kT + 2 * HE;  // E region: rows/cols i0-6 .. i0+37
     __shared__ float sE[NE][NE + 1];
-    __shared__ float sTmp[NE][kT + 4];        // cols j0-2 .. j0+33
-    __shared__ float sSm[kT + 4][kT + 4];     // rows/cols -2 .. +33
-    __shared__ float sOx[kT + 2][kT + 3], sOy[kT + 2][kT + 3];  // -1 .. +32
     __shared__ float2 sDir[kT][kT];
     __shared__ int sRowCnt[kT], sRowOff[kT], sCandOff[kT + 1];
     __shared__ unsigned sOk[kT];              // per row: candidates the fit accepted
-    __shared__ short sCand[kT * kT];          // max-test candidates, row-major (tile pixel a * 32 + b)
-    __shared__ float3 sRes[kT * kT];          // per candidate: subpixel offset (x, y) and |max_f|
+    // the orientation estimate's stages (triangle rows, smoothed map, gradients), dead once the
+    // directions are in, then the NMS candidates: one buffer (five CTAs per SM)
+    constexpr size_t kTmpB = sizeof(float) * NE * (kT + 4), kSmB = sizeof(float) * (kT + 4) * (kT + 4);
+    constexpr size_t kOB = sizeof(float) * (kT + 2) * (kT + 3);
+    constexpr size_t kCandB = sizeof(short) * kT * kT, kResB = sizeof(float3) * kT * kT;
+    static_assert(kCandB + kResB <= kTmpB + kSmB + 2 * kOB, "candidates fit the orientation stages");
+    __shared__ __align__(16) unsigned char sStage[kTmpB + kSmB + 2 * kOB];
+    float(*sTmp)[kT + 4] = reinterpret_cast<float(*)[kT + 4]>(sStage);               // cols j0-2 .. j0+33
+    float(*sSm)[kT + 4] = reinterpret_cast<float(*)[kT + 4]>(sStage + kTmpB);        // rows/cols -2 .. +33
+    float(*sOx)[kT + 3] = reinterpret_cast<float(*)[kT + 3]>(sStage + kTmpB + kSmB);  // -1 .. +32
+    float(*sOy)[kT + 3] = reinterpret_cast<float(*)[kT + 3]>(sStage + kTmpB + kSmB + kOB);
+    short* sCand = reinterpret_cast<short*>(sStage);  // max-test candidates, row-major (tile pixel a * 32 + b)
+    float3* sRes = reinterpret_cast<float3*>(sStage + kCandB);  // per candidate: offset (x, y), |max_f|
 
     const int t = blockIdx.x;
     const int k = find_image(p.n_maps, t, [&](int i) { return p.m[i].tile_base; });
