@@ -1,0 +1,57 @@
+"""Parity at the benchmark's full sizes: the uneven batch of 64 float32
+images (79.4 Mpixel, sigma 1.5) exactly as bench.py generates it, and two of
+the eight 2048 x 2048 ridge maps of the TO-correction workload, against the
+FP64 oracle on all host cores (about ten seconds of CPU work each on a
+16-core host)."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, compare_edgels
+
+pytestmark = pytest.mark.gpu
+
+
+def test_full_uneven_batch_vs_oracle(toed, oracle):
+    import torch
+    sys.path.insert(0, ROOT)
+    import bench
+    images = bench.make_batch(bench.SEED0)  # spawn pool: no CUDA state is inherited
+    det = toed.Detector(0)
+    res = det.detect_batch([torch.as_tensor(im).cuda() for im in images], sigma=bench.SIGMA,
+                           out_dtype=toed.TOED_F64)
+    n_ref = n_common = 0
+    pos_max = ori_max = 0.0
+    ori = []
+    for im, r in zip(images, res):
+        ref = oracle.detect(im.astype(np.float64), bench.SIGMA, nthreads=os.cpu_count())
+        m = compare_edgels(ref["edges"], ref["index"], r["edgels"].cpu().numpy(), r["index"].cpu().numpy())
+        n_ref += m["n_ref"]
+        n_common += m["n_common"]
+        pos_max = max(pos_max, m["pos_max"])
+        ori_max = max(ori_max, m["ori_max"])
+        ori.append(m["ori_p99"])
+    assert n_ref > 2_000_000
+    assert n_common / n_ref >= 0.999
+    assert pos_max <= 1e-3
+    # the batch's noise (std up to 8) makes noise edgels whose third-order vector nearly cancels;
+    # their orientation carries FP32 rounding of the derivative stack
+    assert max(ori) <= 1e-5 and ori_max <= 1e-3, (max(ori), ori_max)
+
+
+def test_full_size_ridge_maps_vs_oracle(toed, oracle, synth):
+    import torch
+    sys.path.insert(0, os.path.dirname(__file__))
+    from test_gpu_subpix import _check
+    maps = [synth.ridge_map(2048, 2048, seed=5000 + k) for k in range(2)]
+    det = toed.Detector(0)
+    res = det.subpix_to_correct_batch([torch.as_tensor(E).cuda() for E in maps], thresh=0.1, sigma=2.0,
+                                      nbr_radius=2.0, out_dtype=toed.TOED_F64, dense=True)
+    for E, r in zip(maps, res):
+        ref = oracle.subpix_to_correct(E.astype(np.float64), 0.1, 2.0, 2.0, nthreads=os.cpu_count(), dense=True)
+        assert len(ref["edges"]) > 10_000
+        _check(ref["edges"], r["edgels"].cpu().numpy())
+        te = r["TO_E"].cpu().numpy()
+        assert np.mean((te != 0) == (ref["TO_E"] != 0)) >= 0.999
