@@ -36,9 +36,9 @@ def test_full_uneven_batch_vs_oracle(toed, oracle):
     assert n_ref > 2_000_000
     assert n_common / n_ref >= 0.999
     assert pos_max <= 1e-3
-    # the batch's noise (std up to 8) makes noise edgels whose third-order vector nearly cancels;
-    # their orientation carries FP32 rounding of the derivative stack
-    assert max(ori) <= 1e-5 and ori_max <= 1e-3, (max(ori), ori_max)
+    # the batch's noise (std up to 8) makes edgels whose third-order vector nearly cancels: their
+    # orientation is recomputed in FP64, so every edgel stays within the 1e-4 rad bound
+    assert max(ori) <= 1e-5 and ori_max <= 1e-4, (max(ori), ori_max)
 
 
 def test_full_size_ridge_maps_vs_oracle(toed, oracle, synth):

@@ -50,7 +50,7 @@ DetectEntry detect_entry(int r, bool hyb, bool async)
 
 // Taps from the reference's own commented generator (cpu_toed.cpp:141-162),
 // evaluated in double and rounded once to float.
-void make_taps(double sigma, int r, TapBlock* tb)
+void make_taps64(double sigma, int r, TapBlock64* tb)
 {
     std::memset(tb, 0, sizeof(*tb));
     const double nrm = std::sqrt(2.0 * 3.14159265358979323846);
@@ -60,12 +60,20 @@ void make_taps(double sigma, int r, TapBlock* tb)
         for (int k = 0; k < 2 * r + 3; ++k) {
             const double x = (double)(k - (r + 1)) + d;
             const double e = std::exp(-(x * x) / (2.0 * s * s));
-            tb->v[4 * sh + 0][k] = (float)(e / (nrm * s));
-            tb->v[4 * sh + 1][k] = (float)((-x * e) / (nrm * s * s * s));
-            tb->v[4 * sh + 2][k] = (float)(((x * x - s * s) * e) / (nrm * s * s * s * s * s));
-            tb->v[4 * sh + 3][k] = (float)(((x * (3.0 * s * s - x * x)) * e) / (nrm * s * s * s * s * s * s * s));
+            tb->v[4 * sh + 0][k] = e / (nrm * s);
+            tb->v[4 * sh + 1][k] = (-x * e) / (nrm * s * s * s);
+            tb->v[4 * sh + 2][k] = ((x * x - s * s) * e) / (nrm * s * s * s * s * s);
+            tb->v[4 * sh + 3][k] = ((x * (3.0 * s * s - x * x)) * e) / (nrm * s * s * s * s * s * s * s);
         }
     }
+}
+
+void make_taps(double sigma, int r, TapBlock* tb)
+{
+    TapBlock64 d;
+    make_taps64(sigma, r, &d);
+    for (int f = 0; f < 8; ++f)
+        for (int k = 0; k < kMaxTaps; ++k) tb->v[f][k] = (float)d.v[f][k];
 }
 
 static PFN_cuTensorMapEncodeTiled_v12000 encode_fn()
@@ -128,7 +136,7 @@ static thread_local std::string g_last_cuda_error;
 struct toed_ctx {
     int device = 0;
     int num_sms = 0;
-    int* words = nullptr;  // [0] queue [1] cursor [2] flags [3] spare
+    int* words = nullptr;  // [0] queue [1] cursor [2] flags [3] refine-list length
     double4_32a* staging = nullptr;
     int* staging_idx = nullptr;
     long long staging_cap = 0;
@@ -138,6 +146,8 @@ struct toed_ctx {
     long long tile_cap = 0;
     long long* img_base = nullptr;
     int img_cap = 0;
+    int4* refine = nullptr;  // orientation recomputation list
+    long long refine_cap = 0;
     float2* dir = nullptr;
     int* eid = nullptr;
     int* win = nullptr;
@@ -237,6 +247,7 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->seg);
     cudaFree(c->tile_sum);
     cudaFree(c->img_base);
+    cudaFree(c->refine);
     cudaFree(c->dir);
     cudaFree(c->eid);
     cudaFree(c->win);
@@ -283,6 +294,8 @@ static toed_status ensure_scratch(toed_ctx* c, long long staging, long long segs
     long long sc2 = c->staging_cap;
     if ((st = grow(&c->staging_idx, &sc2, staging, stream)) != TOED_OK) return st;
     c->staging_cap = std::min(sc, sc2);
+    // one entry per 64 staged edgels (about 1 in 5000 is listed on noisy images)
+    if ((st = grow(&c->refine, &c->refine_cap, staging / 64 + 1024, stream)) != TOED_OK) return st;
     if ((st = grow(&c->seg, &c->seg_cap, segs, stream)) != TOED_OK) return st;
     if ((st = grow(&c->tile_sum, &c->tile_cap, tiles, stream)) != TOED_OK) return st;
     long long ic = c->img_cap;
@@ -378,6 +391,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     BatchParams* p = new BatchParams();
     std::unique_ptr<BatchParams> guard(p);
     make_taps((double)prm->sigma, r, &p->taps);
+    make_taps64((double)prm->sigma, r, &p->taps64);
     p->thr = prm->threshold;
     p->border = prm->border;
     p->S = use ? use->strip_rows : plan_strip_rows(images, n, resident);
@@ -430,8 +444,14 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->sc.seg = c->seg;
     p->sc.tile_sum = c->tile_sum;
     p->sc.img_base = c->img_base;
+    // FP64 orientation recomputation: hybrid precision, grid orientation
+    // (the subpixel orientation replaces the staged one)
+    p->sc.refine = c->refine;
+    p->sc.refine_cap = (hyb && !p->qad) ? (int)std::min<long long>(c->refine_cap, 1LL << 30) : 0;
 
-    TOED_CU(cudaMemsetAsync(c->words, 0, (first_chunk ? 3 : 2) * sizeof(int), stream));
+    // the first chunk clears the flags and the refine-list length too; later
+    // chunks find the list emptied by the previous ordering pass
+    TOED_CU(cudaMemsetAsync(c->words, 0, (first_chunk ? 4 : 2) * sizeof(int), stream));
     const int grid = (int)std::min<long long>(units, resident);
     void* args[] = {p};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;

@@ -29,6 +29,10 @@ constexpr int kStepRows = 16;                      // original rows per sliding 
 constexpr int kColRows = 8;                        // rows per column-pass thread (register blocking)
 constexpr int kSegTile = 1024;                     // segments per ordering-pass tile
 constexpr int kStageBlk = 256;                     // staging records a CTA reserves at a time
+// Edgels whose third-order vector cancels by more than this factor (sum of
+// the terms' magnitudes over the largest component) get their orientation
+// recomputed from the image in FP64 (HYBRID precision, grid orientation).
+constexpr float kRefineKappa = 20.f;
 
 // 1-D taps, index k <-> offset x = k - (r+1) (+0.5 for the shifted set).
 // Filters: 0 G, 1 Gx, 2 Gxx, 3 Gxxx, 4..7 the same shifted by +0.5.
@@ -36,6 +40,11 @@ constexpr int kStageBlk = 256;                     // staging records a CTA rese
 // a constant-bank operand of the FMA.
 struct TapBlock {
     float v[8][kMaxTaps];
+};
+
+// The same taps in FP64, for the orientation recomputation.
+struct TapBlock64 {
+    double v[8][kMaxTaps];
 };
 
 struct DetImage {
@@ -59,18 +68,21 @@ struct DetImage {
 };
 
 struct Scratch {
-    int* words;          // [0] unit queue, [1] staging cursor, [2] flags, [3] spare
+    int* words;          // [0] unit queue, [1] staging cursor, [2] flags, [3] refine-list length
     double4_32a* staging;  // staged edgels (x, y, orientation, strength)
     int* staging_idx;
     long long staging_cap;
     int2* seg;           // per segment {staging offset, count}
     int* tile_sum;       // per ordering tile
     long long* img_base; // per image: exclusive prefix of its first segment
+    int4* refine;        // edgels whose orientation is recomputed in FP64: {staging slot, image, Gr, Gc}
+    int refine_cap;      // entries of `refine` (0: no recomputation)
 };
 
 struct BatchParams {
     CUtensorMap tmap[kBatchMax];  // per image: 2-D map, box (tma_boxw x kStepRows), OOB zero fill
     TapBlock taps;
+    TapBlock64 taps64;
     float thr;
     int border;
     int S;               // strip inner rows (multiple of kStepRows minus 2)
@@ -85,6 +97,7 @@ struct BatchParams {
     Scratch sc;
     DetImage img[kBatchMax];
 };
+static_assert(sizeof(BatchParams) <= 32764, "BatchParams is passed as one kernel parameter");
 
 // Block-wide exclusive scan of one int per thread (NT threads); leaves the
 // block total in *total.  s_warp: 33 ints of shared memory.

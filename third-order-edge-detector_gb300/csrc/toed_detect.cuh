@@ -394,16 +394,17 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 // Per-edgel epilogue from a deferred record: peak fit (FP64 in HYB mode:
 // the cancellations in fm + fp - 2f and fp - fm) and the third-order
 // orientation (cpu_toed.cpp:227-232, FP64 in HYB mode), then the staged
-// output record (x, y, orientation, strength) at its reserved slot.
+// output record (x, y, orientation, strength) at its reserved slot.  The
+// record holds its image's index; W2 is that image's 2x-grid width.
 template <bool HYB>
-__device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Scratch& sc)
+__device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Scratch& sc, int W2)
 {
     const float gx = rc[0], gy = rc[1], mv = rc[2], nx = rc[3], ny = rc[4], sl = rc[5];
     const float Map = rc[6], Mdp = rc[7], Mam = rc[8], Mdm = rc[9];
     const float fxx = rc[10], fxy = rc[11], fyy = rc[12], fxxy = rc[13], fxyy = rc[14], fxxx = rc[15],
                 fyyy = rc[16];
     const int Gr = __float_as_int(rc[17]), Gc = __float_as_int(rc[18]);
-    const int dst = __float_as_int(rc[19]), idx = __float_as_int(rc[20]);
+    const int dst = __float_as_int(rc[19]), img = __float_as_int(rc[20]), idx = Gr * W2 + Gc;
     double x, y;
     float ori, str;
     if (HYB) {
@@ -434,6 +435,19 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         const double tix = 2.0 * (dfx * a2 + dfy * bc + pxy * (double)fxxy) + y2 * (double)fxyy + x2 * (double)fxxx;
         const double tiy = 2.0 * (dfx * bc + dfy * c2 + pxy * (double)fxyy) + x2 * (double)fxxy + y2 * (double)fyyy;
         ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000) : atan2f((float)tix, (float)(-tiy));
+        // Cancellation ratio of the third-order vector: the sum of its terms'
+        // magnitudes over its own size.  The FP32 derivative stack's rounding
+        // reaches the orientation multiplied by this ratio, so edgels above
+        // kRefineKappa are listed for the FP64 recomputation (refine_edgels).
+        const float ax = fabsf(gx), ay = fabsf(gy), pxx = fabsf(fxx * fxy), pyy = fabsf(fyy * fxy);
+        const float sabs = 2.f * ax * (fxx * fxx + fxy * fxy) + 2.f * ay * (fyy * fyy + fxy * fxy) +
+                           2.f * (ax + ay) * (pxx + pyy) + 2.f * ax * ay * (fabsf(fxxy) + fabsf(fxyy)) +
+                           ay * ay * (fabsf(fxyy) + fabsf(fyyy)) + ax * ax * (fabsf(fxxx) + fabsf(fxxy));
+        const float tmax = fmaxf(fabsf((float)tix), fabsf((float)tiy));
+        if (sabs > kRefineKappa * tmax && sc.refine_cap > 0 && dst < sc.staging_cap) {
+            const int slot = atomicAdd(&sc.words[3], 1);
+            if (slot < sc.refine_cap) sc.refine[slot] = make_int4(dst, img, Gr, Gc);
+        }
     } else {
         const float fp = Map * (1.f - sl) + Mdp * sl;
         const float fm = Mam * (1.f - sl) + Mdm * sl;
@@ -784,13 +798,16 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                         rc[17] = __int_as_float(Gr);
                         rc[18] = __int_as_float(Gc);
                         rc[19] = __int_as_float(base + j0 + j);
-                        rc[20] = __int_as_float(Gr * W2 + Gc);
+                        rc[20] = __int_as_float(k);
                     }
                     nrec += chunk;
                     j0 += chunk;
                     if (nrec == C::NREC) {
                         __syncthreads();
-                        for (int r = tid; r < nrec; r += kThreads) finish_edgel<HYB>(sRec + r * C::RECW, p.sc);
+                        for (int r = tid; r < nrec; r += kThreads) {
+                            const float* rc = sRec + r * C::RECW;
+                            finish_edgel<HYB>(rc, p.sc, 2 * p.img[__float_as_int(rc[20])].W);
+                        }
                         nrec = 0;
                         __syncthreads();
                     }
@@ -802,7 +819,10 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         }
     }
     // flush the records still in the ring (the loop exit follows a barrier)
-    for (int r = tid; r < nrec; r += kThreads) finish_edgel<HYB>(sRec + r * C::RECW, p.sc);
+    for (int r = tid; r < nrec; r += kThreads) {
+        const float* rc = sRec + r * C::RECW;
+        finish_edgel<HYB>(rc, p.sc, 2 * p.img[__float_as_int(rc[20])].W);
+    }
 }
 
 

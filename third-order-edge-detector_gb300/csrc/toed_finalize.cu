@@ -4,7 +4,8 @@
 //
 // Segments are (2x-grid row, strip column) pairs laid out row-major per image
 // and padded to whole tiles of kSegTile.  Three short kernels:
-//   fin_tile_sums : edgels per tile
+//   fin_tile_sums : edgels per tile; then the FP64 orientation recomputation
+//                   of the edgels the detection kernel listed
 //   fin_tile_scan : exclusive scan over tiles; per-image base and count,
 //                   capacity flag
 //   fin_scatter   : per tile, scan the segment counts, then copy the tile's
@@ -15,6 +16,77 @@
 #include "toed_internal.h"
 
 namespace toed {
+
+// One listed edgel, one warp: the nine derivatives at 2x-grid point
+// (Gr, Gc) = (2i + a, 2j + b) straight from the image with FP64 taps, zero
+// outside the image -- the (2r+1)^2 window of unshifted taps on sub-grid
+// (0, 0) (cpu_toed.cpp:205-221), the (2r+3)^2 window with the half-pixel
+// shifted taps along the odd axes elsewhere (cpu_toed.cpp:246-344) -- then the
+// third-order vector (cpu_toed.cpp:227-232) and its angle in FP64, written
+// over the staged orientation.  Lane t forms the four column-filtered sums of
+// window row t; the row filters then weight them and the warp reduces.
+constexpr int kRefineChunk = 9;
+
+__device__ void refine_edgel(const BatchParams& p, int4 e, int lane)
+{
+    const DetImage& im = p.img[e.y];
+    const int r = p.radius;
+    const int i = e.z >> 1, a = e.z & 1, j = e.w >> 1, b = e.w & 1;
+    const int h = (a | b) ? r + 1 : r;
+    const double* X = &p.taps64.v[b ? 4 : 0][0];  // filter f, tap k: X[f * kMaxTaps + k]
+    const double* Y = &p.taps64.v[a ? 4 : 0][0];
+    const int dp = lane - h, row = i - dp;
+    double s0 = 0.0, s1 = 0.0, s2 = 0.0, s3 = 0.0, y0 = 0.0, y1 = 0.0, y2 = 0.0, y3 = 0.0;
+    if (lane <= 2 * h && row >= 0 && row < im.H) {
+        // the row in chunks of kRefineChunk columns, each chunk's loads
+        // first (independent, so in flight together)
+        const long long ro = (long long)row * im.pitch;
+        const bool u8 = im.dtype == TOED_U8;
+        const int k0 = r + 1 - h;  // tap of column offset q = -h
+        for (int c0 = 0; c0 <= 2 * h; c0 += kRefineChunk) {
+            float v[kRefineChunk];
+#pragma unroll
+            for (int t = 0; t < kRefineChunk; ++t) {
+                const int col = j + h - (c0 + t);  // column offset q = c0 + t - h
+                v[t] = 0.f;
+                if (c0 + t <= 2 * h && col >= 0 && col < im.W)
+                    v[t] = u8 ? (float)static_cast<const unsigned char*>(im.src)[ro + col]
+                              : static_cast<const float*>(im.src)[ro + col];
+            }
+#pragma unroll
+            for (int t = 0; t < kRefineChunk; ++t) {
+                if (c0 + t > 2 * h) break;
+                const double x = v[t];
+                const int kq = k0 + c0 + t;
+                s0 = fma(x, X[kq], s0);
+                s1 = fma(x, X[kMaxTaps + kq], s1);
+                s2 = fma(x, X[2 * kMaxTaps + kq], s2);
+                s3 = fma(x, X[3 * kMaxTaps + kq], s3);
+            }
+        }
+        const int kp = dp + r + 1;
+        y0 = Y[kp];
+        y1 = Y[kMaxTaps + kp];
+        y2 = Y[2 * kMaxTaps + kp];
+        y3 = Y[3 * kMaxTaps + kp];
+    }
+    // fx fy fxx fxy fyy fxxy fxyy fxxx fyyy
+    double d[9] = {y0 * s1, y1 * s0, y0 * s2, y1 * s1, y2 * s0, y1 * s2, y2 * s1, y0 * s3, y3 * s0};
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+        for (int f = 0; f < 9; ++f) d[f] += __shfl_xor_sync(0xffffffffu, d[f], o);
+    if (lane == 0) {
+        const double fx = d[0], fy = d[1], fxx = d[2], fxy = d[3], fyy = d[4], fxxy = d[5], fxyy = d[6],
+                     fxxx = d[7], fyyy = d[8];
+        const double tix = fx * (2 * fxx * fxx + 2 * fxy * fxy) + fy * (2 * fxx * fxy + 2 * fyy * fxy) +
+                           2 * fx * fy * fxxy + fy * fy * fxyy + fx * fx * fxxx;
+        const double tiy = fx * (2 * fxx * fxy + 2 * fyy * fxy) + fy * (2 * fyy * fyy + 2 * fxy * fxy) +
+                           2 * fx * fy * fxyy + fx * fx * fxxy + fy * fy * fyyy;
+        const double ori = (tix == 0.0 && tiy == 0.0) ? __longlong_as_double(0x7ff8000000000000LL) : atan2(tix, -tiy);
+        p.sc.staging[e.x].z = ori;
+    }
+}
 
 __global__ void __launch_bounds__(256) fin_tile_sums(const __grid_constant__ BatchParams p)
 {
@@ -32,6 +104,13 @@ __global__ void __launch_bounds__(256) fin_tile_sums(const __grid_constant__ Bat
     int total;
     block_excl_scan<256>(sum, s_warp, &total);
     if (threadIdx.x == 0) p.sc.tile_sum[t] = total;
+    if (p.sc.refine_cap > 0) {
+        const int nref = min(p.sc.words[3], p.sc.refine_cap);
+        // entry q to warp q / gridDim of block q % gridDim: a short list
+        // spreads over all SMs' FP64 pipes
+        const int lane = threadIdx.x & 31, w = (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+        for (int q = w; q < nref; q += gridDim.x * 8) refine_edgel(p, p.sc.refine[q], lane);
+    }
 }
 
 __global__ void __launch_bounds__(1024) fin_tile_scan(const __grid_constant__ BatchParams p)
@@ -55,6 +134,7 @@ __global__ void __launch_bounds__(1024) fin_tile_scan(const __grid_constant__ Ba
         *p.img[k].count = cnt;
         if (cnt > p.img[k].cap) atomicOr(&p.sc.words[2], TOED_FLAG_OVER_CAPACITY);
     }
+    if (threadIdx.x == 0) p.sc.words[3] = 0;  // refine list empty for the next launch (fin_tile_sums has read it)
 }
 
 // One CTA per tile of kSegTile segments: an exclusive scan gives every

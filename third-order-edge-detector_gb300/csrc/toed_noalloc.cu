@@ -38,6 +38,7 @@
 
 namespace toed {
 void make_taps(double sigma, int r, TapBlock* tb);
+void make_taps64(double sigma, int r, TapBlock64* tb);
 
 namespace {
 
@@ -47,6 +48,7 @@ constexpr long long kNaMaxEdgels = TOED_NOALLOC_MAX_EDGELS;
 // segments 2H x ceil(W/30) <= pixels/15 + 2H, padded to whole ordering tiles
 constexpr long long kNaMaxTiles = (kNaMaxPixels / 15 + 2LL * kNaMaxDim) / kSegTile + 2;
 constexpr long long kNaMaxSegs = kNaMaxTiles * kSegTile;
+constexpr long long kNaRefine = kNaMaxEdgels / 64 + 1024;  // orientation recomputation list
 
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 constexpr size_t kOffWords = 0;
@@ -55,7 +57,8 @@ constexpr size_t kOffIdx = align256(kOffStaging + sizeof(double4_32a) * kNaMaxEd
 constexpr size_t kOffSeg = align256(kOffIdx + sizeof(int) * kNaMaxEdgels);
 constexpr size_t kOffTiles = align256(kOffSeg + sizeof(int2) * kNaMaxSegs);
 constexpr size_t kOffBase = align256(kOffTiles + sizeof(int) * kNaMaxTiles);
-constexpr size_t kScratchBytes = align256(kOffBase + sizeof(long long));
+constexpr size_t kOffRefine = align256(kOffBase + sizeof(long long));
+constexpr size_t kScratchBytes = align256(kOffRefine + sizeof(int4) * kNaRefine);
 
 // The fixed scratch (see the file comment): about 11 MB per device.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
@@ -116,6 +119,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     BatchParams p;  // on the stack: no heap allocation either
     std::memset(&p, 0, sizeof(p));
     make_taps((double)prm->sigma, r, &p.taps);
+    make_taps64((double)prm->sigma, r, &p.taps64);
     p.thr = prm->threshold;
     p.border = prm->border;
     p.n_img = 1;
@@ -163,9 +167,11 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     p.sc.seg = reinterpret_cast<int2*>(base + kOffSeg);
     p.sc.tile_sum = reinterpret_cast<int*>(base + kOffTiles);
     p.sc.img_base = reinterpret_cast<long long*>(base + kOffBase);
+    p.sc.refine = reinterpret_cast<int4*>(base + kOffRefine);
+    p.sc.refine_cap = (p.hyb && !p.qad) ? (int)kNaRefine : 0;
 
-    // queue, staging cursor and flags start at zero on every call
-    if (cudaMemsetAsync(p.sc.words, 0, 3 * sizeof(int), stream) != cudaSuccess) return TOED_ERR_CUDA;
+    // queue, staging cursor, flags and refine-list length start at zero on every call
+    if (cudaMemsetAsync(p.sc.words, 0, 4 * sizeof(int), stream) != cudaSuccess) return TOED_ERR_CUDA;
     const int grid = (int)std::min<long long>(p.n_units, resident);
     void* args[] = {&p};
     if (cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream) != cudaSuccess)
