@@ -37,66 +37,85 @@ constexpr int kQadThreads = 128;
 constexpr int kQadSegPerThread = kSegTile / kQadThreads;
 
 // Keys cubic convolution kernel, a = -1/2 (subpix_to_correction.cpp:57-67).
-__device__ __forceinline__ float keys(float s)
+template <typename T>
+__device__ __forceinline__ T keys(T s)
 {
-    const float a = -0.5f, x = fabsf(s);
-    if (x <= 1.f) return ((a + 2.f) * x - (a + 3.f)) * x * x + 1.f;
-    if (x < 2.f) return ((a * x - 5.f * a) * x + 8.f * a) * x - 4.f * a;
-    return 0.f;
+    const T a = T(-0.5), x = fabs(s);
+    if (x <= T(1)) return ((a + T(2)) * x - (a + T(3))) * x * x + T(1);
+    if (x < T(2)) return ((a * x - T(5) * a) * x + T(8) * a) * x - T(4) * a;
+    return T(0);
 }
 
-__device__ __forceinline__ float warp_sum(float v)
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v)
 {
 #pragma unroll
     for (int d = 16; d > 0; d >>= 1) v += __shfl_xor_sync(0xffffffffu, v, d);
     return v;
 }
 
+// Four filter values (G, Gx, Gxx, Gxxx) in FP32 (float4) or FP64 (double4_32a).
+template <typename T> struct Vec4;
+template <> struct Vec4<float> {
+    using type = float4;
+    static __device__ __forceinline__ float4 make(float a, float b, float c, float d) { return make_float4(a, b, c, d); }
+};
+template <> struct Vec4<double> {
+    using type = double4_32a;
+    static __device__ __forceinline__ double4_32a make(double a, double b, double c, double d)
+    {
+        return make_double4_32a(a, b, c, d);
+    }
+};
+
 }  // namespace
 
 // The nine derivatives of one (x taps, y contraction) pairing, added in:
 // x = (G, Gx, Gxx, Gxxx) taps of this lane's column (weighted), c = the
 // column's contractions with (G, Gy, Gyy, Gyyy).
-__device__ __forceinline__ void qad_pair(float4 x, float4 c, float (&acc)[9])
+template <typename T, typename V>
+__device__ __forceinline__ void qad_pair(V x, V c, T (&acc)[9])
 {
-    acc[0] = fmaf(x.y, c.x, acc[0]);  // fx   = Gx   (x) G
-    acc[1] = fmaf(x.x, c.y, acc[1]);  // fy   = G    (x) Gy
-    acc[2] = fmaf(x.z, c.x, acc[2]);  // fxx  = Gxx  (x) G
-    acc[3] = fmaf(x.y, c.y, acc[3]);  // fxy  = Gx   (x) Gy
-    acc[4] = fmaf(x.x, c.z, acc[4]);  // fyy  = G    (x) Gyy
-    acc[5] = fmaf(x.z, c.y, acc[5]);  // fxxy = Gxx  (x) Gy
-    acc[6] = fmaf(x.y, c.z, acc[6]);  // fxyy = Gx   (x) Gyy
-    acc[7] = fmaf(x.w, c.x, acc[7]);  // fxxx = Gxxx (x) G
-    acc[8] = fmaf(x.x, c.w, acc[8]);  // fyyy = G    (x) Gyyy
+    acc[0] = fma(x.y, c.x, acc[0]);  // fx   = Gx   (x) G
+    acc[1] = fma(x.x, c.y, acc[1]);  // fy   = G    (x) Gy
+    acc[2] = fma(x.z, c.x, acc[2]);  // fxx  = Gxx  (x) G
+    acc[3] = fma(x.y, c.y, acc[3]);  // fxy  = Gx   (x) Gy
+    acc[4] = fma(x.x, c.z, acc[4]);  // fyy  = G    (x) Gyy
+    acc[5] = fma(x.z, c.y, acc[5]);  // fxxy = Gxx  (x) Gy
+    acc[6] = fma(x.y, c.z, acc[6]);  // fxyy = Gx   (x) Gyy
+    acc[7] = fma(x.w, c.x, acc[7]);  // fxxx = Gxxx (x) G
+    acc[8] = fma(x.x, c.w, acc[8]);  // fyyy = G    (x) Gyyy
 }
 
-__device__ __forceinline__ float4 f4_fma(float a, float4 x, float4 y)
+template <typename T, typename V>
+__device__ __forceinline__ V v4_fma(T a, V x, V y)
 {
-    return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+    return Vec4<T>::make(fma(a, x.x, y.x), fma(a, x.y, y.y), fma(a, x.z, y.z), fma(a, x.w, y.w));
 }
 
-__device__ __forceinline__ float4 f4_scale(float a, float4 x) { return make_float4(a * x.x, a * x.y, a * x.z, a * x.w); }
+template <typename T, typename V>
+__device__ __forceinline__ V v4_scale(T a, V x) { return Vec4<T>::make(a * x.x, a * x.y, a * x.z, a * x.w); }
 
 // Interpolation is linear, so the four columns of the 4 x 4 block fold into
 // three weighted x-tap vectors per lane, one per x variant in use: columns
 // of parity b = 0 take T taps in rows of parity a = 0 and F taps in rows
 // a = 1; columns b = 1 take S taps.  The columns' parities alternate from
 // X1 - 1, so B0 (0 or 1) is the parity of the block's first column.
-template <int R, int B0>
-__device__ __forceinline__ void qad_columns(const float4* __restrict__ sTab, int X1, int j, int l,
-                                            const float (&wx)[4], float4& xT, float4& xF, float4& xS)
+template <int R, int B0, typename T, typename V>
+__device__ __forceinline__ void qad_columns(const V* __restrict__ sTab, int X1, int j, int l, const T (&wx)[4],
+                                            V& xT, V& xF, V& xS)
 {
     constexpr int NT = 2 * R + 3, NTP = NT + 4;
-    xT = xF = xS = make_float4(0.f, 0.f, 0.f, 0.f);
+    xT = xF = xS = Vec4<T>::make(T(0), T(0), T(0), T(0));
 #pragma unroll
     for (int s = 0; s < 4; ++s) {
         const int dj = ((X1 - 1 + s) >> 1) - j;
         const int e = NT + 2 + dj - l;  // padded entry of this lane's column
         if (((B0 + s) & 1) == 0) {
-            xT = f4_fma(wx[s], sTab[e], xT);
-            xF = f4_fma(wx[s], sTab[NTP + e], xF);
+            xT = v4_fma(wx[s], sTab[e], xT);
+            xF = v4_fma(wx[s], sTab[NTP + e], xF);
         } else {
-            xS = f4_fma(wx[s], sTab[2 * NTP + e], xS);
+            xS = v4_fma(wx[s], sTab[2 * NTP + e], xS);
         }
     }
 }
@@ -107,35 +126,116 @@ __device__ __forceinline__ void qad_columns(const float4* __restrict__ sTab, int
 // for A = 1; full (F) for A = 0, the truncated set (T) being F without its
 // two end taps -- weights it by the row's Keys weight and adds the row's
 // sub-grids: (0,0) T x T, (0,1) S x F, (1,0) F x S, (1,1) S x S (x by y).
-template <int R, int A, int DI>
-__device__ __forceinline__ void qad_row(const float (&v)[2 * R + 5], const float4* __restrict__ sTab, float wy,
-                                        float4 xT, float4 xF, float4 xS, float (&acc)[9])
+template <int R, int A, int DI, typename T, typename V>
+__device__ __forceinline__ void qad_row(const float (&v)[2 * R + 5], const V* __restrict__ sTab, T wy, V xT, V xF,
+                                        V xS, T (&acc)[9])
 {
     constexpr int NT = 2 * R + 3, NTP = NT + 4, NU = NT + 2;
-    const float4* Yt = sTab + (A ? 2 : 1) * NTP + NT + 2 + DI;  // entry NT + 2 + DI - u: tap of window row u
-    float4 c = make_float4(0.f, 0.f, 0.f, 0.f);
+    const V* Yt = sTab + (A ? 2 : 1) * NTP + NT + 2 + DI;  // entry NT + 2 + DI - u: tap of window row u
+    V c = Vec4<T>::make(T(0), T(0), T(0), T(0));
 #pragma unroll
     for (int u = 0; u < NU; ++u) {
-        const float4 y = Yt[-u];
-        c.x = fmaf(v[u], y.x, c.x); c.y = fmaf(v[u], y.y, c.y);
-        c.z = fmaf(v[u], y.z, c.z); c.w = fmaf(v[u], y.w, c.w);
+        const V y = Yt[-u];
+        const T x = v[u];
+        c.x = fma(x, y.x, c.x); c.y = fma(x, y.y, c.y);
+        c.z = fma(x, y.z, c.z); c.w = fma(x, y.w, c.w);
     }
     if (A) {
-        const float4 cs = f4_scale(wy, c);
+        const V cs = v4_scale(wy, c);
         qad_pair(xF, cs, acc);
         qad_pair(xS, cs, acc);
     } else {
         // T = F less the taps k = 0 (window row NT + DI) and k = NT - 1 (window row DI + 1)
-        const float4 e0 = sTab[NTP + 2], e1 = sTab[NTP + 2 + NT - 1];
-        const float va = v[NT + DI], vb = v[DI + 1];
-        float4 t;
-        t.x = fmaf(-vb, e1.x, fmaf(-va, e0.x, c.x));
-        t.y = fmaf(-vb, e1.y, fmaf(-va, e0.y, c.y));
-        t.z = fmaf(-vb, e1.z, fmaf(-va, e0.z, c.z));
-        t.w = fmaf(-vb, e1.w, fmaf(-va, e0.w, c.w));
-        qad_pair(xT, f4_scale(wy, t), acc);
-        qad_pair(xS, f4_scale(wy, c), acc);
+        const V e0 = sTab[NTP + 2], e1 = sTab[NTP + 2 + NT - 1];
+        const T va = v[NT + DI], vb = v[DI + 1];
+        V t;
+        t.x = fma(-vb, e1.x, fma(-va, e0.x, c.x));
+        t.y = fma(-vb, e1.y, fma(-va, e0.y, c.y));
+        t.z = fma(-vb, e1.z, fma(-va, e0.z, c.z));
+        t.w = fma(-vb, e1.w, fma(-va, e0.w, c.w));
+        qad_pair(xT, v4_scale(wy, t), acc);
+        qad_pair(xS, v4_scale(wy, c), acc);
     }
+}
+
+// The nine derivatives interpolated at subpixel point (X1 + tx, Y1 + ty) of
+// the 2x grid from this lane's window column v: step 1 (Keys weights) and
+// step 3 of the file comment, before the sum over lanes.
+template <int R, typename T>
+__device__ __forceinline__ void qad_point(const float (&v)[2 * R + 5], const typename Vec4<T>::type* __restrict__ sTab,
+                                          int X1, int Y1, T tx, T ty, int l, T (&acc)[9])
+{
+    using V = typename Vec4<T>::type;
+    const int j = X1 >> 1;
+    T wx[4], wy[4];
+#pragma unroll
+    for (int s = 0; s < 4; ++s) {
+        wx[s] = keys(tx + T(1) - (T)s);
+        wy[s] = keys(ty + T(1) - (T)s);
+    }
+    V xT, xF, xS;
+    if ((X1 & 1) == 0)
+        qad_columns<R, 1>(sTab, X1, j, l, wx, xT, xF, xS);
+    else
+        qad_columns<R, 0>(sTab, X1, j, l, wx, xT, xF, xS);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = T(0);
+    if ((Y1 & 1) == 0) {
+        qad_row<R, 1, -1>(v, sTab, wy[0], xT, xF, xS, acc);
+        qad_row<R, 0, 0>(v, sTab, wy[1], xT, xF, xS, acc);
+        qad_row<R, 1, 0>(v, sTab, wy[2], xT, xF, xS, acc);
+        qad_row<R, 0, 1>(v, sTab, wy[3], xT, xF, xS, acc);
+    } else {
+        qad_row<R, 0, 0>(v, sTab, wy[0], xT, xF, xS, acc);
+        qad_row<R, 1, 0>(v, sTab, wy[1], xT, xF, xS, acc);
+        qad_row<R, 0, 1>(v, sTab, wy[2], xT, xF, xS, acc);
+        qad_row<R, 1, 1>(v, sTab, wy[3], xT, xF, xS, acc);
+    }
+}
+
+// The third-order vector (cpu_toed.cpp:227-232) in FP64 from nine derivatives.
+template <typename T>
+__device__ __forceinline__ void to_vector(const T (&d)[9], double& tix, double& tiy)
+{
+    const double fx = d[0], fy = d[1], fxx = d[2], fxy = d[3], fyy = d[4], fxxy = d[5], fxyy = d[6],
+                 fxxx = d[7], fyyy = d[8];
+    tix = fx * (2.0 * fxx * fxx + 2.0 * fxy * fxy) + fy * (2.0 * fxx * fxy + 2.0 * fyy * fxy) +
+          2.0 * fx * fy * fxxy + fy * fy * fxyy + fx * fx * fxxx;
+    tiy = fx * (2.0 * fxx * fxy + 2.0 * fyy * fxy) + fy * (2.0 * fyy * fyy + 2.0 * fxy * fxy) +
+          2.0 * fx * fy * fxyy + fx * fx * fxxy + fy * fy * fyyy;
+}
+
+// FP64 pass for one record (the whole warp): the window around the record's
+// subpixel point (2x-grid coordinates px, py), the interpolated derivatives
+// with FP64 weights and taps, their sum over the lanes and the third-order
+// vector (every lane gets it).  Out of line: it is rare, and inlined its
+// registers would crowd the FP32 contraction.
+template <int R>
+__device__ __noinline__ double2 qad_refine(const void* src, long long pitch, int H, int W, bool u8,
+                                           const double4_32a* __restrict__ sTab64, double px, double py, int lane)
+{
+    constexpr int NU = 2 * R + 5;
+    const double fpx = floor(px), fpy = floor(py);
+    const int X1 = (int)fpx, Y1 = (int)fpy;
+    const int i = Y1 >> 1, col = (X1 >> 1) - R - 2 + lane;
+    const bool okc = lane < NU && col >= 0 && col < W;
+    float w[NU];
+#pragma unroll
+    for (int u = 0; u < NU; ++u) {
+        const int y = i - R - 2 + u;
+        w[u] = 0.f;
+        if (okc && (unsigned)y < (unsigned)H) {
+            const long long o = (long long)y * pitch + col;
+            w[u] = u8 ? (float)static_cast<const unsigned char*>(src)[o] : static_cast<const float*>(src)[o];
+        }
+    }
+    double acc[9];
+    qad_point<R, double>(w, sTab64, X1, Y1, px - fpx, py - fpy, lane < NU ? lane : NU - 1, acc);
+#pragma unroll
+    for (int q = 0; q < 9; ++q) acc[q] = warp_sum(acc[q]);
+    double2 ti;
+    to_vector(acc, ti.x, ti.y);
+    return ti;
 }
 
 template <int R>
@@ -149,15 +249,22 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
     // taps per variant T (2r+1, ends zero) / F (2r+3) / S (shifted): (G, Gx, Gxx, Gxxx), two zero entries
     // each side, so that entry NT + 2 + d - c is the tap of window row / column c for a point at offset d
     __shared__ float4 sTab[3 * NTP];
+    // the same in FP64 (HYBRID precision: records whose third-order vector nearly cancels)
+    __shared__ double4_32a sTab64[3 * NTP];
     // per warp, the nine derivatives of the 32 records in flight (stride 9: conflict-free per lane)
     __shared__ float sDer[kQadThreads / 32][32 * 9];
     for (int i = threadIdx.x; i < 3 * NTP; i += kQadThreads) {
         const int v = i / NTP, k = i - v * NTP - 2;
         const int f = (v == 2) ? 4 : 0;
         float4 t = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (k >= 0 && k < NT && !(v == 0 && (k == 0 || k == NT - 1)))
+        double4_32a t64 = make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        if (k >= 0 && k < NT && !(v == 0 && (k == 0 || k == NT - 1))) {
             t = make_float4(p.taps.v[f][k], p.taps.v[f + 1][k], p.taps.v[f + 2][k], p.taps.v[f + 3][k]);
+            t64 = make_double4_32a(p.taps64.v[f][k], p.taps64.v[f + 1][k], p.taps64.v[f + 2][k],
+                                   p.taps64.v[f + 3][k]);
+        }
         sTab[i] = t;
+        sTab64[i] = t64;
     }
     const int t = blockIdx.x;
     const int k = find_image(p.n_img, t, [&](int i) { return p.img[i].tile_base; });
@@ -246,35 +353,8 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
             if (e + 1 < ne) load_window(e + 1, vn);
             const int X1 = __shfl_sync(0xffffffffu, mX1, e), Y1 = __shfl_sync(0xffffffffu, mY1, e);
             const float tx = __shfl_sync(0xffffffffu, mtx, e), ty = __shfl_sync(0xffffffffu, mty, e);
-            const int j = X1 >> 1;
-            // 1. the Keys weights of the 4 x 4 block around the subpixel point
-            float wx[4], wy[4];
-#pragma unroll
-            for (int s = 0; s < 4; ++s) {
-                wx[s] = keys(tx + 1.f - (float)s);
-                wy[s] = keys(ty + 1.f - (float)s);
-            }
-            // 3. the block's columns folded into three x-tap vectors, then its
-            // four rows Y1 - 1 .. Y1 + 2 (parities and offsets follow Y1's parity)
-            float4 xT, xF, xS;
-            if ((X1 & 1) == 0)
-                qad_columns<R, 1>(sTab, X1, j, l, wx, xT, xF, xS);
-            else
-                qad_columns<R, 0>(sTab, X1, j, l, wx, xT, xF, xS);
             float acc[9];
-#pragma unroll
-            for (int q = 0; q < 9; ++q) acc[q] = 0.f;
-            if ((Y1 & 1) == 0) {
-                qad_row<R, 1, -1>(v, sTab, wy[0], xT, xF, xS, acc);
-                qad_row<R, 0, 0>(v, sTab, wy[1], xT, xF, xS, acc);
-                qad_row<R, 1, 0>(v, sTab, wy[2], xT, xF, xS, acc);
-                qad_row<R, 0, 1>(v, sTab, wy[3], xT, xF, xS, acc);
-            } else {
-                qad_row<R, 0, 0>(v, sTab, wy[0], xT, xF, xS, acc);
-                qad_row<R, 1, 0>(v, sTab, wy[1], xT, xF, xS, acc);
-                qad_row<R, 0, 1>(v, sTab, wy[2], xT, xF, xS, acc);
-                qad_row<R, 1, 1>(v, sTab, wy[3], xT, xF, xS, acc);
-            }
+            qad_point<R, float>(v, sTab, X1, Y1, tx, ty, l, acc);
             // 4. sums over the window columns, parked for lane e
 #pragma unroll
             for (int q = 0; q < 9; ++q) acc[q] = warp_sum(acc[q]);
@@ -288,18 +368,37 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
 #pragma unroll
         for (int q = 0; q < 9; ++q) mine[q] = sDer[wid][lane * 9 + q];
         __syncwarp();  // the next group overwrites the slots
-        if (my_d < 0) continue;
-        const double4_32a my_rc = p.sc.staging[my_src];
-        // the third-order vector, the angle and the output record
+        const double4_32a my_rc = my_d >= 0 ? p.sc.staging[my_src] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        // the third-order vector and the angle
         const float gx = mine[0], gy = mine[1], fxx = mine[2], fxy = mine[3], fyy = mine[4], fxxy = mine[5],
                     fxyy = mine[6], fxxx = mine[7], fyyy = mine[8];
         float ori;
         if (p.hyb) {
-            const double dfx = gx, dfy = gy, dxx = fxx, dxy = fxy, dyy = fyy;
-            const double tix = dfx * (2.0 * dxx * dxx + 2.0 * dxy * dxy) + dfy * (2.0 * dxx * dxy + 2.0 * dyy * dxy) +
-                               2.0 * dfx * dfy * (double)fxxy + dfy * dfy * (double)fxyy + dfx * dfx * (double)fxxx;
-            const double tiy = dfx * (2.0 * dxx * dxy + 2.0 * dyy * dxy) + dfy * (2.0 * dyy * dyy + 2.0 * dxy * dxy) +
-                               2.0 * dfx * dfy * (double)fxyy + dfx * dfx * (double)fxxy + dfy * dfy * (double)fyyy;
+            double tix, tiy;
+            to_vector(mine, tix, tiy);
+            // Records whose vector cancels by more than kRefineKappa (sum of
+            // the terms' magnitudes over the largest component) carry the FP32
+            // contraction's rounding multiplied by that ratio: the warp
+            // recomputes their nine derivatives in FP64, one record at a time.
+            const float ax = fabsf(gx), ay = fabsf(gy), pxx = fabsf(fxx * fxy), pyy = fabsf(fyy * fxy);
+            const float sabs = 2.f * ax * (fxx * fxx + fxy * fxy) + 2.f * ay * (fyy * fyy + fxy * fxy) +
+                               2.f * (ax + ay) * (pxx + pyy) + 2.f * ax * ay * (fabsf(fxxy) + fabsf(fxyy)) +
+                               ay * ay * (fabsf(fxyy) + fabsf(fyyy)) + ax * ax * (fabsf(fxxx) + fabsf(fxxy));
+            const float tmax = fmaxf(fabsf((float)tix), fabsf((float)tiy));
+            unsigned flag = __ballot_sync(0xffffffffu, my_d >= 0 && sabs > kRefineKappa * tmax);
+            while (flag) {
+                const int e = __ffs(flag) - 1;
+                flag &= flag - 1;
+                // the subpixel point in FP64 from the staged position
+                const double2 xy = *reinterpret_cast<const double2*>(
+                    &p.sc.staging[__shfl_sync(0xffffffffu, my_src, e)]);
+                const double2 ti = qad_refine<R>(im.src, im.pitch, im.H, im.W, im.dtype == TOED_U8, sTab64,
+                                                 2.0 * xy.x + 1.0, 2.0 * xy.y + 1.0, lane);
+                if (lane == e) {
+                    tix = ti.x;
+                    tiy = ti.y;
+                }
+            }
             ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000) : atan2f((float)tix, (float)(-tiy));
         } else {
             const float tix = gx * (2.f * fxx * fxx + 2.f * fxy * fxy) + gy * (2.f * fxx * fxy + 2.f * fyy * fxy) +
@@ -308,6 +407,7 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
                               2.f * gx * gy * fxyy + gx * gx * fxxy + gy * gy * fyyy;
             ori = (tix == 0.f && tiy == 0.f) ? __int_as_float(0x7fc00000) : atan2f(tix, -tiy);
         }
+        if (my_d < 0) continue;
         if (p.out_f64) {
             double2* o = reinterpret_cast<double2*>(im.out) + 2 * my_d;
             o[0] = make_double2(my_rc.x, my_rc.y);
