@@ -273,22 +273,26 @@ def side_measurements(toed, det, images, side, stream):
     seq = _time_ms(lambda: [det.detect_into([d], [o], prm, stream) for d, o in zip(d_imgs, outs)], 3, stream)
     npx = sum(im.size for im in images)
     out["batch_as_64_sequential_launches_mpx_s"] = round(npx / (seq * 1e-3) / 1e6, 1)
-    # the reference's dense two-kernel form rebuilt (toed_convolve_planes + toed_nms_planes), FP32, per image
+    # the reference's single-image GPU form (gpu_convolve + gpu_nms: dense 2x-grid planes, then NMS), FP32,
+    # image by image: its full 2-D window sums restated (toed_convolve_planes_direct), and the same planes
+    # computed separably (toed_convolve_planes), the stronger baseline
     import ctypes
     L = toed.lib()
 
     planes = [torch.empty((6, 2 * d.shape[0], 2 * d.shape[1]), dtype=torch.float32, device=dev) for d in d_imgs]
 
-    def dense_form():
+    def dense_form(conv):
         for d, P in zip(d_imgs, planes):
             H, W = d.shape
-            L.toed_convolve_planes(ctypes.c_void_p(d.data_ptr()), toed.TOED_F32, H, W, W, float(SIGMA), 0, None,
-                                   toed.TOED_F32, *[ctypes.c_void_p(P[k].data_ptr()) for k in range(4)],
-                                   ctypes.c_void_p(stream.cuda_stream))
+            conv(ctypes.c_void_p(d.data_ptr()), toed.TOED_F32, H, W, W, float(SIGMA), 0, None,
+                 toed.TOED_F32, *[ctypes.c_void_p(P[k].data_ptr()) for k in range(4)],
+                 ctypes.c_void_p(stream.cuda_stream))
             L.toed_nms_planes(toed.TOED_F32, 2 * H, 2 * W, *[ctypes.c_void_p(P[k].data_ptr()) for k in range(3)],
                               float(THRESH), 10, ctypes.c_void_p(P[4].data_ptr()), ctypes.c_void_p(P[5].data_ptr()),
                               ctypes.c_void_p(stream.cuda_stream))
-    dms = _time_ms(dense_form, 2, stream)
+    rms = _time_ms(lambda: dense_form(L.toed_convolve_planes_direct), 2, stream)
+    out["reference_gpu_form_direct_windows_mpx_s"] = round(npx / (rms * 1e-3) / 1e6, 1)
+    dms = _time_ms(lambda: dense_form(L.toed_convolve_planes), 2, stream)
     out["dense_two_kernel_form_mpx_s"] = round(npx / (dms * 1e-3) / 1e6, 1)
     del planes
     # -- the MATLAB quick-and-dirty orientation mode on the same batch ------

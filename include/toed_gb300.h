@@ -18,6 +18,9 @@
  *   toed_convolve_planes
  *       gpu_convolve(device_id, h, w, interp_h, interp_w, dev_img, dev_Ix, ...)
  *                                                               gpu_kernels.hpp:24-45
+ *   toed_convolve_planes_direct
+ *       the same call, the reference kernel's summation structure
+ *                                               gpu_convolve.cu:8-349
  *   toed_nms_planes
  *       gpu_nms(device_id, interp_h, interp_w, dev_Ix, dev_Iy, dev_I_grad_mag,
  *               dev_subpix_pos_x_map, dev_subpix_pos_y_map)     gpu_kernels.hpp:48-63
@@ -290,6 +293,18 @@ toed_status toed_convolve_planes(const void* pixels, int dtype, int h, int w, in
                                  float sigma, int radius, const double* taps, int planes_dtype,
                                  void* Ix, void* Iy, void* grad_mag, void* orient,
                                  cudaStream_t stream);
+/* The same planes, same arguments, summed the way the reference's
+ * gpu_convolve_kernel sums them (gpu_convolve.cu:96-300): each of the nine
+ * derivatives of each sub-grid as a full 2-D window -- (2r+1)^2 taps on
+ * sub-grid (0,0), (2r+3)^2 elsewhere -- row offset outer, column offset
+ * inner.  For callers that want the reference's summation order (its FP32
+ * rounding pattern) and as the reference's single-image GPU form in
+ * benchmarks; toed_convolve_planes gives the same planes separably at a
+ * fraction of the cost. */
+toed_status toed_convolve_planes_direct(const void* pixels, int dtype, int h, int w, int pitch,
+                                        float sigma, int radius, const double* taps, int planes_dtype,
+                                        void* Ix, void* Iy, void* grad_mag, void* orient,
+                                        cudaStream_t stream);
 toed_status toed_nms_planes(int planes_dtype, int interp_h, int interp_w, const void* Ix,
                             const void* Iy, const void* grad_mag, float threshold, int border,
                             void* pos_x_map, void* pos_y_map, cudaStream_t stream);

@@ -230,8 +230,15 @@ inline void convolve(int h, int w, T* dev_img, T* dev_Ix, T* dev_Iy, T* dev_I_gr
         report_cuda(cudaMemcpy(tmp.data(), src[f], sizeof(T) * n, cudaMemcpyDeviceToHost), "cudaMemcpy");
         for (int k = 0; k < n; ++k) taps[f * n + k] = (double)tmp[k];
     }
-    report(toed_convolve_planes(dev_img, sizeof(T) == 8 ? TOED_F64 : TOED_F32, h, w, w, 2.0f, r, taps.data(),
-                                sizeof(T) == 8 ? TOED_F64 : TOED_F32, dev_Ix, dev_Iy, dev_I_grad_mag, dev_I_orient, 0),
+    // TOED_GPU_CONVOLVE_DIRECT: the reference kernel's full 2-D window sums (its
+    // FP32 rounding pattern) instead of the separable evaluation of the same planes
+#ifdef TOED_GPU_CONVOLVE_DIRECT
+    auto conv = toed_convolve_planes_direct;
+#else
+    auto conv = toed_convolve_planes;
+#endif
+    report(conv(dev_img, sizeof(T) == 8 ? TOED_F64 : TOED_F32, h, w, w, 2.0f, r, taps.data(),
+                sizeof(T) == 8 ? TOED_F64 : TOED_F32, dev_Ix, dev_Iy, dev_I_grad_mag, dev_I_orient, 0),
            "gpu_convolve");
 }
 }  // namespace toed_shim

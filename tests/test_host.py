@@ -104,9 +104,10 @@ def test_cpp_dropin_header_and_drivers_compile(toed, tmp_path):
     """The header-only C++ drop-in (both classes and the free functions) and
     the reference-style drivers that exercise it compile and link here."""
     toed.build()
-    for drv in ("shim_driver.cpp", "subpix_driver.cpp"):
-        exe = tmp_path / drv.replace(".cpp", "")
-        subprocess.run(["g++", "-O1", "-std=c++17", "-Wall", "-I" + os.path.join(ROOT, "include"),
+    for drv, defs in (("shim_driver.cpp", []), ("shim_driver.cpp", ["-DTOED_GPU_CONVOLVE_DIRECT"]),
+                      ("subpix_driver.cpp", [])):
+        exe = tmp_path / (drv.replace(".cpp", "") + ("_direct" if defs else ""))
+        subprocess.run(["g++", "-O1", "-std=c++17", "-Wall", *defs, "-I" + os.path.join(ROOT, "include"),
                         "-I/usr/local/cuda/include", os.path.join(ROOT, "tests", "cpp", drv), "-o", str(exe),
                         toed.LIB_PATH, "-L/usr/local/cuda/lib64", "-lcudart"], check=True)
         assert exe.exists()

@@ -38,7 +38,7 @@ MAX_RADIUS = 12
 C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
-    "toed_convolve_planes", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
+    "toed_convolve_planes", "toed_convolve_planes_direct", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
     "toed_subpix_to_correct_batch", "toed_detect_noalloc", "toed_backward_batch", "toed_autotune",
     "toed_set_tuning", "toed_detect_host_batch", "toed_edgels_to_columns", "toed_write_edgels_txt",
 ]
@@ -142,6 +142,7 @@ def lib():
         L.toed_device_flags.argtypes = [vp, vp, ctypes.POINTER(ip)]
         L.toed_convolve_planes.argtypes = [vp, ip, ip, ip, ip, ctypes.c_float, ip, vp, ip, vp, vp, vp,
                                            vp, vp]
+        L.toed_convolve_planes_direct.argtypes = L.toed_convolve_planes.argtypes
         L.toed_nms_planes.argtypes = [ip, ip, ip, vp, vp, vp, ctypes.c_float, ip, vp, vp, vp]
         L.toed_profile_begin.argtypes = [vp]
         L.toed_profile_end.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ip)]

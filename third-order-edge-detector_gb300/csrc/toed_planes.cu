@@ -9,6 +9,8 @@
 //                 one thread per original pixel evaluates the nine
 //                 derivatives at its four sub-grids (cpu_toed.cpp:204-355),
 //                 |grad I| and the TO orientation.
+// direct_planes_kernel : the same planes with the reference's full 2-D
+//                 window per derivative (toed_convolve_planes_direct).
 // nms_kernel    : one thread per 2x-grid point, subpixel NMS as
 //                 cpu_toed.cpp:399-495, writing the position maps.
 #include <algorithm>
@@ -156,13 +158,103 @@ __global__ void __launch_bounds__(256) nms_kernel(int H2, int W2, const T* Ix, c
     }
 }
 
+// The reference's own structure (gpu_convolve.cu:96-300): every derivative
+// of every sub-grid a full 2-D window sum -- (2r+1)^2 taps on sub-grid (0,0),
+// (2r+3)^2 on the others -- over a shared-memory tile, one thread per
+// original pixel, row offset p outer and column offset q inner, each term
+// the pixel times its x tap times its y tap.  The four column-tap products
+// of a pixel are shared by the nine derivatives (4 multiplies + 9 FMAs per
+// window tap).  Written with the window width as a template argument so the
+// inner loop unrolls like the reference's fixed-size one.
+constexpr int DTW = 16, DTH = 16;
+
+template <typename T, int R>
+__global__ void __launch_bounds__(DTW * DTH) direct_planes_kernel(const void* src, int dtype, int H, int W,
+                                                                  long long pitch, const __grid_constant__ TapsT<T> tp,
+                                                                  T* Ix, T* Iy, T* mag, T* ori)
+{
+    constexpr int NIN = DTW + 2 * R + 2, NR = DTH + 2 * R + 2;
+    __shared__ T sIn[NR][NIN];
+    const int i0 = blockIdx.y * DTH, j0 = blockIdx.x * DTW;
+    for (int t = threadIdx.x; t < NR * NIN; t += DTW * DTH) {
+        const int rr = t / NIN, cc = t - rr * NIN;
+        sIn[rr][cc] = load_pixel<T>(src, pitch, H, W, dtype, i0 - R - 1 + rr, j0 - R - 1 + cc);
+    }
+    __syncthreads();
+    const int x = threadIdx.x % DTW, y = threadIdx.x / DTW;
+    const int i = i0 + y, j = j0 + x;
+    if (i >= H || j >= W) return;
+    const int W2 = 2 * W;
+#pragma unroll 1
+    for (int sg = 0; sg < 4; ++sg) {
+        const int a = sg >> 1, b = sg & 1;
+        const int h = sg ? R + 1 : R;  // window half-width
+        const T* X = tp.v[b ? 4 : 0];  // filter f, tap k: X[f * kMaxTaps + k]
+        const T* Y = tp.v[a ? 4 : 0];
+        T d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+#pragma unroll 1
+        for (int p = -h; p <= h; ++p) {
+            const T* row = &sIn[y + R + 1 - p][x + R + 1];  // row[-q]: pixel (i - p, j - q)
+            const int kp = p + R + 1;
+            const T yG = Y[kp], yGx = Y[kMaxTaps + kp], yGxx = Y[2 * kMaxTaps + kp], yGxxx = Y[3 * kMaxTaps + kp];
+#pragma unroll
+            for (int q = -(R + 1); q <= R + 1; ++q) {
+                if (q < -h || q > h) continue;
+                const int kq = q + R + 1;
+                const T v = row[-q];
+                const T vG = v * X[kq], vGx = v * X[kMaxTaps + kq], vGxx = v * X[2 * kMaxTaps + kq],
+                        vGxxx = v * X[3 * kMaxTaps + kq];
+                d[0] += vGx * yG;    // fx
+                d[1] += vG * yGx;    // fy
+                d[2] += vGxx * yG;   // fxx
+                d[3] += vGx * yGx;   // fxy
+                d[4] += vG * yGxx;   // fyy
+                d[5] += vGxx * yGx;  // fxxy
+                d[6] += vGx * yGxx;  // fxyy
+                d[7] += vGxxx * yG;  // fxxx
+                d[8] += vG * yGxxx;  // fyyy
+            }
+        }
+        const long long o = (long long)(2 * i + a) * W2 + (2 * j + b);
+        Ix[o] = d[0];
+        Iy[o] = d[1];
+        mag[o] = sqrt(d[0] * d[0] + d[1] * d[1]);
+        ori[o] = to_orient<T>(d[0], d[1], d[2], d[3], d[4], d[5], d[6], d[7], d[8]);
+    }
+}
+
+template <typename T, int R>
+cudaError_t launch_direct(const void* pixels, int dtype, int h, int w, int pitch, const TapsT<T>& tt, void* Ix,
+                          void* Iy, void* gm, void* orient, cudaStream_t stream)
+{
+    dim3 grid((w + DTW - 1) / DTW, (h + DTH - 1) / DTH);
+    direct_planes_kernel<T, R><<<grid, DTW * DTH, 0, stream>>>(pixels, dtype, h, w, (long long)pitch, tt, (T*)Ix,
+                                                               (T*)Iy, (T*)gm, (T*)orient);
+    return cudaGetLastError();
+}
+
 template <typename T>
-cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, float sigma, int r,
-                       const double* taps, void* Ix, void* Iy, void* gm, void* orient, cudaStream_t stream)
+cudaError_t run_direct(const void* pixels, int dtype, int h, int w, int pitch, int r, const TapsT<T>& tt, void* Ix,
+                       void* Iy, void* gm, void* orient, cudaStream_t stream)
+{
+    switch (r) {
+#define TOED_DIRECT_CASE(RR) \
+    case RR: return launch_direct<T, RR>(pixels, dtype, h, w, pitch, tt, Ix, Iy, gm, orient, stream);
+    TOED_DIRECT_CASE(1) TOED_DIRECT_CASE(2) TOED_DIRECT_CASE(3) TOED_DIRECT_CASE(4)
+    TOED_DIRECT_CASE(5) TOED_DIRECT_CASE(6) TOED_DIRECT_CASE(7) TOED_DIRECT_CASE(8)
+    TOED_DIRECT_CASE(9) TOED_DIRECT_CASE(10) TOED_DIRECT_CASE(11) TOED_DIRECT_CASE(12)
+#undef TOED_DIRECT_CASE
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+// Taps for the planes kernels: the library's FP32 taps for float planes,
+// the formula in FP64 for double planes, or the caller's table.
+template <typename T>
+void planes_taps(float sigma, int r, const double* taps, TapsT<T>& tt)
 {
     TapBlock tb;
     make_taps((double)sigma, r, &tb);
-    TapsT<T> tt;
     std::memset(&tt, 0, sizeof(tt));
     // FP64 planes take the taps straight from the formula in double
     const double nrm = std::sqrt(2.0 * 3.14159265358979323846);
@@ -178,6 +270,14 @@ cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, f
     if (taps)
         for (int f = 0; f < 8; ++f)
             for (int k = 0; k < 2 * r + 3; ++k) tt.v[f][k] = (T)taps[f * (2 * r + 3) + k];
+}
+
+template <typename T>
+cudaError_t run_planes(const void* pixels, int dtype, int h, int w, int pitch, float sigma, int r,
+                       const double* taps, void* Ix, void* Iy, void* gm, void* orient, cudaStream_t stream)
+{
+    TapsT<T> tt;
+    planes_taps<T>(sigma, r, taps, tt);
     const int NR = TH + 2 * r + 2, NIN = TW + 2 * r + 2;
     const size_t smem = sizeof(T) * ((size_t)NR * NIN + 12 * (size_t)NR * TW);
     cudaError_t e = cudaFuncSetAttribute((const void*)planes_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -211,6 +311,32 @@ extern "C" toed_status toed_convolve_planes(const void* pixels, int dtype, int h
         e = run_planes<double>(pixels, dtype, h, w, pitch, sigma, r, taps, Ix, Iy, grad_mag, orient, stream);
     else
         return TOED_ERR_INVALID_ARG;
+    return e == cudaSuccess ? TOED_OK : TOED_ERR_CUDA;
+}
+
+extern "C" toed_status toed_convolve_planes_direct(const void* pixels, int dtype, int h, int w, int pitch,
+                                                   float sigma, int radius, const double* taps, int planes_dtype,
+                                                   void* Ix, void* Iy, void* grad_mag, void* orient,
+                                                   cudaStream_t stream)
+{
+    if (!pixels || !Ix || !Iy || !grad_mag || !orient || h <= 0 || w <= 0 || pitch < w) return TOED_ERR_INVALID_ARG;
+    if (!(sigma > 0.f) && !taps) return TOED_ERR_INVALID_ARG;
+    if (taps && radius <= 0) return TOED_ERR_INVALID_ARG;
+    if (dtype != TOED_U8 && dtype != TOED_F32 && dtype != TOED_F64) return TOED_ERR_UNSUPPORTED;
+    const int r = radius > 0 ? radius : (int)std::ceil(4.0 * (double)sigma);
+    if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
+    cudaError_t e;
+    if (planes_dtype == TOED_F32) {
+        TapsT<float> tt;
+        planes_taps<float>(sigma, r, taps, tt);
+        e = run_direct<float>(pixels, dtype, h, w, pitch, r, tt, Ix, Iy, grad_mag, orient, stream);
+    } else if (planes_dtype == TOED_F64) {
+        TapsT<double> tt;
+        planes_taps<double>(sigma, r, taps, tt);
+        e = run_direct<double>(pixels, dtype, h, w, pitch, r, tt, Ix, Iy, grad_mag, orient, stream);
+    } else {
+        return TOED_ERR_INVALID_ARG;
+    }
     return e == cudaSuccess ? TOED_OK : TOED_ERR_CUDA;
 }
 
