@@ -12,11 +12,15 @@ from conftest import ROOT, compare_edgels
 pytestmark = pytest.mark.gpu
 
 
-def test_cpp_shim_matches_oracle(toed, oracle, synth, tmp_path):
+@pytest.mark.parametrize("direct", [False, True])
+def test_cpp_shim_matches_oracle(toed, oracle, synth, tmp_path, direct):
+    """direct: gpu_convolve built with TOED_GPU_CONVOLVE_DIRECT (the reference
+    kernel's full 2-D window sums)."""
     toed.build()
     exe = tmp_path / "shim_driver"
     cuda = "/usr/local/cuda"
-    cmd = ["g++", "-O2", "-std=c++17", "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
+    defs = ["-DTOED_GPU_CONVOLVE_DIRECT"] if direct else []
+    cmd = ["g++", "-O2", "-std=c++17", *defs, "-I" + os.path.join(ROOT, "include"), "-I" + cuda + "/include",
            os.path.join(ROOT, "tests", "cpp", "shim_driver.cpp"), "-o", str(exe),
            toed.LIB_PATH, "-L" + cuda + "/lib64", "-lcudart", "-Wl,-rpath," + os.path.dirname(toed.LIB_PATH),
            "-Wl,-rpath," + cuda + "/lib64"]
