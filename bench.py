@@ -42,7 +42,7 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 SIGMA, THRESH, N_IMAGES, SEED0 = 1.5, 2.0, 64, 3000
-E2E_CHUNKS = 4  # image groups the host-buffer path pipelines over
+E2E_CHUNKS = 16  # image groups the host-buffer path pipelines its copies over
 REF_SECONDS = 120.0  # CPU time the reference arm spends on warm-up plus timed steps
 METRIC = "Mpixel/s (TOED fused forward, uneven batch of 64 float32 images, sigma 1.5)"
 
@@ -490,9 +490,9 @@ def run_ours(args, ws, rank, local):
 
     # ---- end to end through the public API with host buffers -----------
     # toed_detect_host_batch: page-locked host images in, host edgel lists
-    # out; the detection kernel reads the page-locked images in place over the
-    # C2C link and the ordering pass writes the lists into host memory (with
-    # pageable buffers the library pipelines copies over E2E_CHUNKS groups)
+    # out; the copy engine brings the images in over E2E_CHUNKS groups while
+    # one detection launch runs (its CTAs wait for their group's copy), and
+    # the ordering pass writes the lists into host memory
     h_imgs = [torch.as_tensor(im).pin_memory() for im in images]
     h_outs = det.alloc_host_outputs([im.shape for im in images], None, toed.TOED_F32, index=False)
     for o, c in zip(h_outs, caps):
@@ -500,9 +500,11 @@ def run_ours(args, ws, rank, local):
     h2d = sum(im.nbytes for im in images)
     d2h_total = 0
 
+    h_batch = det.host_batch(h_imgs, h_outs)  # the buffers described once, as a serving loop would
+
     def e2e_step():
         nonlocal d2h_total
-        det.detect_host(h_imgs, h_outs, params, chunks=E2E_CHUNKS, stream=stream)
+        det.detect_host(h_batch, params=params, chunks=E2E_CHUNKS, stream=stream)
         d2h_total = sum(16 * min(int(o["count"].item()), o["capacity"]) + 4 for o in h_outs)
 
     for _ in range(max(1, args.warmup)):

@@ -319,8 +319,12 @@ def test_host_batch_flat_images(toed, synth, pin):
     prm = toed.make_params(1.5)
     hp = [im.pin_memory() for im in host] if pin else host
     outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True, pin=pin)
-    for _ in range(2):
-        det.detect_host(hp, outs, prm, chunks=2)
+    plan = det.host_batch(hp, outs)
+    for rep in range(3):
+        if rep == 0:
+            det.detect_host(hp, outs, prm, chunks=2)
+        else:  # the prepared batch, reused
+            det.detect_host(plan, params=prm, chunks=2)
         for k, (r, o) in enumerate(zip(ref, outs)):
             n = int(o["count"].item())
             assert n == r["count"], k
@@ -328,11 +332,14 @@ def test_host_batch_flat_images(toed, synth, pin):
             assert t.equal(o["index"][:n], r["index"].cpu()), k
 
 
-def test_host_batch_zero_copy_layouts(toed, synth):
-    """Page-locked images are read in place by the detection kernel (async
-    row staging): 16-byte copies where rows allow them, 4-byte copies for odd
-    widths, a host pitch wider than the image and uint8 rows (plain loads).
-    Every layout gives the device-buffer batch's lists bit for bit."""
+@pytest.mark.parametrize("chunks", [1, 3])
+def test_host_batch_zero_copy_layouts(toed, synth, chunks):
+    """Page-locked images, chunks == 1: read in place by the detection kernel
+    (async row staging): 16-byte copies where rows allow them, 4-byte copies
+    for odd widths, a host pitch wider than the image and uint8 rows (plain
+    loads).  chunks == 3: copied in groups (1-D and pitched copies) while one
+    launch runs, its CTAs waiting for their group's ready flag.  Every layout
+    gives the device-buffer batch's lists bit for bit."""
     t = _torch()
     det = toed.Detector(0)
     sizes = [(211, 301, np.float32), (97, 127, np.float32), (150, 333, np.uint8), (120, 200, np.float32)]
@@ -344,7 +351,7 @@ def test_host_batch_zero_copy_layouts(toed, synth):
     wide[:, :sizes[3][1]] = host[3]
     pinned[3] = wide[:, :sizes[3][1]]  # pitch 203 floats: rows not 16-byte aligned
     outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True, pin=True)
-    det.detect_host(pinned, outs, toed.make_params(1.5))
+    det.detect_host(pinned, outs, toed.make_params(1.5), chunks=chunks)
     for k, (r, o) in enumerate(zip(ref, outs)):
         n = int(o["count"].item())
         assert n == r["count"] and n > 20, k

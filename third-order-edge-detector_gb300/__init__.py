@@ -214,6 +214,36 @@ def make_params(sigma=2.0, radius=0, threshold=2.0, border=10, out_dtype=TOED_F3
                        int(precision), int(orientation))
 
 
+class HostBatch:
+    """A host-memory batch described once (Detector.host_batch): the C array
+    of toed_host_image for toed_detect_host_batch plus references keeping the
+    tensors alive."""
+
+    def __init__(self, det, images, outs):
+        t = det.torch
+        self.det, self.images, self.outs = det, list(images), list(outs)
+        if len(self.images) != len(self.outs):
+            raise ValueError("one output set per image")
+        arr = (toed_host_image * len(self.images))()
+        for k, (im, o) in enumerate(zip(self.images, self.outs)):
+            if im.dim() != 2 or im.device.type != "cpu" or im.stride(1) != 1:
+                raise ValueError("host images must be 2-D CPU tensors with contiguous rows")
+            dt = TOED_U8 if im.dtype == t.uint8 else (TOED_F32 if im.dtype == t.float32 else None)
+            if dt is None:
+                raise ValueError("image dtype must be uint8 or float32")
+            H, W = im.shape
+            arr[k] = toed_host_image(im.data_ptr(), H, W, im.stride(0), dt, o["edgels"].data_ptr(), o["capacity"],
+                                     o["count"].data_ptr(),
+                                     o["index"].data_ptr() if o.get("index") is not None else None)
+        self.arr = arr
+
+    def run(self, params: toed_params, chunks: int = 4, stream=None):
+        det = self.det
+        s = stream if stream is not None else det.torch.cuda.current_stream(det.device)
+        _check(lib().toed_detect_host_batch(det._ctx, self.arr, len(self.images), ctypes.byref(params), int(chunks),
+                                            ctypes.c_void_p(s.cuda_stream)), "toed_detect_host_batch")
+
+
 class Detector:
     """A detection context on one device: owns the scratch of the fused
     kernel and (optionally) caches CUDA graphs of fixed batches."""
@@ -334,26 +364,23 @@ class Detector:
             outs.append(o)
         return outs
 
-    def detect_host(self, images, outs, params: toed_params, chunks: int = 4, stream=None):
+    def host_batch(self, images, outs):
+        """Prepare a host-memory batch once for repeated detect_host calls on
+        the same buffers (a serving loop's fixed page-locked staging): the
+        returned object holds the images and outputs alive and the C array of
+        toed_host_image describing them, so each call is one C call."""
+        return HostBatch(self, images, outs)
+
+    def detect_host(self, images, outs=None, params: toed_params = None, chunks: int = 4, stream=None):
         """Detect edgels in images held in host memory (2-D CPU tensors,
         page-locked for full speed) into host buffers from
         alloc_host_outputs: copies in, detection and copies out are
-        pipelined over ``chunks`` groups (synchronous)."""
-        t = self.torch
-        arr = (toed_host_image * len(images))()
-        for k, (im, o) in enumerate(zip(images, outs)):
-            if im.dim() != 2 or im.device.type != "cpu" or im.stride(1) != 1:
-                raise ValueError("host images must be 2-D CPU tensors with contiguous rows")
-            dt = TOED_U8 if im.dtype == t.uint8 else (TOED_F32 if im.dtype == t.float32 else None)
-            if dt is None:
-                raise ValueError("image dtype must be uint8 or float32")
-            H, W = im.shape
-            arr[k] = toed_host_image(im.data_ptr(), H, W, im.stride(0), dt, o["edgels"].data_ptr(), o["capacity"],
-                                     o["count"].data_ptr(),
-                                     o["index"].data_ptr() if o.get("index") is not None else None)
-        s = stream if stream is not None else t.cuda.current_stream(self.device)
-        _check(lib().toed_detect_host_batch(self._ctx, arr, len(images), ctypes.byref(params), int(chunks),
-                                            ctypes.c_void_p(s.cuda_stream)), "toed_detect_host_batch")
+        pipelined over ``chunks`` groups (synchronous).  ``images`` may be a
+        HostBatch from host_batch() (then ``outs`` is None)."""
+        if params is None:
+            raise ValueError("params required (make_params)")
+        hb = images if isinstance(images, HostBatch) else HostBatch(self, images, outs)
+        hb.run(params, chunks, stream)
 
     def capture(self, images, outs, params: toed_params, warmup: int = 1):
         """Capture detect_into(images, outs, params) in a CUDA graph (the

@@ -177,6 +177,12 @@ struct toed_ctx {
     int* hb_cnt_host = nullptr;
     long long hb_cnt_host_cap = 0;
     cudaStream_t s_in = nullptr, s_out = nullptr;
+    // copy-group ready flags (device), the epoch they are set to (page-locked
+    // source of the flag copies) and the epoch of the current call
+    int* hb_ready = nullptr;
+    long long hb_ready_cap = 0;
+    int* hb_epoch_src = nullptr;
+    int hb_epoch = 0;
     std::mutex mu;
 };
 
@@ -259,6 +265,8 @@ toed_status toed_destroy(toed_ctx* c)
     cudaFree(c->hb_idx);
     cudaFree(c->hb_cnt);
     if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
+    if (c->hb_epoch_src) cudaFreeHost(c->hb_epoch_src);
+    cudaFree(c->hb_ready);
     if (c->s_in) cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamDestroy(c->s_out);
     cudaSetDevice(prev);
@@ -369,9 +377,11 @@ static int plan_strip_rows(const toed_image* images, int n, long long resident)
 // plain_loads: never stage input rows by TMA (images read in place from
 // page-locked host memory through their device mapping): float32 rows by
 // per-thread async copies one step ahead, uint8 rows by plain loads
+// wait_slot (optional, per image): 0, or g > 0 when the copy engine is still
+// bringing the image in and c->hb_ready[g - 1] == c->hb_epoch marks its arrival
 static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
                                 int r, bool first_chunk, cudaStream_t stream, const toed_tuning* force = nullptr,
-                                bool plain_loads = false)
+                                bool plain_loads = false, const int* wait_slot = nullptr)
 {
     const bool hyb = prm->precision != TOED_FP32;
     const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0][size_class(images, n)];
@@ -400,6 +410,8 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->radius = r;
     p->hyb = hyb ? 1 : 0;
     p->qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
+    p->ready = c->hb_ready;
+    p->ready_epoch = c->hb_epoch;
     long long units = 0, tiles = 0, staging = 0;
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
@@ -419,6 +431,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
         encode_rows_map(&p->tmap[i], d, r);
+        d.wait_slot = wait_slot ? wait_slot[i] : 0;
         if (async_rows)
             d.tma = (d.dtype == TOED_F32) ? 2 : 0;  // async row copies (float32) or plain loads, never TMA
         else if (use && !use->staging)
@@ -486,12 +499,14 @@ static toed_status check_batch(const toed_ctx* c, const toed_image* images, int 
 
 // The batch in chunks of kBatchMax images (caller holds c->mu, device set).
 static toed_status detect_all(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
-                              cudaStream_t stream, const toed_tuning* force = nullptr, bool plain_loads = false)
+                              cudaStream_t stream, const toed_tuning* force = nullptr, bool plain_loads = false,
+                              const int* wait_slot = nullptr)
 {
     const int r = radius_of(prm);
     toed_status st = TOED_OK;
     for (int i0 = 0; i0 < n && st == TOED_OK; i0 += kBatchMax)
-        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force, plain_loads);
+        st = detect_chunk(c, images + i0, std::min(kBatchMax, n - i0), prm, r, i0 == 0, stream, force, plain_loads,
+                          wait_slot ? wait_slot + i0 : nullptr);
     return st;
 }
 
@@ -666,17 +681,31 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         }
         return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
     };
-    // Page-locked inputs are read in place by the detection kernel through
-    // their device mapping (zero copy over the C2C link, plain row loads):
-    // no staging copies, and the batch goes as one launch per 64 images.
+    // Page-locked inputs: with chunks == 1 the detection kernel reads them in
+    // place through their device mapping (zero copy over the C2C link); with
+    // more groups the copy engine brings the groups into device memory while
+    // ONE detection launch runs, each image's CTAs waiting (bounded) for its
+    // group's ready flag, which the copy engine writes after the group's
+    // pixels -- every pixel crosses the link once and no group boundary
+    // drains the GPU.  Pageable inputs: staged copies per group, one
+    // detection launch per group once its copy is in.
     bool zin = true;
     std::vector<const void*> in_map(n, nullptr);
     for (int i = 0; i < n && zin; ++i) {
         in_map[i] = mapped(const_cast<void*>(images[i].pixels));
         zin = in_map[i] != nullptr;
     }
-    if (zin) chunks = 1;
-    if (!zin && (st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
+    const bool inplace = zin && chunks == 1, flagged = zin && chunks > 1;
+    if (!inplace && (st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
+    if (flagged) {
+        const long long had = c->hb_ready_cap;
+        if ((st = grow(&c->hb_ready, &c->hb_ready_cap, (long long)chunks, stream)) != TOED_OK) return fail(st);
+        if (c->hb_ready_cap != had) TOED_HB(cudaMemsetAsync(c->hb_ready, 0, sizeof(int) * c->hb_ready_cap, stream));
+        if (!c->hb_epoch_src) TOED_HB(cudaMallocHost((void**)&c->hb_epoch_src, sizeof(int)));
+        // a new epoch per call: flags left by earlier calls never match
+        c->hb_epoch = c->hb_epoch % 0x3fffffff + 1;
+        *c->hb_epoch_src = c->hb_epoch;
+    }
     if ((st = grow(&c->hb_out, &c->hb_out_cap, std::max(out_b, 1LL), stream)) != TOED_OK) return fail(st);
     if ((st = grow(&c->hb_idx, &c->hb_idx_cap, std::max(idx_n, 1LL), stream)) != TOED_OK) return fail(st);
     if ((st = grow(&c->hb_cnt, &c->hb_cnt_cap, (long long)n + chunks, stream)) != TOED_OK) return fail(st);
@@ -700,8 +729,8 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         dev[i].grid_index = static_cast<int*>(gi);
     }
     for (int i = 0; i < n; ++i) {
-        dev[i].pixels = zin ? in_map[i] : c->hb_in + in_off[i];
-        if (zin) dev[i].pitch = images[i].pitch;
+        dev[i].pixels = inplace ? in_map[i] : c->hb_in + in_off[i];
+        if (inplace) dev[i].pitch = images[i].pitch;
         if (!direct) {
             dev[i].edgels = c->hb_out + out_off[i];
             dev[i].count = c->hb_cnt + i;
@@ -713,11 +742,12 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         if (st != TOED_OK) return fail(st);
     }
     // groups of consecutive images whose pixel counts grow geometrically
-    // (ratio 1.6, about detection time / copy time per pixel): the first
-    // group is small so detection starts early, and each later copy still
-    // finishes before the detection in front of it
+    // (ratio at most detection time / copy time per pixel, about 1.6): the
+    // first group is small so detection starts early, and each later copy
+    // still finishes before the detection in front of it.  Flagged groups
+    // cost no launch, so they grow more slowly (1.3) from a smaller start.
     {
-        const double g = 1.6, gn = std::pow(g, chunks) - 1.0;
+        const double g = flagged ? 1.3 : 1.6, gn = std::pow(g, chunks) - 1.0;
         long long acc = 0;
         int k = 0;
         first[0] = 0;
@@ -732,40 +762,67 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         TOED_HB(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
         TOED_HB(cudaEventCreateWithFlags(&ev_det[k], cudaEventDisableTiming));
     }
-    // 1. every group's images to the device, in order (whole-image 1-D
-    // copies where the rows are contiguous: those run on the copy engines)
-    for (int k = 0; k < chunks && !zin; ++k) {
+    auto copy_group = [&](int k) -> cudaError_t {  // group k's images to the device on s_in
         for (int i = first[k]; i < first[k + 1]; ++i) {
             const toed_host_image& h = images[i];
             const int esz = h.dtype == TOED_U8 ? 1 : 4;
-            if (h.pitch == h.width && dev[i].pitch == h.width)
-                TOED_HB(cudaMemcpyAsync(const_cast<void*>(dev[i].pixels), h.pixels, (size_t)h.width * h.height * esz,
-                                        cudaMemcpyHostToDevice, c->s_in));
-            else
-                TOED_HB(cudaMemcpy2DAsync(const_cast<void*>(dev[i].pixels), (size_t)dev[i].pitch * esz, h.pixels,
-                                          (size_t)h.pitch * esz, (size_t)h.width * esz, (size_t)h.height,
-                                          cudaMemcpyHostToDevice, c->s_in));
+            // whole-image 1-D copies where the rows are contiguous: those run on the copy engines
+            const cudaError_t e =
+                (h.pitch == h.width && dev[i].pitch == h.width)
+                    ? cudaMemcpyAsync(const_cast<void*>(dev[i].pixels), h.pixels, (size_t)h.width * h.height * esz,
+                                      cudaMemcpyHostToDevice, c->s_in)
+                    : cudaMemcpy2DAsync(const_cast<void*>(dev[i].pixels), (size_t)dev[i].pitch * esz, h.pixels,
+                                        (size_t)h.pitch * esz, (size_t)h.width * esz, (size_t)h.height,
+                                        cudaMemcpyHostToDevice, c->s_in);
+            if (e != cudaSuccess) return e;
         }
-        TOED_HB(cudaEventRecord(ev_in[k], c->s_in));
-    }
-    // 2. detection of each group once its images are in
-    for (int k = 0; k < chunks; ++k) {
-        if (!zin) TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
-        st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream, nullptr, zin);
+        return cudaSuccess;
+    };
+    // launch groups: the detection launches, each followed by a read of the flags word
+    int launches = chunks;
+    if (flagged) {
+        // the copies wait only for what the caller's stream held before this
+        // call (never for the detection launch, whose CTAs wait for them)
+        TOED_HB(cudaEventRecord(ev_in[0], stream));
+        TOED_HB(cudaStreamWaitEvent(c->s_in, ev_in[0], 0));
+        std::vector<int> slot(n);
+        for (int k = 0; k < chunks; ++k)
+            for (int i = first[k]; i < first[k + 1]; ++i) slot[i] = k + 1;
+        st = detect_all(c, dev.data(), n, prm, stream, nullptr, true, slot.data());
         if (st != TOED_OK) return fail(st);
-        TOED_HB(cudaMemcpyAsync(c->hb_cnt + n + k, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
-        TOED_HB(cudaEventRecord(ev_det[k], stream));
+        TOED_HB(cudaMemcpyAsync(c->hb_cnt + n, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
+        TOED_HB(cudaEventRecord(ev_det[0], stream));
+        for (int k = 0; k < chunks; ++k) {
+            TOED_HB(copy_group(k));
+            TOED_HB(cudaMemcpyAsync(c->hb_ready + k, c->hb_epoch_src, sizeof(int), cudaMemcpyHostToDevice, c->s_in));
+        }
+        launches = 1;
+        first[1] = n;
+    } else {
+        // 1. every group's images to the device, in order
+        for (int k = 0; k < chunks && !inplace; ++k) {
+            TOED_HB(copy_group(k));
+            TOED_HB(cudaEventRecord(ev_in[k], c->s_in));
+        }
+        // 2. detection of each group once its images are in
+        for (int k = 0; k < chunks; ++k) {
+            if (!inplace) TOED_HB(cudaStreamWaitEvent(stream, ev_in[k], 0));
+            st = detect_all(c, dev.data() + first[k], first[k + 1] - first[k], prm, stream, nullptr, inplace);
+            if (st != TOED_OK) return fail(st);
+            TOED_HB(cudaMemcpyAsync(c->hb_cnt + n + k, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
+            TOED_HB(cudaEventRecord(ev_det[k], stream));
+        }
     }
     // 3. per group: counts (and the group's device flags) to the host, then
     // the lists, while later groups are still being copied in or detected
     int flags = 0;
     if (direct) {
-        TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + n, c->hb_cnt + n, sizeof(int) * chunks, cudaMemcpyDeviceToHost,
+        TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + n, c->hb_cnt + n, sizeof(int) * launches, cudaMemcpyDeviceToHost,
                                 stream));
         TOED_HB(cudaStreamSynchronize(stream));
-        for (int k = 0; k < chunks; ++k) flags |= c->hb_cnt_host[n + k];
+        for (int k = 0; k < launches; ++k) flags |= c->hb_cnt_host[n + k];
     }
-    for (int k = 0; k < chunks && !direct; ++k) {
+    for (int k = 0; k < launches && !direct; ++k) {
         TOED_HB(cudaStreamWaitEvent(c->s_out, ev_det[k], 0));
         const int i0 = first[k], nk = first[k + 1] - first[k];
         TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + i0, c->hb_cnt + i0, sizeof(int) * nk, cudaMemcpyDeviceToHost,
@@ -788,6 +845,7 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     }
     TOED_HB(cudaStreamSynchronize(c->s_out));
     TOED_HB(cudaStreamSynchronize(stream));
+    TOED_HB(cudaStreamSynchronize(c->s_in));
 #undef TOED_HB
     fail(TOED_OK);  // releases the events, restores the device
     if (flags & TOED_FLAG_TIMEOUT) return TOED_ERR_TIMEOUT;

@@ -33,6 +33,9 @@ constexpr int kStageBlk = 256;                     // staging records a CTA rese
 // the terms' magnitudes over the largest component) get their orientation
 // recomputed from the image in FP64 (HYBRID precision, grid orientation).
 constexpr float kRefineKappa = 20.f;
+// Bound of the wait for a copy group's ready flag (polls ~256 ns apart: a few
+// seconds), after which the kernel flags TOED_FLAG_TIMEOUT and goes on.
+constexpr int kReadySpinLimit = 1 << 24;
 
 // 1-D taps, index k <-> offset x = k - (r+1) (+0.5 for the shifted set).
 // Filters: 0 G, 1 Gx, 2 Gxx, 3 Gxxx, 4..7 the same shifted by +0.5.
@@ -65,6 +68,8 @@ struct DetImage {
                          // copies (float32, any address); 0: plain loads
     int tma_align;       // element alignment of a TMA box's x coordinate (16 bytes)
     int tma_boxw;        // box width in elements (the halo row plus the alignment shift)
+    int wait_slot;       // 0: pixels ready at launch; g > 0: the copy engine is still bringing them in,
+                         // BatchParams::ready[g - 1] reads ready_epoch once they are complete
 };
 
 struct Scratch {
@@ -94,6 +99,8 @@ struct BatchParams {
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
     int hyb;             // 1: FP64 third-order vector and peak fit (TOED_HYBRID)
     int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
+    const int* ready;    // per copy group: ready_epoch once the group's images are in device memory
+    int ready_epoch;
     Scratch sc;
     DetImage img[kBatchMax];
 };

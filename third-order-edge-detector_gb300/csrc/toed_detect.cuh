@@ -470,6 +470,19 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
     }
 }
 
+// Bounded wait (one thread) until a copy group's ready flag reads `epoch`:
+// the copy engine writes the flag after the group's pixels, in stream order.
+static __device__ __noinline__ void wait_ready(const int* flag, int epoch, int* words)
+{
+    for (int it = 0; it < kReadySpinLimit; ++it) {
+        int v;
+        asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
+        if (v == epoch) return;
+        __nanosleep(256);
+    }
+    atomicOr(&words[2], TOED_FLAG_TIMEOUT);
+}
+
 // ASYNC: input rows by per-thread async copies (images with tma == 2) or
 // plain loads; otherwise by TMA (tma == 1) or plain loads.
 template <int R, bool HYB, bool ASYNC>
@@ -519,6 +532,10 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         if (u >= p.n_units) break;
         const int k = find_image(p.n_img, u, [&](int i) { return p.img[i].unit_base; });
         const DetImage& im = p.img[k];
+        if (im.wait_slot > 0) {  // pixels still arriving: wait for the group (uniform across the CTA)
+            if (tid == 0) wait_ready(p.ready + (im.wait_slot - 1), p.ready_epoch, p.sc.words);
+            __syncthreads();
+        }
         const void* src = im.src;
         const long long pitch = im.pitch;
         const int H = im.H, W = im.W, dtype = im.dtype;
