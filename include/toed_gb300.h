@@ -210,10 +210,11 @@ toed_status toed_detect_noalloc(const toed_image* image, const toed_params* para
  * :415-441) for a whole batch, pipelined: the batch is cut into `chunks`
  * groups of consecutive images, growing in pixel count, and the copy of
  * group k+1 to the device overlaps the detection of group k.  Page-locked
- * images: one detection launch for the whole batch whose CTAs wait (bounded)
- * for their group's copy, or with chunks == 1 no copy at all (the kernel
- * reads them in place through their device mapping).  Pageable images: one
- * launch per group (streams of the context, ordered by events).  Page-locked
+ * images, at most 64: one detection launch for the whole batch whose CTAs
+ * wait (bounded) for their group's copy; with chunks == 1 no copy at all
+ * (the kernel reads them in place through their device mapping).  Pageable
+ * images, or more than 64: one launch per group (streams of the context,
+ * ordered by events).  Page-locked
  * output buffers (edgels, count,
  * grid_index) are written by the detection's ordering pass directly through
  * their device mapping; pageable ones are filled by copies per group once its

@@ -695,7 +695,9 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         in_map[i] = mapped(const_cast<void*>(images[i].pixels));
         zin = in_map[i] != nullptr;
     }
-    const bool inplace = zin && chunks == 1, flagged = zin && chunks > 1;
+    // (flagged: one launch of at most kBatchMax images, so that nothing between
+    // the launch and the copies' enqueueing can wait for the device)
+    const bool inplace = zin && chunks == 1, flagged = zin && chunks > 1 && n <= kBatchMax;
     if (!inplace && (st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
     if (flagged) {
         const long long had = c->hb_ready_cap;
@@ -788,6 +790,7 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         std::vector<int> slot(n);
         for (int k = 0; k < chunks; ++k)
             for (int i = first[k]; i < first[k + 1]; ++i) slot[i] = k + 1;
+        TOED_HB(preload_finalize(radius_of(prm), prm->orientation == TOED_ORI_QAD));
         st = detect_all(c, dev.data(), n, prm, stream, nullptr, true, slot.data());
         if (st != TOED_OK) return fail(st);
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));

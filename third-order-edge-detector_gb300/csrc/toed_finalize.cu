@@ -193,6 +193,15 @@ __global__ void __launch_bounds__(kFinThreads) fin_scatter(const __grid_constant
     }
 }
 
+cudaError_t preload_finalize(int radius, bool qad)
+{
+    cudaFuncAttributes fa;
+    cudaError_t e = cudaFuncGetAttributes(&fa, (const void*)fin_tile_sums);
+    if (e == cudaSuccess) e = cudaFuncGetAttributes(&fa, (const void*)fin_tile_scan);
+    if (e == cudaSuccess) e = qad ? preload_scatter_qad(radius) : cudaFuncGetAttributes(&fa, (const void*)fin_scatter);
+    return e;
+}
+
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream)
 {
     void* args[] = {const_cast<BatchParams*>(&p)};

@@ -19,8 +19,14 @@ struct DetectEntry {
 DetectEntry detect_entry(int radius, bool hyb, bool async = false);
 
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
+// Load the ordering pass' kernels for `radius` (and the QaD variant) now:
+// with lazy module loading a kernel's first launch may wait for the device,
+// which must not happen while a detection launch waits for copies that the
+// host has yet to enqueue.
+cudaError_t preload_finalize(int radius, bool qad);
 // The ordering pass's last kernel in the TOED_ORI_QAD orientation mode (toed_qad.cu).
 cudaError_t launch_scatter_qad(const BatchParams& p, cudaStream_t stream);
+cudaError_t preload_scatter_qad(int radius);
 
 // Fill d.tma / d.tma_align / d.tma_boxw and encode the image's row map for
 // TMA staging (kStepRows-row boxes, zero fill outside the image).  Leaves

@@ -420,10 +420,10 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
     }
 }
 
-cudaError_t launch_scatter_qad(const BatchParams& p, cudaStream_t stream)
+static const void* scatter_qad_fn(int radius)
 {
     const void* f = nullptr;
-    switch (p.radius) {
+    switch (radius) {
     case 1: f = (const void*)fin_scatter_qad<1>; break;
     case 2: f = (const void*)fin_scatter_qad<2>; break;
     case 3: f = (const void*)fin_scatter_qad<3>; break;
@@ -436,8 +436,23 @@ cudaError_t launch_scatter_qad(const BatchParams& p, cudaStream_t stream)
     case 10: f = (const void*)fin_scatter_qad<10>; break;
     case 11: f = (const void*)fin_scatter_qad<11>; break;
     case 12: f = (const void*)fin_scatter_qad<12>; break;
-    default: return cudaErrorInvalidValue;
+    default: break;
     }
+    return f;
+}
+
+cudaError_t preload_scatter_qad(int radius)
+{
+    const void* f = scatter_qad_fn(radius);
+    if (!f) return cudaErrorInvalidValue;
+    cudaFuncAttributes fa;
+    return cudaFuncGetAttributes(&fa, f);
+}
+
+cudaError_t launch_scatter_qad(const BatchParams& p, cudaStream_t stream)
+{
+    const void* f = scatter_qad_fn(p.radius);
+    if (!f) return cudaErrorInvalidValue;
     void* args[] = {const_cast<BatchParams*>(&p)};
     return cudaLaunchKernel(f, dim3(p.n_tiles), dim3(kQadThreads), args, 0, stream);
 }
