@@ -332,6 +332,35 @@ def test_host_batch_flat_images(toed, synth, pin):
             assert t.equal(o["index"][:n], r["index"].cpu()), k
 
 
+@pytest.mark.parametrize("n,chunks", [(64, 16), (70, 5)])
+def test_host_batch_many_groups(toed, synth, n, chunks):
+    """Page-locked batches at the edges of the copy-group flow: 64 images over
+    16 groups (one launch, a ready flag per group, called twice so the second
+    call's epoch must not match the first call's flags) and 70 images (more
+    than one launch: groups launched one by one).  Lists equal the device
+    batch's bit for bit."""
+    t = _torch()
+    det = toed.Detector(0)
+    rng = np.random.default_rng(1700)
+    sizes = [(int(rng.integers(40, 200)), int(rng.integers(40, 200))) for _ in range(n)]
+    host = [t.as_tensor(synth.shapes_image(h, w, seed=1700 + k, n_shapes=3, radius_range=(8, 30),
+                                           dtype=np.float32 if k % 3 else np.uint8).image)
+            for k, (h, w) in enumerate(sizes)]
+    ref = det.detect_batch([im.cuda() for im in host], sigma=1.5)
+    pinned = [im.pin_memory() for im in host]
+    outs = det.alloc_host_outputs([tuple(im.shape) for im in host], index=True, pin=True)
+    plan = det.host_batch(pinned, outs)
+    for _ in range(2):
+        for o in outs:
+            o["count"].fill_(-1)
+        det.detect_host(plan, params=toed.make_params(1.5), chunks=chunks)
+        for k, (r, o) in enumerate(zip(ref, outs)):
+            c = int(o["count"].item())
+            assert c == r["count"], k
+            assert t.equal(o["edgels"][:c], r["edgels"].cpu()), k
+            assert t.equal(o["index"][:c], r["index"].cpu()), k
+
+
 @pytest.mark.parametrize("chunks", [1, 3])
 def test_host_batch_zero_copy_layouts(toed, synth, chunks):
     """Page-locked images, chunks == 1: read in place by the detection kernel

@@ -654,6 +654,9 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     std::vector<cudaEvent_t> ev_in(chunks, nullptr), ev_det(chunks, nullptr);
     std::vector<int> first(chunks + 1, n);
     auto fail = [&](toed_status s) {
+        // an early return must not leave copies in flight: the next call
+        // reuses the staging and rewrites the epoch their flag copies read
+        if (s != TOED_OK && c->s_in) cudaStreamSynchronize(c->s_in);
         for (auto e : ev_in)
             if (e) cudaEventDestroy(e);
         for (auto e : ev_det)
