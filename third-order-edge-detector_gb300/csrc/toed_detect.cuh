@@ -393,7 +393,8 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 
 // Per-edgel epilogue from a deferred record: peak fit (FP64 in HYB mode:
 // the cancellations in fm + fp - 2f and fp - fm) and the third-order
-// orientation (cpu_toed.cpp:227-232, FP64 in HYB mode), then the staged
+// orientation (cpu_toed.cpp:227-232; in HYB mode listed for the FP64
+// recomputation when the vector nearly cancels), then the staged
 // output record (x, y, orientation, strength) at its reserved slot.  The
 // record holds its image's index; W2 is that image's 2x-grid width.
 template <bool HYB>
@@ -426,15 +427,17 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         x = (double)(0.5f * (float)(Gc - 1)) + (double)(0.5f * sst * nx);
         y = (double)(0.5f * (float)(Gr - 1)) + (double)(0.5f * sst * ny);
         str = sqrtf((maxf * nx) * (maxf * nx) + (maxf * ny) * (maxf * ny));
-        // cpu_toed.cpp:227-232 with the shared products factored out (FP64):
+        // cpu_toed.cpp:227-232 with the shared products factored out, in FP32:
         // TIx = 2 (fx (fxx^2 + fxy^2) + fy fxy (fxx + fyy) + fx fy fxxy) + fy^2 fxyy + fx^2 fxxx
         // TIy = 2 (fx fxy (fxx + fyy) + fy (fyy^2 + fxy^2) + fx fy fxyy) + fx^2 fxxy + fy^2 fyyy
-        const double dfx = gx, dfy = gy, dxx = fxx, dxy = fxy, dyy = fyy;
-        const double a2 = dxx * dxx + dxy * dxy, c2 = dyy * dyy + dxy * dxy, bc = dxy * (dxx + dyy);
-        const double pxy = dfx * dfy, x2 = dfx * dfx, y2 = dfy * dfy;
-        const double tix = 2.0 * (dfx * a2 + dfy * bc + pxy * (double)fxxy) + y2 * (double)fxyy + x2 * (double)fxxx;
-        const double tiy = 2.0 * (dfx * bc + dfy * c2 + pxy * (double)fxyy) + x2 * (double)fxxy + y2 * (double)fyyy;
-        ori = (tix == 0.0 && tiy == 0.0) ? __int_as_float(0x7fc00000) : atan2f((float)tix, (float)(-tiy));
+        // Its own rounding reaches the angle times the cancellation ratio
+        // below (~1e-7 x ratio); the ill-conditioned vectors are recomputed
+        // in FP64 from FP64 derivatives, so FP64 here would buy nothing.
+        const float a2 = fmaf(fxx, fxx, fxy * fxy), c2 = fmaf(fyy, fyy, fxy * fxy), bc = fxy * (fxx + fyy);
+        const float pxy = gx * gy, x2 = gx * gx, y2 = gy * gy;
+        const float tixf = fmaf(2.f, fmaf(gx, a2, fmaf(gy, bc, pxy * fxxy)), fmaf(y2, fxyy, x2 * fxxx));
+        const float tiyf = fmaf(2.f, fmaf(gx, bc, fmaf(gy, c2, pxy * fxyy)), fmaf(x2, fxxy, y2 * fyyy));
+        ori = (tixf == 0.f && tiyf == 0.f) ? __int_as_float(0x7fc00000) : atan2f(tixf, -tiyf);
         // Cancellation ratio of the third-order vector: the sum of its terms'
         // magnitudes over its own size.  The FP32 derivative stack's rounding
         // reaches the orientation multiplied by this ratio, so edgels above
@@ -443,7 +446,7 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         const float sabs = 2.f * ax * (fxx * fxx + fxy * fxy) + 2.f * ay * (fyy * fyy + fxy * fxy) +
                            2.f * (ax + ay) * (pxx + pyy) + 2.f * ax * ay * (fabsf(fxxy) + fabsf(fxyy)) +
                            ay * ay * (fabsf(fxyy) + fabsf(fyyy)) + ax * ax * (fabsf(fxxx) + fabsf(fxxy));
-        const float tmax = fmaxf(fabsf((float)tix), fabsf((float)tiy));
+        const float tmax = fmaxf(fabsf(tixf), fabsf(tiyf));
         if (sabs > kRefineKappa * tmax && sc.refine_cap > 0 && dst < sc.staging_cap) {
             const int slot = atomicAdd(&sc.words[3], 1);
             if (slot < sc.refine_cap) sc.refine[slot] = make_int4(dst, img, Gr, Gc);

@@ -24,8 +24,9 @@
 //      each point row's y taps (lane-local) and accumulates the nine
 //      interpolated derivatives;
 //   4. sums the nine values over the lanes (butterfly) and parks them; after
-//      32 records lane e forms record e's third-order vector (FP64 in HYBRID
-//      precision, all lanes busy), the angle and the output record.
+//      32 records lane e forms record e's third-order vector, the angle and
+//      the output record; in HYBRID precision the records whose vector nearly
+//      cancels are first contracted again in FP64 by the whole warp.
 #include "toed_common.cuh"
 #include "toed_internal.h"
 
@@ -374,8 +375,11 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
                     fxyy = mine[6], fxxx = mine[7], fyyy = mine[8];
         float ori;
         if (p.hyb) {
-            double tix, tiy;
-            to_vector(mine, tix, tiy);
+            // FP32 vector; the ill-conditioned ones are redone in FP64 below
+            const float a2 = fmaf(fxx, fxx, fxy * fxy), c2 = fmaf(fyy, fyy, fxy * fxy), bc = fxy * (fxx + fyy);
+            const float pxy = gx * gy, x2 = gx * gx, y2 = gy * gy;
+            double tix = fmaf(2.f, fmaf(gx, a2, fmaf(gy, bc, pxy * fxxy)), fmaf(y2, fxyy, x2 * fxxx));
+            double tiy = fmaf(2.f, fmaf(gx, bc, fmaf(gy, c2, pxy * fxyy)), fmaf(x2, fxxy, y2 * fyyy));
             // Records whose vector cancels by more than kRefineKappa (sum of
             // the terms' magnitudes over the largest component) carry the FP32
             // contraction's rounding multiplied by that ratio: the warp
