@@ -3,6 +3,7 @@
 // scratch owned by a context, strip planning and kernel launches.
 #include <algorithm>
 #include <cmath>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -610,6 +611,23 @@ extern "C" toed_status toed_detect(toed_ctx* c, const toed_image* image, const t
     return toed_detect_batch(c, image, 1, prm, stream);
 }
 
+// Launches run one at a time, each waited for: CUDA_LAUNCH_BLOCKING=1, or a
+// tool injected into the runtime (profilers and checkers serialise work).
+// (Nsight Compute marks its target process with NV_NSIGHT_INJECTION_* and
+// NV_COMPUTE_PROFILER_PERFWORKS_DIR; runtime-injected tools with
+// CUDA_INJECTION64_PATH.)
+static bool launches_serialised()
+{
+    const char* lb = std::getenv("CUDA_LAUNCH_BLOCKING");
+    if (lb && lb[0] == '1') return true;
+    for (const char* v : {"CUDA_INJECTION64_PATH", "NV_NSIGHT_INJECTION_TRANSPORT_TYPE",
+                          "NV_COMPUTE_PROFILER_PERFWORKS_DIR"}) {
+        const char* e = std::getenv(v);
+        if (e && e[0]) return true;
+    }
+    return false;
+}
+
 // Host-memory batch, pipelined over `chunks` groups of images (see the
 // header).  Streams: s_in (H2D), the caller's stream (detection), s_out
 // (D2H, pageable outputs only); events order them per group.
@@ -699,8 +717,12 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         zin = in_map[i] != nullptr;
     }
     // (flagged: one launch of at most kBatchMax images, so that nothing between
-    // the launch and the copies' enqueueing can wait for the device)
-    const bool inplace = zin && chunks == 1, flagged = zin && chunks > 1 && n <= kBatchMax;
+    // the launch and the copies' enqueueing can wait for the device; never
+    // when launches run serialised -- CUDA_LAUNCH_BLOCKING, or a profiler or
+    // checker injected into the runtime -- since then the waiting launch
+    // would hold the host or the device until its wait gives up)
+    const bool inplace = zin && chunks == 1,
+               flagged = zin && chunks > 1 && n <= kBatchMax && !launches_serialised();
     if (!inplace && (st = grow(&c->hb_in, &c->hb_in_cap, std::max(in_b, 1LL), stream)) != TOED_OK) return fail(st);
     if (flagged) {
         const long long had = c->hb_ready_cap;
