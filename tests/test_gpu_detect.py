@@ -361,6 +361,34 @@ def test_host_batch_many_groups(toed, synth, n, chunks):
             assert t.equal(o["index"][:c], r["index"].cpu()), k
 
 
+def test_host_batch_serialised_launches(toed):
+    """With CUDA_LAUNCH_BLOCKING=1 a launch returns only when it is done, so
+    the copy-group flow, whose launch waits for copies enqueued after it,
+    must not be used: the call falls back to per-group launches and returns
+    the same lists promptly (a fresh process: the variable is read there)."""
+    import subprocess
+    import sys
+    code = (
+        "import sys, time; sys.path.insert(0, {tests!r}); from conftest import load_package\n"
+        "toed = load_package(); import importlib, torch, numpy as np\n"
+        "synth = importlib.import_module('toed_gb300.synth'); det = toed.Detector(0)\n"
+        "ims = [torch.as_tensor(synth.shapes_image(120 + 9 * k, 150, seed=1800 + k, dtype=np.float32).image)"
+        " for k in range(5)]\n"
+        "ref = det.detect_batch([im.cuda() for im in ims], sigma=1.5)\n"
+        "outs = det.alloc_host_outputs([tuple(im.shape) for im in ims], pin=True)\n"
+        "t0 = time.time(); det.detect_host([im.pin_memory() for im in ims], outs, toed.make_params(1.5), chunks=3)\n"
+        "dt = time.time() - t0\n"
+        "ok = all(int(o['count'].item()) == r['count'] and torch.equal(o['edgels'][:r['count']], r['edgels'].cpu())"
+        " for o, r in zip(outs, ref))\n"
+        "print('RESULT', ok, dt)\n"
+    ).format(tests=os.path.dirname(os.path.abspath(__file__)))
+    env = dict(os.environ, CUDA_LAUNCH_BLOCKING="1")
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600, env=env)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("RESULT")][-1].split()
+    assert line[1] == "True" and float(line[2]) < 2.0, line
+
+
 @pytest.mark.parametrize("chunks", [1, 3])
 def test_host_batch_zero_copy_layouts(toed, synth, chunks):
     """Page-locked images, chunks == 1: read in place by the detection kernel
