@@ -543,7 +543,7 @@ def run_ours(args, ws, rank, local):
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mpixel/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 per-edgel fit and TO orientation)",
+        "vs_baseline": None, "dtype": "f32 (FP64 per-edgel peak fit; FP64 TO orientation where the vector cancels)",
         "data": "synthetic (seeded shapes generator; inputs 318 MB > L2, no flush needed)",
         "config": {"workload": "uneven batch: 64 float32 images, H and W U[256,2048] (x4), noise U[1,8]",
                    "launch": "one CUDA graph per step (persistent detection kernel + 3-kernel ordering pass)",

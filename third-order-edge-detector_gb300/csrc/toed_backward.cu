@@ -9,7 +9,7 @@
 //      of its (frozen) sector, each with its d/dsigma (one pass over the
 //      union window of the five points, coalesced rows);
 //   2. a thread per edgel runs the chain rule through the peak fit and the
-//      third-order orientation (FP64 where the forward needs it) and
+//      third-order orientation (the peak fit's sums and the vector in FP64) and
 //      accumulates dL/dsigma;
 //   3. a warp per edgel adds the separable cotangent windows
 //      sum_f X_f(q) V_f(p) of its five points onto the pixel gradient with

@@ -97,7 +97,7 @@ struct BatchParams {
     int out_f64;
     int radius;
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
-    int hyb;             // 1: FP64 third-order vector and peak fit (TOED_HYBRID)
+    int hyb;             // 1: FP64 peak fit, FP64 recomputation of ill-conditioned orientations (TOED_HYBRID)
     int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
     const int* ready;    // per copy group: ready_epoch once the group's images are in device memory
     int ready_epoch;
