@@ -211,8 +211,13 @@ toed_status toed_detect_noalloc(const toed_image* image, const toed_params* para
  * groups of consecutive images, growing in pixel count, and the copy of
  * group k+1 to the device overlaps the detection of group k.  Page-locked
  * images, at most 64: one detection launch for the whole batch whose CTAs
- * wait (bounded) for their group's copy; with chunks == 1 no copy at all
- * (the kernel reads them in place through their device mapping).  Pageable
+ * wait (bounded) for their group's copy, which the call enqueues right after
+ * the launch -- another host thread that waits for the whole device in that
+ * moment (cudaDeviceSynchronize, cudaFree) can hold those copies back until
+ * the wait gives up (TOED_ERR_TIMEOUT), so serialise such calls; with
+ * CUDA_LAUNCH_BLOCKING or under a profiler this flow is not used.  With
+ * chunks == 1 no copy at all (the kernel reads them in place through their
+ * device mapping).  Pageable
  * images, or more than 64: one launch per group (streams of the context,
  * ordered by events).  Page-locked
  * output buffers (edgels, count,
