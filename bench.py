@@ -43,7 +43,7 @@ sys.path.insert(0, ROOT)
 
 SIGMA, THRESH, N_IMAGES, SEED0 = 1.5, 2.0, 64, 3000
 E2E_CHUNKS = 16  # image groups the host-buffer path pipelines its copies over
-REF_SECONDS = 120.0  # CPU time the reference arm spends on warm-up plus timed steps
+REF_SAMPLE_IMAGES = 4  # the CPU reference's per-step sample: the batch's first four images (5.50 Mpixel)
 METRIC = "Mpixel/s (TOED fused forward, uneven batch of 64 float32 images, sigma 1.5)"
 
 
@@ -75,19 +75,66 @@ def make_batch(seed0: int, n: int = N_IMAGES, procs: int | None = None):
 
 
 class ClockSampler:
-    """nvidia-smi sampling of SM clocks and throttle reasons during a region."""
+    """SM clocks and throttle reasons sampled DURING a timed region: NVML
+    through ctypes every 5 ms on a thread (so a region of ~50 ms still gets
+    about ten samples), else nvidia-smi at its 50 ms loop."""
 
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
          "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
          "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+    # nvmlClocksEventReason* bits (nvml.h)
+    BITS = {"sw_power_cap": 0x4, "hw_slowdown": 0x8, "sw_thermal_slowdown": 0x20, "hw_thermal_slowdown": 0x40}
+    PERIOD_S = 0.005
 
     def __init__(self, gpu_index: int):
         self.gpu = gpu_index
         self.proc = None
         self.f = None
+        self.thread = None
+        self.samples = []
+        self.source = None
+
+    def _nvml(self):
+        import ctypes
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+        except OSError:
+            return None
+        h = ctypes.c_void_p()
+        if nv.nvmlInit_v2() != 0 or nv.nvmlDeviceGetHandleByIndex_v2(self.gpu, ctypes.byref(h)) != 0:
+            return None
+        mx = ctypes.c_uint(0)
+        if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) != 0:  # NVML_CLOCK_SM
+            return None
+        reasons = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons", None) or \
+            nv.nvmlDeviceGetCurrentClocksThrottleReasons
+        return nv, h, mx.value, reasons
 
     def start(self):
+        import threading
+        got = None
         try:
+            got = self._nvml()
+        except Exception:
+            got = None
+        if got is not None:
+            import ctypes
+            nv, h, mx, reasons = got
+            self.stop_evt = threading.Event()
+            self.source = "nvml"
+
+            def loop():
+                c, r = ctypes.c_uint(0), ctypes.c_ulonglong(0)
+                while not self.stop_evt.is_set():
+                    if nv.nvmlDeviceGetClockInfo(h, 1, ctypes.byref(c)) == 0 and reasons(h, ctypes.byref(r)) == 0:
+                        self.samples.append((float(c.value), float(mx), int(r.value)))
+                    time.sleep(self.PERIOD_S)
+
+            self.thread = threading.Thread(target=loop, daemon=True)
+            self.thread.start()
+            return
+        try:
+            self.source = "nvidia-smi"
             self.f = tempfile.TemporaryFile(mode="w+")
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
                                           "--format=csv,noheader,nounits", "-lms", "50"],
@@ -96,30 +143,36 @@ class ClockSampler:
             self.proc = None
 
     def stop(self):
-        if self.proc is None:
-            return None
-        self.proc.terminate()
-        try:
-            self.proc.wait(timeout=5)
-        except Exception:
-            self.proc.kill()
-        self.f.seek(0)
-        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
         sm, mx, reasons = [], [], set()
-        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for r in rows:
+        if self.thread is not None:
+            self.stop_evt.set()
+            self.thread.join(timeout=5)
+            for c, m, r in self.samples:
+                sm.append(c)
+                mx.append(m)
+                reasons.update(nm for nm, b in self.BITS.items() if r & b)
+        elif self.proc is not None:
+            self.proc.terminate()
             try:
-                sm.append(float(r[1]))
-                mx.append(float(r[2]))
-                for nm, v in zip(names, r[5:9]):
-                    if "Active" in v and "Not" not in v:
-                        reasons.add(nm)
-            except (ValueError, IndexError):
-                continue
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+            self.f.seek(0)
+            rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+            names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+            for r in rows:
+                try:
+                    sm.append(float(r[1]))
+                    mx.append(float(r[2]))
+                    for nm, v in zip(names, r[5:9]):
+                        if "Active" in v and "Not" not in v:
+                            reasons.add(nm)
+                except (ValueError, IndexError):
+                    continue
         if not sm:
             return None
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": self.source}
 
 
 def dist_init():
@@ -156,14 +209,15 @@ def barrier(ws: int):
 
 
 def cpu_oracle_rate(images, seconds: float, threads: int):
-    """Oracle (reference FP64 CPU path restated) over whole images until
-    ``seconds`` elapse; returns (Mpixel/s, pixels, images)."""
+    """Oracle (reference FP64 CPU path restated) over the sample images,
+    repeated until ``seconds`` elapse; returns (Mpixel/s, pixels, passes, s)."""
     import oracle
     oracle.build()
     px, t0, n = 0, time.perf_counter(), 0
-    for im in images:
-        oracle.detect(im.astype(np.float64), SIGMA, threshold=THRESH, nthreads=threads)
-        px += im.size
+    while True:
+        for im in images:
+            oracle.detect(im.astype(np.float64), SIGMA, threshold=THRESH, nthreads=threads)
+            px += im.size
         n += 1
         if time.perf_counter() - t0 >= seconds:
             break
@@ -171,43 +225,89 @@ def cpu_oracle_rate(images, seconds: float, threads: int):
     return px / dt / 1e6, px, n, dt
 
 
+def ref_sample(images):
+    """The CPU reference's bounded sample of the batch, the same for the
+    reference arm and the cpu_baseline leg: the first REF_SAMPLE_IMAGES whole
+    images of the batch (5.50 Mpixel of its 79.42)."""
+    return images[:REF_SAMPLE_IMAGES]
+
+
+def reference_build_crosscheck(threads: int):
+    """The reference's own CPU class (ThirdOrderEdgeDetectionCPU<double>,
+    cpu_toed.cpp, built on this host by oracle/Makefile `ref`) beside the
+    oracle port, both on the 752x480 uint8 image at sigma 2 / kernel 17 --
+    the only configuration the reference's literal taps and byte input
+    allow -- so that the port's speed is anchored to the reference's.
+    Median of three runs after one warm-up; None where it is not built."""
+    import oracle
+    if not oracle.ref_available():
+        try:
+            if oracle.ref_sources_present():
+                oracle.build(ref=True)
+        except Exception:
+            pass
+    if not oracle.ref_available():
+        return None
+    img = _gen_shapes((480, 752, 1, "u8", False))
+    lit = oracle.taps(2.0, 8)
+    t_ref, t_port, t_conv_nms = [], [], []
+    n_ref = n_port = 0
+    for rep in range(4):
+        t0 = time.perf_counter()
+        r = oracle.ref_detect_u8(img, nthreads=threads)
+        t1 = time.perf_counter()
+        o = oracle.detect(img.astype(np.float64), 2.0, 8, tap_block=lit, nthreads=threads)
+        t2 = time.perf_counter()
+        if rep:
+            t_ref.append(t1 - t0)
+            t_port.append(t2 - t1)
+            t_conv_nms.append((r["time_conv"] + r["time_nms"]))
+        n_ref, n_port = len(r["edges"]), len(o["edges"])
+    px = img.size
+    return {"config": "752x480 uint8, sigma 2, kernel 17", "threads": threads,
+            "reference_mpx_s": round(px / float(np.median(t_ref)) / 1e6, 3),
+            "reference_conv_nms_mpx_s": round(px / float(np.median(t_conv_nms)) / 1e6, 3),
+            "port_mpx_s": round(px / float(np.median(t_port)) / 1e6, 3),
+            "edgels": [n_ref, n_port]}
+
+
 def run_reference(args, ws, rank):
     """Reference arm: the reference's CPU path (FP64, OpenMP) on all host
-    cores, each step a bounded sample of the batch (crops of its first image)
-    sized so that warm-up plus timed steps take about two minutes."""
+    cores, each step the same fixed sample of the batch as the cpu_baseline
+    leg of our arm (its first four images, whole).  The reference's own
+    build reads uint8 at sigma 2 only, so the timed code is the oracle port
+    of that path on the exact float32 / sigma 1.5 workload; a cross-check
+    line times the reference's own build beside the port where they can
+    both run."""
     if rank != 0:
         return
     import oracle
     oracle.build()
-    # the reference's own build reads uint8 at sigma 2 only, so the timed
-    # restatement of its path runs the exact float32 / sigma 1.5 workload
     kind = "port"
     threads = os.cpu_count() or 1
-    img = make_batch(SEED0, n=1, procs=1)[0].astype(np.float64)
-    probe = img[:256, :256]
-    t0 = time.perf_counter()
-    oracle.detect(probe, SIGMA, threshold=THRESH, nthreads=threads)
-    rate = probe.size / (time.perf_counter() - t0)
-    budget_px = rate * REF_SECONDS / (args.steps + args.warmup)
-    side = int(max(128, min(img.shape[0], img.shape[1], math.sqrt(max(budget_px, 1.0)))))
-    crop = np.ascontiguousarray(img[:side, :side])
+    sample = [im.astype(np.float64) for im in ref_sample(make_batch(SEED0, n=REF_SAMPLE_IMAGES,
+                                                                    procs=REF_SAMPLE_IMAGES))]
+    spx = sum(im.size for im in sample)
     times = []
     for s in range(args.warmup + args.steps):
         t0 = time.perf_counter()
-        oracle.detect(crop, SIGMA, threshold=THRESH, nthreads=threads)
+        for im in sample:
+            oracle.detect(im, SIGMA, threshold=THRESH, nthreads=threads)
         if s >= args.warmup:
             times.append(time.perf_counter() - t0)
     dt = float(sum(times))
-    v = crop.size * args.steps / dt / 1e6
-    sample = f"{side}x{side} crop of batch image 0 per step (FP64 restatement of ThirdOrderEdgeDetectionCPU<double>)"
+    v = spx * args.steps / dt / 1e6
+    desc = (f"first {len(sample)} images of the batch per step ({spx / 1e6:.2f} Mpixel, whole images; "
+            "FP64 restatement of ThirdOrderEdgeDetectionCPU<double> on all host cores)")
     line = {
         "metric": METRIC, "impl": "reference", "value": round(v, 4), "unit": "Mpixel/s", "n_gpus": ws,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1e3 * dt / args.steps, 3),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": "uneven batch: 64 float32 images, H and W U[256,2048] (x4), noise U[1,8]",
-                   "sigma": SIGMA, "threshold": THRESH, "sample": sample},
-        "cpu_baseline": {"value": round(v, 4), "unit": "Mpixel/s", "cores": threads, "kind": kind, "sample": sample},
+                   "sigma": SIGMA, "threshold": THRESH, "sample": desc},
+        "cpu_baseline": {"value": round(v, 4), "unit": "Mpixel/s", "cores": threads, "kind": kind, "sample": desc},
         "e2e": {"value": round(v, 4), "unit": "Mpixel/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "reference_build_crosscheck": reference_build_crosscheck(threads),
     }
     print(json.dumps(line), flush=True)
 
@@ -250,6 +350,65 @@ def _time_ms(fn, reps, stream):
     e1.record(stream)
     e1.synchronize()
     return e0.elapsed_time(e1) / reps
+
+
+def reference_gpu_form(toed, det, images, side, stream, ours_c1_sigma2):
+    """The reference's own plain single-image GPU form on this GPU: its class
+    ThirdOrderEdgeDetectionGPU<float> with gpu_convolve_kernel and
+    gpu_nms_kernel compiled unchanged for sm_103a (oracle/_ref/libref_gpu.so),
+    driven as the reference drives them (gpu_toed.hpp:340-441).  Its fixed
+    configuration is sigma 2 / kernel 17 on uint8 input, so it runs on the
+    752x480 uint8 image and on the 64 batch images rounded to uint8, image
+    by image; the batched path runs the same uint8 images at sigma 2 beside
+    it.  'kernels' = the class's own CUDA-event times of its two kernels;
+    'call' = wall time of convolve_img + non_maximum_suppresion (copies,
+    both kernels, plane read-backs, host edgel list and the text file the
+    reference writes)."""
+    import torch
+    import oracle
+    if not oracle.refgpu_available():
+        try:
+            if oracle.ref_sources_present():
+                oracle.build(refgpu=True)
+        except Exception as e:  # reported in the line
+            return {"unavailable": f"reference GPU build failed: {str(e)[:200]}"}
+    if not oracle.refgpu_available():
+        return {"unavailable": "the reference's sources are not on this host (no checkout, no baseline/_ref/src copy)"}
+    dev = torch.device("cuda", torch.cuda.current_device())
+    res = {}
+    c1 = side["c1"]
+    r = oracle.ref_gpu_detect_u8(c1, reps=5, device=dev.index)
+    k1, w1 = float(np.median(r["kernel_ms"])), float(np.median(r["call_ms"]))
+    ours = det.detect(torch.as_tensor(c1).to(dev), sigma=2.0)
+    oe = ours["edgels"].double().cpu().numpy()
+    from scipy.spatial import cKDTree
+    d, _ = cKDTree(oe[:, :2]).query(r["edges"][:, :2].astype(np.float64), k=1)
+    res["single_752x480_u8_sigma2"] = {
+        "reference_kernels_ms": round(k1, 4), "reference_call_ms": round(w1, 3),
+        "reference_kernels_mpx_s": round(c1.size / (k1 * 1e-3) / 1e6, 1),
+        "reference_call_mpx_s": round(c1.size / (w1 * 1e-3) / 1e6, 2),
+        "ours_mpx_s": ours_c1_sigma2,
+        "edgels_reference": int(len(r["edges"])), "edgels_ours": int(ours["count"]),
+        "reference_edgels_within_2e-3px_of_ours": round(float(np.mean(d <= 2e-3)), 5)}
+    u8 = [np.clip(np.rint(im), 0, 255).astype(np.uint8) for im in images]
+    kt = wt = 0.0
+    for im in u8:
+        rr = oracle.ref_gpu_detect_u8(im, reps=1, device=dev.index)
+        kt += rr["kernel_ms"][0]
+        wt += rr["call_ms"][0]
+    npx = sum(im.size for im in u8)
+    d_u8 = [torch.as_tensor(im).to(dev) for im in u8]
+    o_u8 = det.alloc_outputs([im.shape for im in u8], None, index=False)
+    p2 = toed.make_params(2.0, 0, THRESH)
+    bms = _time_ms(lambda: det.detect_into(d_u8, o_u8, p2, stream), 5, stream)
+    res["batch64_u8_sigma2"] = {
+        "reference_kernels_mpx_s": round(npx / (kt * 1e-3) / 1e6, 1),
+        "reference_call_mpx_s": round(npx / (wt * 1e-3) / 1e6, 2),
+        "ours_batched_mpx_s": round(npx / (bms * 1e-3) / 1e6, 1),
+        "batched_over_reference_kernels": round(kt / bms, 2),
+        "batched_over_reference_call": round(wt / bms, 1)}
+    del d_u8, o_u8
+    return res
 
 
 def side_measurements(toed, det, images, side, stream):
@@ -295,6 +454,8 @@ def side_measurements(toed, det, images, side, stream):
     dms = _time_ms(lambda: dense_form(L.toed_convolve_planes), 2, stream)
     out["dense_two_kernel_form_mpx_s"] = round(npx / (dms * 1e-3) / 1e6, 1)
     del planes
+    out["reference_gpu_kernels"] = reference_gpu_form(toed, det, images, side, stream,
+                                                       out.get("single_752x480_u8_sigma2_mpx_s"))
     # -- the MATLAB quick-and-dirty orientation mode on the same batch ------
     pq = toed.make_params(SIGMA, 0, THRESH, orientation=toed.TOED_ORI_QAD)
     qms = _time_ms(lambda: det.detect_into(d_imgs, outs, pq, stream), 3, stream)
@@ -575,10 +736,12 @@ def run_ours(args, ws, rank, local):
         line["other_configs"] = side_measurements(toed, det, images, side, stream)
     if rank == 0 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        v, px, n, dt = cpu_oracle_rate(images, args.cpu_seconds, threads)
+        samp = ref_sample(images)
+        v, px, n, dt = cpu_oracle_rate(samp, args.cpu_seconds, threads)
         line["cpu_baseline"] = {"value": round(v, 4), "unit": "Mpixel/s", "cores": threads, "kind": "port",
-                                "sample": f"first {n} of the batch images ({px / 1e6:.2f} Mpixel), "
-                                          f"FP64 oracle restatement of the reference OpenMP path, {dt:.1f} s"}
+                                "sample": f"first {len(samp)} images of the batch, whole "
+                                          f"({sum(im.size for im in samp) / 1e6:.2f} Mpixel) x {n} passes, FP64 "
+                                          f"oracle restatement of the reference OpenMP path, {dt:.1f} s"}
     if rank == 0:
         print(json.dumps(line), flush=True)
 

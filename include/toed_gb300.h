@@ -190,16 +190,20 @@ toed_status toed_subpix_to_correct_batch(toed_ctx* ctx, const toed_edgemap* maps
  * forbid allocation after start-up, plug-in hosts that hand out only
  * pre-sized buffers -- and therefore cannot use a toed_ctx, whose scratch
  * grows on demand.  One image per call on the current device; the caller
- * passes the image and the output buffers as for toed_detect.  The scratch
- * is a fixed array compiled into the library (about 11 MB, reserved on every
- * GPU that loads the library until the process exits).  The first call on a
- * device looks up that array's device address, so make the first call
- * before any stream capture.  Images above TOED_NOALLOC_MAX_DIM rows or
- * columns or TOED_NOALLOC_MAX_PIXELS pixels, or a capacity above
+ * passes the image and the output buffers as for toed_detect, and the same
+ * image checks apply.  The scratch is a fixed array compiled into the
+ * library (about 11 MB).  The CUDA runtime loads it lazily: the first call
+ * on a device reserves it there (until the process exits) and looks up its
+ * device address, so make that first call at start-up, before a pool or
+ * arena claims the device's memory (else TOED_ERR_CUDA) and before any
+ * stream capture.  Images above TOED_NOALLOC_MAX_DIM rows or columns or
+ * TOED_NOALLOC_MAX_PIXELS pixels, or a capacity above
  * TOED_NOALLOC_MAX_EDGELS, return TOED_ERR_CAPACITY.  All calls share the
  * array: calls that overlap on the GPU (other streams or host threads on the
  * same device) race and must be serialised by the caller.  If the image has
- * more edgels than `capacity`, count is exact and the list is incomplete. */
+ * more edgels than `capacity`, count is exact but the contents of edgels
+ * and grid_index are undefined (entries may be missing or hold an earlier
+ * call's data): size the capacity for the image, (2H)(2W) at most. */
 #define TOED_NOALLOC_MAX_DIM 4096
 #define TOED_NOALLOC_MAX_PIXELS (2048LL * 2048LL)
 #define TOED_NOALLOC_MAX_EDGELS 262144

@@ -38,11 +38,51 @@ def _ptr(a):
     return None if a is None else a.ctypes.data_as(_dp)
 
 
-def build(ref: bool = False) -> None:
-    """Compile liboracle.so (and, if ``ref``, the reference build)."""
+REF_COPY = os.path.abspath(os.path.join(_HERE, "..", "baseline", "_ref", "src"))
+
+
+def _has_sources(d) -> bool:
+    return bool(d) and os.path.exists(os.path.join(d, "cpu_toed.cpp")) and \
+        os.path.exists(os.path.join(d, "gpu_convolve.cu"))
+
+
+def checkout_dir() -> str:
+    """The reference checkout: the TOED_REF_DIR environment variable, else
+    the recipe's default (may not exist on this host)."""
+    env = os.environ.get("TOED_REF_DIR")
+    if env:
+        return env
+    r = subprocess.run(["make", "-s", "-C", _HERE, "refdir"], capture_output=True, text=True)
+    return r.stdout.strip()
+
+
+def ref_dir() -> str:
+    """Where the reference builds read the reference's sources: the checkout
+    where it exists, else the git-ignored copy baseline/_ref/src that
+    ``make -C oracle refsrc`` made from it (it travels with the working tree
+    to hosts that have no checkout)."""
+    d = checkout_dir()
+    return d if _has_sources(d) else REF_COPY
+
+
+def ref_sources_present() -> bool:
+    """True where the reference's sources can be compiled: its checkout, or
+    the copy of its files in baseline/_ref/src."""
+    return _has_sources(ref_dir())
+
+
+def build(ref: bool = False, refgpu: bool = False) -> None:
+    """Compile liboracle.so; with ``ref`` the reference's own CPU classes,
+    with ``refgpu`` its GPU class and kernels (oracle/_ref).  Where the
+    checkout exists, its files are first copied to baseline/_ref/src."""
     subprocess.run(["make", "-s", "-C", _HERE], check=True)
-    if ref:
-        subprocess.run(["make", "-s", "-C", _HERE, "ref"], check=True)
+    if not (ref or refgpu):
+        return
+    d = ref_dir()
+    if d != REF_COPY:
+        subprocess.run(["make", "-s", "-C", _HERE, "refsrc", f"REF_DIR={d}"], check=True)
+    targets = (["ref"] if ref else []) + (["refgpu"] if refgpu else [])
+    subprocess.run(["make", "-s", "-j4", "-C", _HERE] + targets + [f"REF_DIR={d}"], check=True)
 
 
 def lib():
@@ -214,6 +254,45 @@ def ref_detect_u8(img_u8, nthreads: int = 0, planes: bool = False):
     out = {"edges": edges[:n].copy(), "time_conv": t[0], "time_nms": t[1]}
     if planes:
         out["planes"], out["posmaps"] = pl, pm
+    return out
+
+
+def refgpu_available() -> bool:
+    return os.path.exists(os.path.join(_HERE, "_ref", "libref_gpu.so"))
+
+
+_REFGPU = None
+
+
+def ref_gpu_detect_u8(img_u8, reps: int = 3, device: int = 0, planes: bool = False):
+    """The reference's own GPU class ThirdOrderEdgeDetectionGPU<float>
+    (sigma 2, kernel 17; gpu_convolve + gpu_nms compiled for sm_103a) on
+    one uint8 image.  Returns dict(edges=(N,4) float32, kernel_ms=[...],
+    call_ms=[...] [, planes=(4,2H,2W) float32 Ix/Iy/mag/orientation]) --
+    per repetition the class's own kernel event times and the wall time of
+    its convolve_img + non_maximum_suppresion calls."""
+    global _REFGPU
+    if _REFGPU is None:
+        L = ctypes.CDLL(os.path.join(_HERE, "_ref", "libref_gpu.so"))
+        L.ref_gpu_detect_u8.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_char_p,
+                                        ctypes.c_int, ctypes.c_void_p, ctypes.c_long, _dp, ctypes.c_void_p]
+        L.ref_gpu_detect_u8.restype = ctypes.c_long
+        _REFGPU = L
+    img = np.ascontiguousarray(img_u8, dtype=np.uint8)
+    H, W = img.shape
+    cap = 4 * H * W
+    edges = np.zeros((cap, 4), np.float32)
+    t = np.zeros(3 * reps)
+    pl = np.zeros((4, 2 * H, 2 * W), np.float32) if planes else None
+    with tempfile.TemporaryDirectory() as d:
+        n = _REFGPU.ref_gpu_detect_u8(img.ctypes.data, H, W, int(device), d.encode(), int(reps),
+                                      edges.ctypes.data, cap, _ptr(t), pl.ctypes.data if planes else None)
+    if n < 0:
+        raise RuntimeError("reference GPU harness IO error")
+    t = t.reshape(reps, 3)
+    out = {"edges": edges[:n].copy(), "kernel_ms": t[:, 0].tolist(), "call_ms": t[:, 1].tolist()}
+    if planes:
+        out["planes"] = pl
     return out
 
 

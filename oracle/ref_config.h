@@ -1,6 +1,7 @@
 /*
  * ref_config.h -- forced-include configuration for compiling the reference's
- * CPU sources where they lie (TEST INFRASTRUCTURE ONLY; see oracle/Makefile).
+ * CPU and GPU sources (TEST AND MEASUREMENT INFRASTRUCTURE ONLY; see
+ * oracle/Makefile).
  *
  * The reference configures itself through indices.hpp (indices.hpp:5-15),
  * whose switches are unconditional #defines (OpenCV and curvelets on).  This
@@ -31,5 +32,14 @@
 #define subpix_grad_mag_map(i, j) subpix_grad_mag_map[(i)*interp_img_width + (j)]
 #define subpix_edge_pts_final(i, j) subpix_edge_pts_final[(i)*num_of_edge_data + (j)]
 #define TOED_edges(i, j) TOED_edges[(i)*4 + (j)]
+
+/* device-plane accessors of the reference's GPU sources (indices.hpp:30-37) */
+#define dev_img(i, j) dev_img[(i)*img_width + (j)]
+#define dev_Ix(i, j) dev_Ix[(i)*interp_img_width + (j)]
+#define dev_Iy(i, j) dev_Iy[(i)*interp_img_width + (j)]
+#define dev_I_grad_mag(i, j) dev_I_grad_mag[(i)*interp_img_width + (j)]
+#define dev_I_orient(i, j) dev_I_orient[(i)*interp_img_width + (j)]
+#define dev_subpix_pos_x_map(i, j) dev_subpix_pos_x_map[(i)*interp_img_width + (j)]
+#define dev_subpix_pos_y_map(i, j) dev_subpix_pos_y_map[(i)*interp_img_width + (j)]
 
 #endif

@@ -22,6 +22,9 @@
 #include <algorithm>
 #include <unordered_map>
 
+#include <fcntl.h>
+#include <unistd.h>
+
 // Read access to the intermediate planes for plane-level pinning (both
 // classes keep them in their implicit private sections).
 #define class struct
@@ -30,6 +33,34 @@
 #include "subpix_to_correction.hpp"
 #undef private
 #undef class
+
+// The reference classes print progress lines to stdout; each entry point
+// sends them to /dev/null so that a caller's own stdout stays parseable.
+namespace {
+struct QuietStdout {
+    int saved = -1;
+    QuietStdout()
+    {
+        std::fflush(stdout);
+        std::cout.flush();
+        saved = dup(1);
+        const int nul = open("/dev/null", O_WRONLY);
+        if (nul >= 0) {
+            dup2(nul, 1);
+            close(nul);
+        }
+    }
+    ~QuietStdout()
+    {
+        std::fflush(stdout);
+        std::cout.flush();
+        if (saved >= 0) {
+            dup2(saved, 1);
+            close(saved);
+        }
+    }
+};
+}  // namespace
 
 extern "C" {
 
@@ -42,6 +73,7 @@ long ref_toed_detect_u8(const unsigned char* img, int H, int W, int nthreads,
                         const char* scratch_dir, double* edges, long capacity,
                         double* planes4, double* posmaps, double* time_conv_nms)
 {
+    QuietStdout quiet;
     std::string dir(scratch_dir ? scratch_dir : ".");
     std::string path = dir + "/ref_input.bin";
     {
@@ -88,6 +120,7 @@ long ref_subpix_to_correct(const double* E, int h, int w, double thresh, double 
                            const char* scratch_dir, double* edges, long capacity,
                            double* TO_E, double* TO_O, double* theta_out, double* times)
 {
+    QuietStdout quiet;
     SubpixelTOCorrectionCPU<double> tc(h, w, thresh, sigma, nthreads, 0);
     tc.set_output_dir(scratch_dir ? scratch_dir : ".");
     tc.set_neighbor_radius(nbr_radius);
@@ -122,6 +155,7 @@ long ref_subpix_to_correct_n(const double* E, int h, int w, int interp_n, double
                              int nthreads, double nbr_radius, const double* theta, const char* scratch_dir,
                              double* edges, long capacity, double* TO_E, double* TO_O)
 {
+    QuietStdout quiet;
     SubpixelTOCorrectionCPU<double> tc(h, w, thresh, sigma, nthreads, interp_n);
     tc.set_output_dir(scratch_dir ? scratch_dir : ".");
     tc.set_neighbor_radius(nbr_radius);

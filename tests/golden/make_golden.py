@@ -74,7 +74,9 @@ def kat_images():
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref-dir", default="/root/reference")
+    ap.add_argument("--ref-dir", default=os.environ.get("TOED_REF_DIR") or subprocess.run(
+        ["make", "-s", "-C", os.path.join(ROOT, "oracle"), "refdir"], capture_output=True, text=True).stdout.strip(),
+        help="reference checkout (default: $TOED_REF_DIR, else the oracle recipe's default)")
     ap.add_argument("--only", default="", help="regenerate only fixtures whose name starts with this")
     args = ap.parse_args()
     subprocess.run(["make", "-s", "-C", os.path.join(ROOT, "oracle"), "ref", f"REF_DIR={args.ref_dir}"],

@@ -51,14 +51,22 @@ def test_two_ranks_gloo():
 
 
 def test_reference_arm_line(monkeypatch, capsys):
-    """bench.py --impl reference prints one JSON line with the contract's keys
-    (a short CPU budget here)."""
+    """bench.py --impl reference prints exactly one line, JSON with the
+    contract's keys (a one-image sample here), and the cross-check of the
+    reference's own CPU build against the port where that build exists."""
     import json
     import types
     import bench
-    monkeypatch.setattr(bench, "REF_SECONDS", 2.0)
+    import oracle
+    monkeypatch.setattr(bench, "REF_SAMPLE_IMAGES", 1)
     bench.run_reference(types.SimpleNamespace(steps=1, warmup=1), 1, 0)
-    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    out = capsys.readouterr().out.strip().splitlines()
+    assert len(out) == 1  # the reference classes' own prints are silenced
+    line = json.loads(out[0])
     assert line["impl"] == "reference" and line["value"] > 0 and line["unit"] == "Mpixel/s"
     assert line["cpu_baseline"]["kind"] == "port" and line["cpu_baseline"]["cores"] >= 1
+    assert line["cpu_baseline"]["sample"].startswith("first 1 images of the batch")
     assert line["e2e"]["h2d_bytes_per_step"] == 0 and line["e2e"]["d2h_bytes_per_step"] == 0
+    cc = line["reference_build_crosscheck"]
+    if oracle.ref_sources_present():
+        assert cc["reference_mpx_s"] > 0 and cc["port_mpx_s"] > 0 and cc["edgels"][0] == cc["edgels"][1]

@@ -389,6 +389,48 @@ def test_host_batch_serialised_launches(toed):
     assert line[1] == "True" and float(line[2]) < 2.0, line
 
 
+def test_host_batch_lost_copy_times_out(toed):
+    """Failure injection on the host (no device fault): the ready-flag copy of
+    one copy group is withheld (TOED_TEST_WITHHOLD_READY) and the wait bound
+    made short (TOED_TEST_READY_SPINS), so that group's work units wait, give
+    up and are skipped.  The call returns TOED_ERR_TIMEOUT within a bounded
+    wall time; the images of the other groups keep their edgels; the next
+    call on the same context, without the injection, succeeds and matches the
+    device-buffer batch.  A fresh process: the variables are read there."""
+    import subprocess
+    import sys
+    code = (
+        "import os, sys, time; sys.path.insert(0, {tests!r}); from conftest import load_package\n"
+        "toed = load_package(); import importlib, torch, numpy as np\n"
+        "synth = importlib.import_module('toed_gb300.synth'); det = toed.Detector(0)\n"
+        "ims = [torch.as_tensor(synth.shapes_image(150 + 13 * k, 170, seed=1900 + k, dtype=np.float32).image)"
+        " for k in range(6)]\n"
+        "ref = det.detect_batch([im.cuda() for im in ims], sigma=1.5)\n"
+        "pinned = [im.pin_memory() for im in ims]\n"
+        "outs = det.alloc_host_outputs([tuple(im.shape) for im in ims], pin=True)\n"
+        "os.environ['TOED_TEST_WITHHOLD_READY'] = '1'; os.environ['TOED_TEST_READY_SPINS'] = '4096'\n"
+        "t0 = time.time(); st = None\n"
+        "try:\n"
+        "    det.detect_host(pinned, outs, toed.make_params(1.5), chunks=3)\n"
+        "except toed.ToedError as e:\n"
+        "    st = e.status\n"
+        "dt = time.time() - t0; flags = det.flags()\n"
+        "first = int(outs[0]['count'].item()) == ref[0]['count']\n"
+        "del os.environ['TOED_TEST_WITHHOLD_READY'], os.environ['TOED_TEST_READY_SPINS']\n"
+        "det.detect_host(pinned, outs, toed.make_params(1.5), chunks=3)\n"
+        "ok = all(int(o['count'].item()) == r['count'] and torch.equal(o['edgels'][:r['count']], r['edgels'].cpu())"
+        " for o, r in zip(outs, ref))\n"
+        "print('RESULT', st, round(dt, 3), flags, first, ok)\n"
+    ).format(tests=os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    line = [l for l in r.stdout.splitlines() if l.startswith("RESULT")][-1].split()
+    assert int(line[1]) == toed.TOED_ERR_TIMEOUT, line
+    assert float(line[2]) < 3.0, line
+    assert int(line[3]) & 4, line  # TOED_FLAG_TIMEOUT
+    assert line[4] == "True" and line[5] == "True", line
+
+
 @pytest.mark.parametrize("chunks", [1, 3])
 def test_host_batch_zero_copy_layouts(toed, synth, chunks):
     """Page-locked images, chunks == 1: read in place by the detection kernel

@@ -55,3 +55,33 @@ def test_full_size_ridge_maps_vs_oracle(toed, oracle, synth):
         _check(ref["edges"], r["edgels"].cpu().numpy())
         te = r["TO_E"].cpu().numpy()
         assert np.mean((te != 0) == (ref["TO_E"] != 0)) >= 0.999
+
+
+@pytest.mark.parametrize("H,W", [(1080, 1920), (2160, 3840)])
+def test_precision_study_sizes_vs_oracle(toed, oracle, synth, H, W):
+    """The precision study at its sizes: one float32 image of the shapes
+    generator scaled to 1920x1080 / 3840x2160 (seed 2, as the benchmark
+    makes it), sigma 1 and 2, threshold 2.  FP32 convolutions with the FP64
+    peak fit and orientation recomputation (TOED_HYBRID) meet the stated
+    bounds against the FP64 oracle: edgel-set agreement >= 99.9 %, position
+    <= 1e-3 px, orientation <= 1e-4 rad (wrapped).  The all-FP32 mode is the
+    comparison: same agreement and position bound, and the FP64 fit makes
+    the hybrid position p99 smaller than all-FP32's."""
+    import torch
+    img = synth.shapes_image(H, W, seed=2, dtype=np.float32).image
+    x = torch.as_tensor(img).cuda()
+    det = toed.Detector(0)
+    for sigma in (1.0, 2.0):
+        ref = oracle.detect(img.astype(np.float64), sigma, nthreads=os.cpu_count())
+        assert len(ref["index"]) > 40_000
+        got = {}
+        for name, prec in (("hybrid", toed.TOED_HYBRID), ("fp32", toed.TOED_FP32)):
+            r = det.detect(x, sigma=sigma, out_dtype=toed.TOED_F64, precision=prec)
+            got[name] = compare_edgels(ref["edges"], ref["index"], r["edgels"].cpu().numpy(),
+                                       r["index"].cpu().numpy())
+        hy, f32 = got["hybrid"], got["fp32"]
+        assert hy["agreement"] >= 0.999 and f32["agreement"] >= 0.999, (sigma, hy, f32)
+        assert hy["pos_max"] <= 1e-3 and f32["pos_max"] <= 1e-3, (sigma, hy, f32)
+        assert hy["ori_max"] <= 1e-4, (sigma, hy)
+        assert f32["ori_max"] <= 2e-4, (sigma, f32)
+        assert hy["pos_p99"] < f32["pos_p99"], (sigma, hy, f32)

@@ -184,6 +184,7 @@ struct toed_ctx {
     long long hb_ready_cap = 0;
     int* hb_epoch_src = nullptr;
     int hb_epoch = 0;
+    int ready_spins = kReadySpinLimit;  // bound of each ready-flag wait (polls)
     std::mutex mu;
 };
 
@@ -331,7 +332,7 @@ extern "C" toed_status toed_reserve(toed_ctx* c, long long max_pixels, long long
     return st;
 }
 
-static toed_status check_image(const toed_image& im)
+toed_status toed::check_image(const toed_image& im)
 {
     if (!im.pixels || !im.edgels || !im.count) return TOED_ERR_INVALID_ARG;
     if (im.height <= 0 || im.width <= 0 || im.pitch < im.width || im.capacity < 0) return TOED_ERR_INVALID_ARG;
@@ -413,6 +414,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
     p->ready = c->hb_ready;
     p->ready_epoch = c->hb_epoch;
+    p->ready_spins = c->ready_spins;
     long long units = 0, tiles = 0, staging = 0;
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
@@ -808,6 +810,16 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     // launch groups: the detection launches, each followed by a read of the flags word
     int launches = chunks;
     if (flagged) {
+        // Host-side failure injection for tests (no device fault): with
+        // TOED_TEST_WITHHOLD_READY=k the ready-flag copy of group k is not
+        // enqueued, so that group's units wait TOED_TEST_READY_SPINS polls
+        // (default: the normal bound), give up, and the call returns
+        // TOED_ERR_TIMEOUT; the image copies themselves still run.
+        int withhold = -1;
+        if (const char* e = std::getenv("TOED_TEST_WITHHOLD_READY")) withhold = std::atoi(e);
+        c->ready_spins = kReadySpinLimit;
+        if (const char* e = std::getenv("TOED_TEST_READY_SPINS"))
+            c->ready_spins = std::max(1, std::min(std::atoi(e), kReadySpinLimit));
         // the copies wait only for what the caller's stream held before this
         // call (never for the detection launch, whose CTAs wait for them)
         TOED_HB(cudaEventRecord(ev_in[0], stream));
@@ -817,12 +829,15 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
             for (int i = first[k]; i < first[k + 1]; ++i) slot[i] = k + 1;
         TOED_HB(preload_finalize(radius_of(prm), prm->orientation == TOED_ORI_QAD));
         st = detect_all(c, dev.data(), n, prm, stream, nullptr, true, slot.data());
+        c->ready_spins = kReadySpinLimit;
         if (st != TOED_OK) return fail(st);
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
         TOED_HB(cudaEventRecord(ev_det[0], stream));
         for (int k = 0; k < chunks; ++k) {
             TOED_HB(copy_group(k));
-            TOED_HB(cudaMemcpyAsync(c->hb_ready + k, c->hb_epoch_src, sizeof(int), cudaMemcpyHostToDevice, c->s_in));
+            if (k != withhold)
+                TOED_HB(cudaMemcpyAsync(c->hb_ready + k, c->hb_epoch_src, sizeof(int), cudaMemcpyHostToDevice,
+                                        c->s_in));
         }
         launches = 1;
         first[1] = n;

@@ -33,8 +33,9 @@ constexpr int kStageBlk = 256;                     // staging records a CTA rese
 // the terms' magnitudes over the largest component) get their orientation
 // recomputed from the image in FP64 (HYBRID precision, grid orientation).
 constexpr float kRefineKappa = 20.f;
-// Bound of the wait for a copy group's ready flag (polls ~256 ns apart: a few
-// seconds), after which the kernel flags TOED_FLAG_TIMEOUT and goes on.
+// Default bound of the wait for a copy group's ready flag (polls ~256 ns
+// apart: a few seconds), after which the kernel flags TOED_FLAG_TIMEOUT and
+// skips the units whose pixels have not arrived (BatchParams::ready_spins).
 constexpr int kReadySpinLimit = 1 << 24;
 
 // 1-D taps, index k <-> offset x = k - (r+1) (+0.5 for the shifted set).
@@ -101,6 +102,7 @@ struct BatchParams {
     int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
     const int* ready;    // per copy group: ready_epoch once the group's images are in device memory
     int ready_epoch;
+    int ready_spins;     // polls of a ready flag before the wait gives up (TOED_FLAG_TIMEOUT)
     Scratch sc;
     DetImage img[kBatchMax];
 };

@@ -475,15 +475,26 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
 
 // Bounded wait (one thread) until a copy group's ready flag reads `epoch`:
 // the copy engine writes the flag after the group's pixels, in stream order.
-static __device__ __noinline__ void wait_ready(const int* flag, int epoch, int* words)
+// Returns false -- the unit is skipped -- once `spins` polls have gone by, or
+// while the flag is not yet set and some CTA's wait has already given up
+// (TOED_FLAG_TIMEOUT in words[2], checked after the first poll and every 256
+// polls): a lost copy costs one bounded wait per resident CTA, not one per
+// work unit, and units whose group did arrive are still detected.
+static __device__ __noinline__ bool wait_ready(const int* flag, int epoch, int spins, int* words)
 {
-    for (int it = 0; it < kReadySpinLimit; ++it) {
+    for (int it = 0; it < spins; ++it) {
         int v;
         asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(flag) : "memory");
-        if (v == epoch) return;
+        if (v == epoch) return true;
+        if ((it & 255) == 0) {
+            int f;
+            asm volatile("ld.relaxed.gpu.global.b32 %0, [%1];" : "=r"(f) : "l"(words + 2) : "memory");
+            if (f & TOED_FLAG_TIMEOUT) return false;
+        }
         __nanosleep(256);
     }
     atomicOr(&words[2], TOED_FLAG_TIMEOUT);
+    return false;
 }
 
 // ASYNC: input rows by per-thread async copies (images with tma == 2) or
@@ -535,10 +546,6 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         if (u >= p.n_units) break;
         const int k = find_image(p.n_img, u, [&](int i) { return p.img[i].unit_base; });
         const DetImage& im = p.img[k];
-        if (im.wait_slot > 0) {  // pixels still arriving: wait for the group (uniform across the CTA)
-            if (tid == 0) wait_ready(p.ready + (im.wait_slot - 1), p.ready_epoch, p.sc.words);
-            __syncthreads();
-        }
         const void* src = im.src;
         const long long pitch = im.pitch;
         const int H = im.H, W = im.W, dtype = im.dtype;
@@ -546,6 +553,19 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         const int sr = local / im.nsc, sc = local - sr * im.nsc;
         const int ys = sr * p.S, x0 = sc * kInner;
         const int S_act = min(p.S, H - ys);
+        if (im.wait_slot > 0) {  // pixels still arriving: wait for the group (uniform across the CTA)
+            if (tid == 0)
+                sScal[2] = wait_ready(p.ready + (im.wait_slot - 1), p.ready_epoch, p.ready_spins, p.sc.words) ? 1 : 0;
+            __syncthreads();
+            if (!sScal[2]) {
+                // the copy never arrived: the unit finds no edgels (its row
+                // segments are written empty, so the ordering pass reads no
+                // stale entries) and the call reports TOED_ERR_TIMEOUT
+                for (int i = tid; i < 2 * S_act; i += kThreads)
+                    p.sc.seg[im.seg_base + (long long)(2 * ys + i) * im.nsc + sc] = make_int2(0, 0);
+                continue;
+            }
+        }
         const int nsteps = (2 * S_act + 3 + 2 * B - 1) / (2 * B);
         const int W2 = 2 * W;
         const int row_lo = max(p.border, 2 * ys), row_hi = min(2 * H - p.border, 2 * ys + 2 * S_act);

@@ -28,6 +28,11 @@ cudaError_t preload_finalize(int radius, bool qad);
 cudaError_t launch_scatter_qad(const BatchParams& p, cudaStream_t stream);
 cudaError_t preload_scatter_qad(int radius);
 
+// Host-side checks of one device image (pointers, sizes, dtype, the
+// 16-byte edgel and 4-byte float32 pixel alignment): TOED_OK or the status
+// every detection entry point returns for it.
+toed_status check_image(const toed_image& im);
+
 // Fill d.tma / d.tma_align / d.tma_boxw and encode the image's row map for
 // TMA staging (kStepRows-row boxes, zero fill outside the image).  Leaves
 // d.tma = 0 -- plain loads -- when the driver entry point is unavailable or

@@ -11,13 +11,16 @@
 // How: the scratch the fused kernel and the ordering pass need (work-queue
 // and flag words, staged edgel records, the row-segment table, tile sums)
 // lives in one file-scope __device__ array of fixed size, g_noalloc_scratch.
-// The module that holds it is loaded with the library, so every GPU that
-// loads the library keeps these bytes reserved until the process exits.
+// The CUDA runtime loads the module that holds it lazily (the default since
+// CUDA 12): the bytes are reserved on a device when the first call on that
+// device looks the array up, and stay reserved until the process exits.
 // Host code may not use the array's name as a device address (on the host it
-// names a host-side stand-in), so the device address is looked up once per
-// device with cudaGetSymbolAddress, with that device current, by the first
-// call on that device; that first call should therefore happen before any
-// stream capture that includes this entry point.
+// names a host-side stand-in), so that first call looks the device address
+// up with cudaGetSymbolAddress, with the device current, and caches it with
+// the device's SM count and the kernels' occupancy.  Make the first call on
+// each device at start-up -- before a pool or arena claims the device's
+// memory (else it returns TOED_ERR_CUDA) and before any stream capture that
+// includes this entry point.
 //
 // Limits: an image of at most TOED_NOALLOC_MAX_DIM rows and columns and
 // TOED_NOALLOC_MAX_PIXELS pixels, and an edgel capacity of at most
@@ -66,18 +69,38 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[kScratchBytes];
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char* g_dev_scratch[kMaxDevices] = {};
+int g_dev_sms[kMaxDevices] = {};
+int g_dev_bps[kMaxDevices][TOED_MAX_RADIUS + 1][2] = {};  // resident CTAs per SM [radius][hybrid]
 
-// Device address of g_noalloc_scratch on `dev` (current), looked up once.
-cudaError_t scratch_address(int dev, unsigned char** out)
+// Device address of g_noalloc_scratch on `dev` (current), the device's SM
+// count and the detection kernel's occupancy, looked up once per device
+// (and radius / precision) so that later calls make no such queries.
+cudaError_t device_setup(int dev, int r, bool hyb, const DetectEntry& ent, unsigned char** base, int* sms, int* bps)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_dev_scratch[dev]) {
         void* ptr = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
+        cudaError_t e = cudaGetSymbolAddress(&ptr, g_noalloc_scratch);
         if (e != cudaSuccess) return e;
+        int n = 0;
+        e = cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (e != cudaSuccess) return e;
+        g_dev_sms[dev] = n;
         g_dev_scratch[dev] = static_cast<unsigned char*>(ptr);
     }
-    *out = g_dev_scratch[dev];
+    int& b = g_dev_bps[dev][r][hyb ? 1 : 0];
+    if (b == 0) {
+        cudaError_t e = cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem);
+        if (e != cudaSuccess) return e;
+        int n = 0;
+        e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, ent.func, kThreads, ent.smem);
+        if (e != cudaSuccess) return e;
+        if (n <= 0) return cudaErrorInvalidConfiguration;
+        b = n;
+    }
+    *base = g_dev_scratch[dev];
+    *sms = g_dev_sms[dev];
+    *bps = b;
     return cudaSuccess;
 }
 
@@ -88,10 +111,10 @@ using namespace toed;
 
 extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_params* prm, cudaStream_t stream)
 {
-    if (!im || !prm || !im->pixels || !im->edgels || !im->count) return TOED_ERR_INVALID_ARG;
-    if (im->height <= 0 || im->width <= 0 || im->pitch < im->width || im->capacity < 0) return TOED_ERR_INVALID_ARG;
-    if (im->dtype != TOED_U8 && im->dtype != TOED_F32) return TOED_ERR_UNSUPPORTED;
-    if ((reinterpret_cast<uintptr_t>(im->edgels) & 15u) != 0) return TOED_ERR_INVALID_ARG;
+    if (!im || !prm) return TOED_ERR_INVALID_ARG;
+    // the same image checks as toed_detect (pointers, sizes, dtype, alignment)
+    const toed_status ist = check_image(*im);
+    if (ist != TOED_OK) return ist;
     if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma) || !std::isfinite(prm->threshold) || prm->border < 1)
         return TOED_ERR_INVALID_ARG;
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
@@ -109,12 +132,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     int dev = 0, sms = 0, bps = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TOED_ERR_CUDA;
     unsigned char* base = nullptr;
-    if (scratch_address(dev, &base) != cudaSuccess) return TOED_ERR_CUDA;
-    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return TOED_ERR_CUDA;
-    if (cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem) != cudaSuccess)
-        return TOED_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ent.func, kThreads, ent.smem) != cudaSuccess || bps <= 0)
-        return TOED_ERR_CUDA;
+    if (device_setup(dev, r, prm->precision != TOED_FP32, ent, &base, &sms, &bps) != cudaSuccess) return TOED_ERR_CUDA;
 
     BatchParams p;  // on the stack: no heap allocation either
     std::memset(&p, 0, sizeof(p));
