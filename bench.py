@@ -462,6 +462,11 @@ def side_measurements(toed, det, images, side, stream):
     gms = _time_ms(lambda: det.detect_into(d_imgs, outs, prm, stream), 3, stream)
     out["qad_orientation_batch"] = {"ms": round(qms, 3), "grid_mode_ms": round(gms, 3),
                                     "mpx_s": round(npx / (qms * 1e-3) / 1e6, 1)}
+    # -- NMS along the corrected normal on the same batch --------------------
+    pn = toed.make_params(SIGMA, 0, THRESH, nms_direction=toed.TOED_NMS_TO_NORMAL)
+    nms_ms = _time_ms(lambda: det.detect_into(d_imgs, outs, pn, stream), 3, stream)
+    out["nms_to_normal_batch"] = {"ms": round(nms_ms, 3), "gradient_nms_ms": round(gms, 3),
+                                  "mpx_s": round(npx / (nms_ms * 1e-3) / 1e6, 1)}
     # -- config 4: forward vs forward + backward (16 x 512^2, sigma learnable)
     c4 = [torch.as_tensor(im).to(dev) for im in side["c4"]]
     o4 = det.alloc_outputs([im.shape for im in c4], None)
@@ -513,6 +518,21 @@ def side_measurements(toed, det, images, side, stream):
                 row["qad_orientation"] = {"agreement": round(len(common) / max(len(gi), len(refq["index"])), 6),
                                           "ori_err_max_rad": float(f"{np.nanmax(oe):.3g}"),
                                           "ori_err_p99_rad": float(f"{np.nanquantile(oe, .99):.3g}")}
+            if name == "c2_1080":
+                # NMS and peak fit along the corrected normal against its own FP64 oracle
+                reft = oracle.detect(im.astype(np.float64), sg, nthreads=os.cpu_count(), nms="to_normal")
+                r = det.detect(torch.as_tensor(im).to(dev), sigma=sg, out_dtype=toed.TOED_F64,
+                               nms_direction=toed.TOED_NMS_TO_NORMAL)
+                gi = r["index"].cpu().numpy().astype(np.int64)
+                ge = r["edgels"].cpu().numpy()
+                common, ia, ib = np.intersect1d(reft["index"], gi, return_indices=True)
+                pe = np.hypot(*(reft["edges"][ia, :2] - ge[ib, :2]).T)
+                oe = np.abs(np.angle(np.exp(1j * (reft["edges"][ia, 2] - ge[ib, 2]))))
+                row["nms_to_normal"] = {"agreement": round(len(common) / max(len(gi), len(reft["index"])), 6),
+                                        "pos_err_max_px": float(f"{pe.max():.3g}"),
+                                        "pos_err_p99_px": float(f"{np.quantile(pe, .99):.3g}"),
+                                        "ori_err_max_rad": float(f"{np.nanmax(oe):.3g}"),
+                                        "ori_err_p99_rad": float(f"{np.nanquantile(oe, .99):.3g}")}
             row["n_ref"] = int(len(ref["index"]))
             prec[f"{name[3:]}_sigma{sg:g}"] = row
     out["precision_vs_fp64_oracle"] = prec

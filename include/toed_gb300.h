@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define TOED_ABI_VERSION 1
+#define TOED_ABI_VERSION 2 /* 2: toed_params.nms_direction */
 #define TOED_MAX_RADIUS 12 /* kernel half-width r = ceil(4 sigma) <= 12, i.e. sigma <= 3 */
 
 typedef enum toed_status {
@@ -75,6 +75,17 @@ typedef enum toed_orientation {
                           subpixel point; positions and strengths unchanged */
 } toed_orientation;
 
+/* Direction of the subpixel NMS and its parabola peak fit. */
+typedef enum toed_nms_direction {
+    TOED_NMS_GRADIENT = 0, /* along the first-order gradient (Ix, Iy): the reference
+                              (cpu_toed.cpp:411-489) */
+    TOED_NMS_TO_NORMAL = 1 /* along the corrected normal, the unit third-order vector
+                              (TO_Ix, TO_Iy) of cpu_toed.cpp:227-230 whose tangent is the
+                              emitted orientation; same candidates (threshold, gradient
+                              epsilon), same emitted orientation.  No reference counterpart;
+                              grid orientation only, no adjoint */
+} toed_nms_direction;
+
 /* Device flags (toed_device_flags) */
 #define TOED_FLAG_OVER_CAPACITY 0x1 /* some image found more edgels than its capacity */
 #define TOED_FLAG_STAGING_FULL 0x2  /* the context staging buffer overflowed */
@@ -103,6 +114,7 @@ typedef struct toed_params {
     int out_dtype;     /* TOED_F32 (16-byte edgels) or TOED_F64 (32-byte edgels) */
     int precision;     /* toed_precision */
     int orientation;   /* toed_orientation (TOED_ORI_GRID: the reference C++ detector) */
+    int nms_direction; /* toed_nms_direction (TOED_NMS_GRADIENT: the reference) */
 } toed_params;
 
 /* Fill `p` with the reference's configuration for a given sigma. */

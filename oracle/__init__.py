@@ -97,6 +97,8 @@ def lib():
             _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, ctypes.c_double,
             ctypes.c_int, _dp, ctypes.c_long, _dp, _dp, _i64p]
         L.toed_oracle_detect.restype = ctypes.c_long
+        L.toed_oracle_detect_ex.argtypes = L.toed_oracle_detect.argtypes + [ctypes.c_int]
+        L.toed_oracle_detect_ex.restype = ctypes.c_long
         L.toed_oracle_detect_qad.argtypes = [
             _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, ctypes.c_int, _dp, ctypes.c_double,
             ctypes.c_int, _dp, ctypes.c_long, _i64p]
@@ -131,14 +133,21 @@ def taps(sigma: float, r: int | None = None) -> np.ndarray:
 
 
 def detect(img, sigma: float = 2.0, r: int | None = None, tap_block=None, threshold: float = 2.0,
-           nthreads: int = 0, planes: bool = False, orientation: str = "grid"):
+           nthreads: int = 0, planes: bool = False, orientation: str = "grid", nms: str = "gradient"):
     """FP64 TOED.  Returns dict(edges=(N,4), index=(N,) 2x-grid linear index
     [, planes=(4,2H,2W) Ix/Iy/mag/ori, posmaps=(3,2H,2W)]).
     orientation="qad": the MATLAB quick-and-dirty mode
     (third_order_edge_detector.m:91-141), derivatives cubic-interpolated at
-    the subpixel point (no plane outputs)."""
+    the subpixel point (no plane outputs).
+    nms="to_normal": NMS and peak fit along the corrected normal (the
+    third-order vector) instead of the gradient (cpu_toed.cpp:411-489), an
+    extension beyond the reference."""
     if orientation not in ("grid", "qad"):
         raise ValueError(orientation)
+    if nms not in ("gradient", "to_normal"):
+        raise ValueError(nms)
+    if nms == "to_normal" and orientation != "grid":
+        raise ValueError("nms='to_normal' is defined with the grid orientation")
     img = np.ascontiguousarray(img, dtype=np.float64)
     H, W = img.shape
     r = default_radius(sigma) if r is None else r
@@ -157,9 +166,9 @@ def detect(img, sigma: float = 2.0, r: int | None = None, tap_block=None, thresh
         return {"edges": edges[:n].copy(), "index": index[:n].copy()}
     pl = np.zeros((4, 2 * H, 2 * W), np.float64) if planes else None
     pm = np.zeros((3, 2 * H, 2 * W), np.float64) if planes else None
-    n = lib().toed_oracle_detect(_ptr(img), H, W, float(sigma), int(r), _ptr(tb), float(threshold),
-                                 int(nthreads), _ptr(edges), cap, _ptr(pl), _ptr(pm),
-                                 index.ctypes.data_as(_i64p))
+    n = lib().toed_oracle_detect_ex(_ptr(img), H, W, float(sigma), int(r), _ptr(tb), float(threshold),
+                                    int(nthreads), _ptr(edges), cap, _ptr(pl), _ptr(pm),
+                                    index.ctypes.data_as(_i64p), 1 if nms == "to_normal" else 0)
     out = {"edges": edges[:n].copy(), "index": index[:n].copy()}
     if planes:
         out["planes"] = pl

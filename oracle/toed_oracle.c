@@ -19,6 +19,9 @@
  *     - MATLAB QaD orientation (third_order_edge_detector.m:91-141):
  *                       toed_oracle_detect_qad, derivatives cubic-interpolated
  *                       at the subpixel point
+ *     - extension: NMS and peak fit along the corrected normal (the
+ *                       third-order vector) instead of the gradient,
+ *                       toed_oracle_detect_ex(nms_dir = 1)
  *     Extensions over the reference (which hard-codes sigma = 2 through literal
  *     taps, kernel 17 and threshold 2): any sigma with taps from the
  *     reference's own commented formula, any half-width r, any threshold,
@@ -105,9 +108,31 @@ static inline void to_orientation(double fx, double fy, double fxx, double fxy,
     *ori = atan2(tix, -tiy);
 }
 
+/* The third-order vector itself (cpu_toed.cpp:227-230), before normalisation. */
+static inline void to_vector(double fx, double fy, double fxx, double fxy, double fyy, double fxxy,
+                             double fxyy, double fxxx, double fyyy, double *tix, double *tiy)
+{
+    *tix = fx * (2 * fxx * fxx + 2 * fxy * fxy) + fy * (2 * fxx * fxy + 2 * fyy * fxy) +
+           2 * fx * fy * fxxy + fy * fy * fxyy + fx * fx * fxxx;
+    *tiy = fx * (2 * fxx * fxy + 2 * fyy * fxy) + fy * (2 * fyy * fyy + 2 * fxy * fxy) +
+           2 * fx * fy * fxyy + fx * fx * fxxy + fy * fy * fyyy;
+}
+
+static void oracle_planes(const double *img, int H, int W, int r, const double *taps, int nthreads,
+                          double *Ix, double *Iy, double *mag, double *ori, double *derivs9,
+                          double *tvec);
+
 void toed_oracle_planes(const double *img, int H, int W, int r, const double *taps,
                         int nthreads, double *Ix, double *Iy, double *mag, double *ori,
                         double *derivs9 /* optional: 9 planes of (2H)(2W) */)
+{
+    oracle_planes(img, H, W, r, taps, nthreads, Ix, Iy, mag, ori, derivs9, NULL);
+}
+
+/* tvec (optional): 2 planes, the third-order vector (TO_Ix, TO_Iy) per point. */
+static void oracle_planes(const double *img, int H, int W, int r, const double *taps, int nthreads,
+                          double *Ix, double *Iy, double *mag, double *ori, double *derivs9,
+                          double *tvec)
 {
     const int n = 2 * r + 3;
     const double *G = taps + 0 * n, *Gx = taps + 1 * n, *Gxx = taps + 2 * n, *Gxxx = taps + 3 * n;
@@ -172,6 +197,7 @@ void toed_oracle_planes(const double *img, int H, int W, int r, const double *ta
                 if (Iy) Iy[o] = fy;
                 if (mag) mag[o] = sqrt(fx * fx + fy * fy);
                 if (ori) to_orientation(fx, fy, fxx, fxy, fyy, fxxy, fxyy, fxxx, fyyy, &ori[o]);
+                if (tvec) to_vector(fx, fy, fxx, fxy, fyy, fxxy, fxyy, fxxx, fyyy, &tvec[o], &tvec[P2 + o]);
                 if (derivs9) {
                     const double d9[9] = {fx, fy, fxx, fxy, fyy, fxxy, fxyy, fxxx, fyyy};
                     for (int k = 0; k < 9; k++) derivs9[(size_t)k * P2 + o] = d9[k];
@@ -245,8 +271,27 @@ static inline void nms_sector(const double *M, int w, int i, int j, double gx, d
  * NMS over the 2x grid interior [10, 2H-10) x [10, 2W-10) (cpu_toed.cpp:400-401).
  * pos_x/pos_y/smag: (2H)(2W) planes, zeroed here, written where accepted.
  */
+static void oracle_nms(const double *Ix, const double *Iy, const double *mag, const double *tvec, int H2,
+                       int W2, double threshold, int nthreads, double *pos_x, double *pos_y, double *smag);
+
 void toed_oracle_nms(const double *Ix, const double *Iy, const double *mag, int H2, int W2,
                      double threshold, int nthreads, double *pos_x, double *pos_y, double *smag)
+{
+    oracle_nms(Ix, Iy, mag, NULL, H2, W2, threshold, nthreads, pos_x, pos_y, smag);
+}
+
+/*
+ * tvec == NULL: the reference's NMS along the first-order gradient (Ix, Iy).
+ * tvec != NULL (extension, no counterpart in the reference): the same
+ * candidates (threshold and gradient checks, :403, :407), but the sector,
+ * the interpolated neighbours, the parabola fit and the subpixel offset are
+ * taken along the unit third-order vector (TO_Ix, TO_Iy) -- the corrected
+ * normal of the edge, whose tangent is the emitted orientation
+ * atan2(TO_Ix, -TO_Iy) -- instead of along the gradient; a point whose
+ * vector vanishes has no direction and is skipped.
+ */
+static void oracle_nms(const double *Ix, const double *Iy, const double *mag, const double *tvec, int H2,
+                       int W2, double threshold, int nthreads, double *pos_x, double *pos_y, double *smag)
 {
     const size_t P2 = (size_t)H2 * W2;
     memset(pos_x, 0, P2 * sizeof(double));
@@ -260,9 +305,16 @@ void toed_oracle_nms(const double *Ix, const double *Iy, const double *mag, int 
             const double m = mag[o];
             if (m <= threshold) continue;                                  /* :403 */
             if ((fabs(Ix[o]) < 10e-6) && (fabs(Iy[o]) < 10e-6)) continue; /* :407 */
-            const double nx = Ix[o] / m, ny = Iy[o] / m;                   /* :411-412 */
+            double dx = Ix[o], dy = Iy[o], dm = m;
+            if (tvec) {
+                dx = tvec[o];
+                dy = tvec[P2 + o];
+                dm = sqrt(dx * dx + dy * dy);
+                if (!(dm > 0) || !isfinite(dm)) continue;
+            }
+            const double nx = dx / dm, ny = dy / dm; /* :411-412 */
             double slope, fp, fm;
-            nms_sector(mag, W2, i, j, Ix[o], Iy[o], nx, ny, &slope, &fp, &fm);
+            nms_sector(mag, W2, i, j, dx, dy, nx, ny, &slope, &fp, &fm);
             const double s = sqrt(1 + slope * slope); /* :465 */
             if ((m > fm && m > fp) || (m > fm && m >= fp) || (m >= fm && m > fp)) {
                 const double A = (fm + fp - 2 * m) / (2 * s * s); /* :471-476 */
@@ -313,9 +365,23 @@ long toed_oracle_compact(const double *pos_x, const double *pos_y, const double 
  * (row * 2W + col) of each edgel.  Returns N (may exceed capacity; only the
  * first `capacity` edgels are written).
  */
+long toed_oracle_detect_ex(const double *img, int H, int W, double sigma, int r, const double *taps_in,
+                           double threshold, int nthreads, double *edges, long capacity, double *planes4,
+                           double *posmaps, int64_t *index_out, int nms_dir);
+
 long toed_oracle_detect(const double *img, int H, int W, double sigma, int r,
                         const double *taps_in, double threshold, int nthreads, double *edges,
                         long capacity, double *planes4, double *posmaps, int64_t *index_out)
+{
+    return toed_oracle_detect_ex(img, H, W, sigma, r, taps_in, threshold, nthreads, edges, capacity, planes4,
+                                 posmaps, index_out, 0);
+}
+
+/* nms_dir 0: NMS along the gradient (the reference); 1: along the corrected
+ * normal, the third-order vector (see oracle_nms). */
+long toed_oracle_detect_ex(const double *img, int H, int W, double sigma, int r, const double *taps_in,
+                           double threshold, int nthreads, double *edges, long capacity, double *planes4,
+                           double *posmaps, int64_t *index_out, int nms_dir)
 {
     const int n = 2 * r + 3;
     double *taps = (double *)malloc(sizeof(double) * 8 * n);
@@ -327,10 +393,11 @@ long toed_oracle_detect(const double *img, int H, int W, double sigma, int r,
     const size_t P2 = (size_t)H2 * W2;
     double *pl = planes4 ? planes4 : (double *)malloc(sizeof(double) * 4 * P2);
     double *pm = posmaps ? posmaps : (double *)malloc(sizeof(double) * 3 * P2);
+    double *tv = nms_dir ? (double *)malloc(sizeof(double) * 2 * P2) : NULL;
     memset(pl, 0, sizeof(double) * 4 * P2);
-    toed_oracle_planes(img, H, W, r, taps, nthreads, pl, pl + P2, pl + 2 * P2, pl + 3 * P2, NULL);
-    toed_oracle_nms(pl, pl + P2, pl + 2 * P2, H2, W2, threshold, nthreads, pm, pm + P2,
-                    pm + 2 * P2);
+    oracle_planes(img, H, W, r, taps, nthreads, pl, pl + P2, pl + 2 * P2, pl + 3 * P2, NULL, tv);
+    oracle_nms(pl, pl + P2, pl + 2 * P2, tv, H2, W2, threshold, nthreads, pm, pm + P2, pm + 2 * P2);
+    free(tv);
     long N = toed_oracle_compact(pm, pm + P2, pl + 3 * P2, pm + 2 * P2, H2, W2, edges, capacity,
                                  index_out);
     if (!planes4) free(pl);

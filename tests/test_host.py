@@ -41,6 +41,7 @@ def test_status_strings(toed):
     p = toed.toed_params()
     L.toed_params_default(ctypes.byref(p), ctypes.c_float(2.0))
     assert (p.sigma, p.radius, p.threshold, p.border) == (2.0, 0, 2.0, 10)
+    assert (p.orientation, p.nms_direction) == (toed.TOED_ORI_GRID, toed.TOED_NMS_GRADIENT)
 
 
 def test_struct_layout_matches_header(toed, tmp_path):
@@ -50,11 +51,12 @@ def test_struct_layout_matches_header(toed, tmp_path):
 #include <stddef.h>
 #include "toed_gb300.h"
 int main(void) {
-  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(toed_image), offsetof(toed_image, dtype),
+  printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(toed_image), offsetof(toed_image, dtype),
          offsetof(toed_image, edgels), offsetof(toed_image, capacity), offsetof(toed_image, count),
          offsetof(toed_image, grid_index), sizeof(toed_params), offsetof(toed_params, precision),
          offsetof(toed_params, orientation), sizeof(toed_tuning), sizeof(toed_host_image),
-         offsetof(toed_host_image, grid_index), sizeof(toed_edgemap), sizeof(toed_subpix_params));
+         offsetof(toed_host_image, grid_index), sizeof(toed_edgemap), sizeof(toed_subpix_params),
+         offsetof(toed_params, nms_direction));
   return 0;
 }
 """)
@@ -66,7 +68,7 @@ int main(void) {
     want = [ctypes.sizeof(T), T.dtype.offset, T.edgels.offset, T.capacity.offset, T.count.offset,
             T.grid_index.offset, ctypes.sizeof(P), P.precision.offset, P.orientation.offset,
             ctypes.sizeof(toed.toed_tuning), ctypes.sizeof(HI), HI.grid_index.offset,
-            ctypes.sizeof(toed.toed_edgemap), ctypes.sizeof(toed.toed_subpix_params)]
+            ctypes.sizeof(toed.toed_edgemap), ctypes.sizeof(toed.toed_subpix_params), P.nms_direction.offset]
     assert got == want
 
 

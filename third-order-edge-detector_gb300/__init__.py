@@ -31,7 +31,8 @@ TOED_OK, TOED_ERR_INVALID_ARG, TOED_ERR_CAPACITY, TOED_ERR_CUDA, TOED_ERR_TIMEOU
 TOED_U8, TOED_F32, TOED_F64 = 0, 1, 2
 TOED_HYBRID, TOED_FP32 = 0, 1
 TOED_ORI_GRID, TOED_ORI_QAD = 0, 1
-TOED_FLAG_OVER_CAPACITY, TOED_FLAG_STAGING_FULL = 1, 2
+TOED_NMS_GRADIENT, TOED_NMS_TO_NORMAL = 0, 1
+TOED_FLAG_OVER_CAPACITY, TOED_FLAG_STAGING_FULL, TOED_FLAG_TIMEOUT, TOED_FLAG_BOUNDS = 1, 2, 4, 8
 MAX_RADIUS = 12
 
 # exported C symbols (checked by tests against include/toed_gb300.h)
@@ -62,7 +63,7 @@ class toed_params(ctypes.Structure):
     _fields_ = [
         ("sigma", ctypes.c_float), ("radius", ctypes.c_int), ("threshold", ctypes.c_float),
         ("border", ctypes.c_int), ("out_dtype", ctypes.c_int), ("precision", ctypes.c_int),
-        ("orientation", ctypes.c_int),
+        ("orientation", ctypes.c_int), ("nms_direction", ctypes.c_int),
     ]
 
 
@@ -207,11 +208,13 @@ def _torch():
 
 
 def make_params(sigma=2.0, radius=0, threshold=2.0, border=10, out_dtype=TOED_F32,
-                precision=TOED_HYBRID, orientation=TOED_ORI_GRID) -> toed_params:
+                precision=TOED_HYBRID, orientation=TOED_ORI_GRID, nms_direction=TOED_NMS_GRADIENT) -> toed_params:
     """orientation: TOED_ORI_GRID (0, the C++ detector) or TOED_ORI_QAD (1,
-    the MATLAB quick-and-dirty mode)."""
+    the MATLAB quick-and-dirty mode).  nms_direction: TOED_NMS_GRADIENT (0,
+    the reference) or TOED_NMS_TO_NORMAL (1, NMS and peak fit along the
+    corrected normal)."""
     return toed_params(float(sigma), int(radius), float(threshold), int(border), int(out_dtype),
-                       int(precision), int(orientation))
+                       int(precision), int(orientation), int(nms_direction))
 
 
 class HostBatch:
@@ -404,11 +407,11 @@ class Detector:
 
     def detect_batch(self, images, sigma=2.0, threshold=2.0, radius=0, border=10,
                      out_dtype=TOED_F32, precision=TOED_HYBRID, capacity=None, index=True,
-                     stream=None, orientation=TOED_ORI_GRID):
+                     stream=None, orientation=TOED_ORI_GRID, nms_direction=TOED_NMS_GRADIENT):
         """Detect edgels in a list of 2-D CUDA tensors.  Returns a list of
         dicts with ``edgels`` (N x 4: x, y, orientation, strength) and,
         with ``index``, the 2x-grid linear index of each edgel."""
-        p = make_params(sigma, radius, threshold, border, out_dtype, precision, orientation)
+        p = make_params(sigma, radius, threshold, border, out_dtype, precision, orientation, nms_direction)
         outs = self.alloc_outputs([tuple(im.shape) for im in images], capacity, out_dtype, index)
         self.detect_into(images, outs, p, stream)
         s = stream if stream is not None else self.torch.cuda.current_stream(self.device)

@@ -17,34 +17,35 @@
 #include "toed_internal.h"
 
 namespace toed {
-DetectEntry detect_entry_r1(bool, bool);
-DetectEntry detect_entry_r2(bool, bool);
-DetectEntry detect_entry_r3(bool, bool);
-DetectEntry detect_entry_r4(bool, bool);
-DetectEntry detect_entry_r5(bool, bool);
-DetectEntry detect_entry_r6(bool, bool);
-DetectEntry detect_entry_r7(bool, bool);
-DetectEntry detect_entry_r8(bool, bool);
-DetectEntry detect_entry_r9(bool, bool);
-DetectEntry detect_entry_r10(bool, bool);
-DetectEntry detect_entry_r11(bool, bool);
-DetectEntry detect_entry_r12(bool, bool);
+DetectEntry detect_entry_r1(bool, bool, bool);
+DetectEntry detect_entry_r2(bool, bool, bool);
+DetectEntry detect_entry_r3(bool, bool, bool);
+DetectEntry detect_entry_r4(bool, bool, bool);
+DetectEntry detect_entry_r5(bool, bool, bool);
+DetectEntry detect_entry_r6(bool, bool, bool);
+DetectEntry detect_entry_r7(bool, bool, bool);
+DetectEntry detect_entry_r8(bool, bool, bool);
+DetectEntry detect_entry_r9(bool, bool, bool);
+DetectEntry detect_entry_r10(bool, bool, bool);
+DetectEntry detect_entry_r11(bool, bool, bool);
+DetectEntry detect_entry_r12(bool, bool, bool);
 
-DetectEntry detect_entry(int r, bool hyb, bool async)
+DetectEntry detect_entry(int r, bool hyb, bool async, bool nmsto)
 {
+    if (nmsto) async = false;
     switch (r) {
-    case 1: return detect_entry_r1(hyb, async);
-    case 2: return detect_entry_r2(hyb, async);
-    case 3: return detect_entry_r3(hyb, async);
-    case 4: return detect_entry_r4(hyb, async);
-    case 5: return detect_entry_r5(hyb, async);
-    case 6: return detect_entry_r6(hyb, async);
-    case 7: return detect_entry_r7(hyb, async);
-    case 8: return detect_entry_r8(hyb, async);
-    case 9: return detect_entry_r9(hyb, async);
-    case 10: return detect_entry_r10(hyb, async);
-    case 11: return detect_entry_r11(hyb, async);
-    case 12: return detect_entry_r12(hyb, async);
+    case 1: return detect_entry_r1(hyb, async, nmsto);
+    case 2: return detect_entry_r2(hyb, async, nmsto);
+    case 3: return detect_entry_r3(hyb, async, nmsto);
+    case 4: return detect_entry_r4(hyb, async, nmsto);
+    case 5: return detect_entry_r5(hyb, async, nmsto);
+    case 6: return detect_entry_r6(hyb, async, nmsto);
+    case 7: return detect_entry_r7(hyb, async, nmsto);
+    case 8: return detect_entry_r8(hyb, async, nmsto);
+    case 9: return detect_entry_r9(hyb, async, nmsto);
+    case 10: return detect_entry_r10(hyb, async, nmsto);
+    case 11: return detect_entry_r11(hyb, async, nmsto);
+    case 12: return detect_entry_r12(hyb, async, nmsto);
     default: return DetectEntry{nullptr, 0};
     }
 }
@@ -159,7 +160,7 @@ struct toed_ctx {
     long long keep_cap = 0;
     double* sp_work = nullptr;  // TO correction at interp_n > 0: maps resized onto the work grid
     long long sp_work_cap = 0;
-    int blocks_per_sm[TOED_MAX_RADIUS + 1][2][2] = {};  // [radius][hybrid][async row staging]
+    int blocks_per_sm[TOED_MAX_RADIUS + 1][2][3] = {};  // [radius][hybrid][TMA/plain, async, corrected normal]
     // launch shape chosen by toed_autotune per (radius, precision, size class of
     // the launch: floor(log2(pixels))); strip_rows 0 = heuristic
     toed_tuning tune[TOED_MAX_RADIUS + 1][2][kSizeClasses] = {};
@@ -200,6 +201,7 @@ void toed_params_default(toed_params* p, float sigma)
     p->out_dtype = TOED_F32;
     p->precision = TOED_HYBRID;
     p->orientation = TOED_ORI_GRID;
+    p->nms_direction = TOED_NMS_GRADIENT;
 }
 
 const char* toed_status_string(toed_status s)
@@ -386,13 +388,16 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
                                 bool plain_loads = false, const int* wait_slot = nullptr)
 {
     const bool hyb = prm->precision != TOED_FP32;
+    const bool nmsto = prm->nms_direction == TOED_NMS_TO_NORMAL;
     const toed_tuning& tuned = c->tune[r][hyb ? 1 : 0][size_class(images, n)];
     const toed_tuning* use = force ? force : (tuned.strip_rows > 0 ? &tuned : nullptr);
-    // async row staging: images read in place from host memory, or the tuned shape asks for it
-    const bool async_rows = plain_loads || (use && use->staging == 2);
-    DetectEntry ent = detect_entry(r, hyb, async_rows);
+    // async row staging: images read in place from host memory, or the tuned
+    // shape asks for it (the corrected-normal kernel stages rows by TMA or
+    // plain loads only)
+    const bool async_rows = !nmsto && (plain_loads || (use && use->staging == 2));
+    DetectEntry ent = detect_entry(r, hyb, async_rows, nmsto);
     if (!ent.func) return TOED_ERR_UNSUPPORTED;
-    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0][async_rows ? 1 : 0];
+    int& bps = c->blocks_per_sm[r][hyb ? 1 : 0][nmsto ? 2 : (async_rows ? 1 : 0)];
     if (bps == 0) {
         TOED_CU(cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem));
         TOED_CU(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, ent.func, kThreads, ent.smem));
@@ -412,6 +417,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->radius = r;
     p->hyb = hyb ? 1 : 0;
     p->qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
+    p->nms_to = nmsto ? 1 : 0;
     p->ready = c->hb_ready;
     p->ready_epoch = c->hb_epoch;
     p->ready_spins = c->ready_spins;
@@ -439,6 +445,8 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
             d.tma = (d.dtype == TOED_F32) ? 2 : 0;  // async row copies (float32) or plain loads, never TMA
         else if (use && !use->staging)
             d.tma = 0;
+        else if (nmsto && plain_loads)
+            d.tma = 0;  // host memory read in place: plain loads
         const long long nseg = 2LL * im.height * d.nsc;
         d.nseg = nseg;
         units += (long long)d.nsc * d.nsr;
@@ -491,6 +499,10 @@ static toed_status check_batch(const toed_ctx* c, const toed_image* images, int 
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
     if (prm->orientation != TOED_ORI_GRID && prm->orientation != TOED_ORI_QAD) return TOED_ERR_INVALID_ARG;
+    if (prm->nms_direction != TOED_NMS_GRADIENT && prm->nms_direction != TOED_NMS_TO_NORMAL)
+        return TOED_ERR_INVALID_ARG;
+    // the quick-and-dirty orientation is defined on the gradient-direction NMS
+    if (prm->nms_direction == TOED_NMS_TO_NORMAL && prm->orientation != TOED_ORI_GRID) return TOED_ERR_UNSUPPORTED;
     const int r = radius_of(prm);
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
     for (int i = 0; i < n; ++i) {
@@ -1021,7 +1033,8 @@ extern "C" toed_status toed_backward_batch(toed_ctx* c, const toed_grad_image* i
     if (!c || !items || n <= 0 || !prm || !grad_sigma) return TOED_ERR_INVALID_ARG;
     if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma)) return TOED_ERR_INVALID_ARG;
     // the adjoint is that of the grid-point orientation (cpu_toed.cpp:227-232)
-    if (prm->orientation != TOED_ORI_GRID) return TOED_ERR_UNSUPPORTED;
+    // and of the gradient-direction NMS (cpu_toed.cpp:411-489)
+    if (prm->orientation != TOED_ORI_GRID || prm->nms_direction != TOED_NMS_GRADIENT) return TOED_ERR_UNSUPPORTED;
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     const int r = radius_of(prm);
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;

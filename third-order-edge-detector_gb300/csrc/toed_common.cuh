@@ -100,6 +100,7 @@ struct BatchParams {
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
     int hyb;             // 1: FP64 peak fit, FP64 recomputation of ill-conditioned orientations (TOED_HYBRID)
     int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
+    int nms_to;          // 1: NMS and peak fit along the corrected normal (TOED_NMS_TO_NORMAL)
     const int* ready;    // per copy group: ready_epoch once the group's images are in device memory
     int ready_epoch;
     int ready_spins;     // polls of a ready flag before the wait gives up (TOED_FLAG_TIMEOUT)

@@ -356,7 +356,13 @@ struct NmsEval {
     bool cand;
 };
 
-__device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int m, int c, float thr)
+// TOD (the corrected-normal mode, an extension beyond the reference): the
+// sector, neighbours, fit and offset are taken along the unit vector of
+// (tx, ty) -- the third-order vector -- instead of along (Ix, Iy); the
+// candidate tests (threshold, gradient epsilon) stay those of the reference.
+template <bool TOD = false>
+__device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int m, int c, float thr,
+                                            float tx = 0.f, float ty = 0.f)
 {
     NmsEval r;
     r.cand = false;
@@ -367,13 +373,23 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     r.gx = g.x;
     r.gy = g.y;
     if (fabsf(g.x) < 10e-6f && fabsf(g.y) < 10e-6f) return r;  // :407
-    r.nx = __fdividef(g.x, r.mv);
-    r.ny = __fdividef(g.y, r.mv);
+    float dx = g.x, dy = g.y;
+    if (TOD) {
+        const float tm = sqrtf(fmaf(tx, tx, ty * ty));
+        if (!(tm > 0.f) || !isfinite(tm)) return r;  // no direction
+        r.nx = tx / tm;
+        r.ny = ty / tm;
+        dx = tx;
+        dy = ty;
+    } else {
+        r.nx = __fdividef(g.x, r.mv);
+        r.ny = __fdividef(g.y, r.mv);
+    }
     // Eight sectors of cpu_toed.cpp:415-462 in closed form: x-major when
     // |Ix| >= |Iy|; the axis neighbour steps along the major axis towards
     // the gradient, the diagonal one along both; fm mirrors fp.
-    const bool xmaj = fabsf(g.x) >= fabsf(g.y);
-    const int sx = (g.x >= 0.f) ? 1 : -1, sy = (g.y >= 0.f) ? 1 : -1;
+    const bool xmaj = fabsf(dx) >= fabsf(dy);
+    const int sx = (dx >= 0.f) ? 1 : -1, sy = (dy >= 0.f) ? 1 : -1;
     r.slope = xmaj ? __fdividef(fabsf(r.ny), fabsf(r.nx)) : __fdividef(fabsf(r.nx), fabsf(r.ny));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
     r.Map = grad_mag(sFxy[(m + ar) * FW + c + ac]);
@@ -389,6 +405,53 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     r.sstar = __fdividef(-(fp - fm) * s, 2.f * (fm + fp - 2.f * mv));
     r.cand = maxt && (fabsf(r.sstar) <= 1.41421356f);  // :478
     return r;
+}
+
+// The seven higher derivatives at 2x-grid slot (m, c) of the step window
+// from the row-pass ring (the Q planes hold the Gxx / Gxxx row responses):
+// fxx, fxy, fyy, fxxy, fxyy, fxxx, fyyy, contracted with the y taps of the
+// point's sub-grid.  Used by the per-edgel stage and, in the corrected-normal
+// mode, by the NMS decision, so that both see identical numbers.
+template <int R>
+__device__ __forceinline__ void gather_hi(const float2* __restrict__ sP, const float4* __restrict__ sTab, int rb, int m,
+                                          int c, float (&d)[7])
+{
+    using C = Cfg<R>;
+    constexpr int NT = C::NT;
+    const int a = m & 1, xe = c >> 1, b = c & 1;
+    const int xv = b ? 2 : (a ? 1 : 0);
+    const int yv = a ? 2 : (b ? 1 : 0);
+    const float2* Pp = sP + xv * C::RING * kExt + xe;
+    const float2* Qp = sP + (3 + xv) * C::RING * kExt + xe;
+    const float4* tab = sTab + yv * NT;
+    float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
+    const int h0 = rb + (m >> 1);
+#pragma unroll
+    for (int kk = 0; kk < NT; ++kk) {
+        const int ph = ring_wrap<C::RING>(h0 + kk) * kExt;
+        const float2 hp = Pp[ph];
+        const float2 hq = Qp[ph];
+        const float4 t = tab[NT - 1 - kk];
+        fxy = fmaf(hp.y, t.y, fxy);
+        fyy = fmaf(hp.x, t.z, fyy);
+        fxyy = fmaf(hp.y, t.z, fxyy);
+        fyyy = fmaf(hp.x, t.w, fyyy);
+        fxx = fmaf(hq.x, t.x, fxx);
+        fxxy = fmaf(hq.x, t.y, fxxy);
+        fxxx = fmaf(hq.y, t.x, fxxx);
+    }
+    d[0] = fxx; d[1] = fxy; d[2] = fyy; d[3] = fxxy; d[4] = fxyy; d[5] = fxxx; d[6] = fyyy;
+}
+
+// The third-order vector (cpu_toed.cpp:227-230) in FP32 with its shared
+// products factored out (the corrected-normal direction of the NMS).
+__device__ __forceinline__ void to_vec32(float gx, float gy, const float (&d)[7], float* tix, float* tiy)
+{
+    const float fxx = d[0], fxy = d[1], fyy = d[2], fxxy = d[3], fxyy = d[4], fxxx = d[5], fyyy = d[6];
+    const float a2 = fmaf(fxx, fxx, fxy * fxy), c2 = fmaf(fyy, fyy, fxy * fxy), bc = fxy * (fxx + fyy);
+    const float pxy = gx * gy, x2 = gx * gx, y2 = gy * gy;
+    *tix = fmaf(2.f, fmaf(gx, a2, fmaf(gy, bc, pxy * fxxy)), fmaf(y2, fxyy, x2 * fxxx));
+    *tiy = fmaf(2.f, fmaf(gx, bc, fmaf(gy, c2, pxy * fxyy)), fmaf(x2, fxxy, y2 * fyyy));
 }
 
 // Per-edgel epilogue from a deferred record: peak fit (FP64 in HYB mode:
@@ -498,8 +561,9 @@ static __device__ __noinline__ bool wait_ready(const int* flag, int epoch, int s
 }
 
 // ASYNC: input rows by per-thread async copies (images with tma == 2) or
-// plain loads; otherwise by TMA (tma == 1) or plain loads.
-template <int R, bool HYB, bool ASYNC>
+// plain loads; otherwise by TMA (tma == 1) or plain loads.  NMSTO: NMS and
+// peak fit along the corrected normal (TOED_NMS_TO_NORMAL).
+template <int R, bool HYB, bool ASYNC, bool NMSTO = false>
 __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(const __grid_constant__ BatchParams p)
 {
     using C = Cfg<R>;
@@ -750,7 +814,16 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 bool acc = false;
                 if (e < LA) {
                     rec = sList[e];
-                    acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr).cand;
+                    if (NMSTO) {
+                        const int m = rec >> 8, c = rec & 255;
+                        float d7[7], tx, ty;
+                        gather_hi<R>(sP, sTab, rb, m, c, d7);
+                        const float2 g = sFxy[m * C::FW + c];
+                        to_vec32(g.x, g.y, d7, &tx, &ty);
+                        acc = nms_eval<true>(sFxy, m, c, p.thr, tx, ty).cand;
+                    } else {
+                        acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr).cand;
+                    }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
                 int* wc = sWarp + (kThreads / 32) * rd;
@@ -806,29 +879,19 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     for (int j = tid - 32; wid > 0 && j < chunk; j += kThreads - 32) {
                         const unsigned rec = sList[j0 + j];
                         const int m = rec >> 8, c = rec & 255;
-                        const int a = m & 1, xe = c >> 1, b = c & 1;
-                        const int xv = b ? 2 : (a ? 1 : 0);
-                        const int yv = a ? 2 : (b ? 1 : 0);
-                        const float2* Pp = sP + xv * C::RING * kExt + xe;
-                        const float2* Qp = sP + (3 + xv) * C::RING * kExt + xe;
-                        const float4* tab = sTab + yv * NT;
-                        float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
-                        const int h0 = rb + (m >> 1);
-#pragma unroll
-                        for (int kk = 0; kk < NT; ++kk) {
-                            const int ph = ring_wrap<C::RING>(h0 + kk) * kExt;
-                            const float2 hp = Pp[ph];
-                            const float2 hq = Qp[ph];
-                            const float4 t = tab[NT - 1 - kk];
-                            fxy = fmaf(hp.y, t.y, fxy);
-                            fyy = fmaf(hp.x, t.z, fyy);
-                            fxyy = fmaf(hp.y, t.z, fxyy);
-                            fyyy = fmaf(hp.x, t.w, fyyy);
-                            fxx = fmaf(hq.x, t.x, fxx);
-                            fxxy = fmaf(hq.x, t.y, fxxy);
-                            fxxx = fmaf(hq.y, t.x, fxxx);
+                        float d7[7];
+                        gather_hi<R>(sP, sTab, rb, m, c, d7);
+                        const float fxx = d7[0], fxy = d7[1], fyy = d7[2], fxxy = d7[3], fxyy = d7[4],
+                                    fxxx = d7[5], fyyy = d7[6];
+                        NmsEval e;
+                        if (NMSTO) {
+                            const float2 g = sFxy[m * C::FW + c];
+                            float tx, ty;
+                            to_vec32(g.x, g.y, d7, &tx, &ty);
+                            e = nms_eval<true>(sFxy, m, c, p.thr, tx, ty);
+                        } else {
+                            e = nms_eval(sFxy, m, c, p.thr);
                         }
-                        const NmsEval e = nms_eval(sFxy, m, c, p.thr);
                         const int Gr = gr_base + m, Gc = gc_base + c;
                         float* rc = sRec + (nrec + j) * C::RECW;
                         rc[0] = e.gx; rc[1] = e.gy; rc[2] = e.mv; rc[3] = e.nx; rc[4] = e.ny; rc[5] = e.slope;

@@ -6,11 +6,14 @@
 
 #define TOED_DETECT_INSTANCE(R)                                                    \
     namespace toed {                                                               \
-    DetectEntry detect_entry_r##R(bool hyb, bool async)                            \
+    DetectEntry detect_entry_r##R(bool hyb, bool async, bool nmsto)                \
     {                                                                              \
         DetectEntry e;                                                             \
         e.smem = Cfg<R>::smem;                                                     \
-        if (async)                                                                 \
+        if (nmsto)                                                                 \
+            e.func = hyb ? (const void*)toed_detect_kernel<R, true, false, true>   \
+                         : (const void*)toed_detect_kernel<R, false, false, true>; \
+        else if (async)                                                            \
             e.func = hyb ? (const void*)toed_detect_kernel<R, true, true>          \
                          : (const void*)toed_detect_kernel<R, false, true>;        \
         else                                                                       \

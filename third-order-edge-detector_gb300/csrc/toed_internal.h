@@ -15,8 +15,9 @@ struct DetectEntry {
 };
 
 // Per-radius instantiations (toed_detect_r<R>.cu); hyb selects the FP64
-// epilogue, async the variant that stages rows by per-thread async copies.
-DetectEntry detect_entry(int radius, bool hyb, bool async = false);
+// epilogue, async the variant that stages rows by per-thread async copies,
+// nmsto the corrected-normal NMS (rows by TMA or plain loads).
+DetectEntry detect_entry(int radius, bool hyb, bool async = false, bool nmsto = false);
 
 cudaError_t launch_finalize(const BatchParams& p, cudaStream_t stream);
 // Load the ordering pass' kernels for `radius` (and the QaD variant) now:

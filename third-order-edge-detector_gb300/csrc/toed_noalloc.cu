@@ -70,12 +70,13 @@ constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 unsigned char* g_dev_scratch[kMaxDevices] = {};
 int g_dev_sms[kMaxDevices] = {};
-int g_dev_bps[kMaxDevices][TOED_MAX_RADIUS + 1][2] = {};  // resident CTAs per SM [radius][hybrid]
+int g_dev_bps[kMaxDevices][TOED_MAX_RADIUS + 1][2][2] = {};  // resident CTAs per SM [radius][hybrid][TO normal]
 
 // Device address of g_noalloc_scratch on `dev` (current), the device's SM
 // count and the detection kernel's occupancy, looked up once per device
 // (and radius / precision) so that later calls make no such queries.
-cudaError_t device_setup(int dev, int r, bool hyb, const DetectEntry& ent, unsigned char** base, int* sms, int* bps)
+cudaError_t device_setup(int dev, int r, bool hyb, bool nmsto, const DetectEntry& ent, unsigned char** base, int* sms,
+                         int* bps)
 {
     std::lock_guard<std::mutex> lk(g_mu);
     if (!g_dev_scratch[dev]) {
@@ -88,7 +89,7 @@ cudaError_t device_setup(int dev, int r, bool hyb, const DetectEntry& ent, unsig
         g_dev_sms[dev] = n;
         g_dev_scratch[dev] = static_cast<unsigned char*>(ptr);
     }
-    int& b = g_dev_bps[dev][r][hyb ? 1 : 0];
+    int& b = g_dev_bps[dev][r][hyb ? 1 : 0][nmsto ? 1 : 0];
     if (b == 0) {
         cudaError_t e = cudaFuncSetAttribute(ent.func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ent.smem);
         if (e != cudaSuccess) return e;
@@ -120,19 +121,24 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     if (prm->out_dtype != TOED_F32 && prm->out_dtype != TOED_F64) return TOED_ERR_INVALID_ARG;
     if (prm->precision != TOED_HYBRID && prm->precision != TOED_FP32) return TOED_ERR_INVALID_ARG;
     if (prm->orientation != TOED_ORI_GRID && prm->orientation != TOED_ORI_QAD) return TOED_ERR_INVALID_ARG;
+    if (prm->nms_direction != TOED_NMS_GRADIENT && prm->nms_direction != TOED_NMS_TO_NORMAL)
+        return TOED_ERR_INVALID_ARG;
+    if (prm->nms_direction == TOED_NMS_TO_NORMAL && prm->orientation != TOED_ORI_GRID) return TOED_ERR_UNSUPPORTED;
     // the fixed scratch bounds the image and the edgel capacity
     if (im->height > kNaMaxDim || im->width > kNaMaxDim || (long long)im->height * im->width > kNaMaxPixels ||
         im->capacity > kNaMaxEdgels)
         return TOED_ERR_CAPACITY;
     const int r = prm->radius > 0 ? prm->radius : (int)std::ceil(4.0 * (double)prm->sigma);
     if (r < 1 || r > TOED_MAX_RADIUS) return TOED_ERR_UNSUPPORTED;
-    const DetectEntry ent = detect_entry(r, prm->precision != TOED_FP32);
+    const bool nmsto = prm->nms_direction == TOED_NMS_TO_NORMAL;
+    const DetectEntry ent = detect_entry(r, prm->precision != TOED_FP32, false, nmsto);
     if (!ent.func) return TOED_ERR_UNSUPPORTED;
 
     int dev = 0, sms = 0, bps = 0;
     if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) return TOED_ERR_CUDA;
     unsigned char* base = nullptr;
-    if (device_setup(dev, r, prm->precision != TOED_FP32, ent, &base, &sms, &bps) != cudaSuccess) return TOED_ERR_CUDA;
+    if (device_setup(dev, r, prm->precision != TOED_FP32, nmsto, ent, &base, &sms, &bps) != cudaSuccess)
+        return TOED_ERR_CUDA;
 
     BatchParams p;  // on the stack: no heap allocation either
     std::memset(&p, 0, sizeof(p));
@@ -145,6 +151,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     p.radius = r;
     p.hyb = prm->precision != TOED_FP32 ? 1 : 0;
     p.qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
+    p.nms_to = nmsto ? 1 : 0;
     p.stage_blk = 1;  // staging sized to the capacity exactly: reserve each step's edgels alone
     // strip height: the tallest of 254 / 126 / 62 / 30 / 14 rows that still
     // gives every resident CTA a few strips
