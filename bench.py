@@ -489,6 +489,27 @@ def side_measurements(toed, det, images, side, stream):
     oracle.subpix_to_correct(E0, 0.1, 2.0, 2.0, nthreads=os.cpu_count())
     cpu_s = time.perf_counter() - t0
     out["subpix_8x2048"]["cpu_port_mpx_s_one_map"] = round(E0.size / cpu_s / 1e6, 2)
+    # precision against the FP64 oracle on the first two maps (edgels matched by position)
+    from scipy.spatial import cKDTree
+    res5 = det.subpix_to_correct_batch(c5[:2], thresh=0.1, sigma=2.0, nbr_radius=2.0, out_dtype=toed.TOED_F64,
+                                       dense=False)
+    n_ref = n_match = n_got = 0
+    pe_max = oe_max = 0.0
+    oe_all = []
+    for E, r5 in zip(side["c5"][:2], res5):
+        ref = oracle.subpix_to_correct(E.astype(np.float64), 0.1, 2.0, 2.0, nthreads=os.cpu_count())["edges"]
+        got = r5["edgels"].cpu().numpy()
+        dd, jj = cKDTree(got[:, :2]).query(ref[:, :2], k=1)
+        ok = dd < 0.05
+        oe = np.abs(np.angle(np.exp(1j * (ref[ok, 2] - got[jj[ok], 2]))))
+        n_ref, n_got, n_match = n_ref + len(ref), n_got + len(got), n_match + int(ok.sum())
+        pe_max, oe_max = max(pe_max, float(dd[ok].max())), max(oe_max, float(oe.max()))
+        oe_all.append(oe)
+    oe_all = np.concatenate(oe_all)
+    out["subpix_8x2048"].update({"agreement": round(n_match / max(n_ref, n_got), 6), "pos_err_max_px": float(f"{pe_max:.3g}"),
+                                 "ori_err_max_rad": float(f"{oe_max:.3g}"),
+                                 "ori_err_p99_rad": float(f"{np.quantile(oe_all, .99):.3g}"),
+                                 "precision_sample": "maps 0 and 1 vs the FP64 oracle", "n_ref": n_ref})
     # -- config 2: precision vs the FP64 oracle ---------------------------
     prec = {}
     for name in ("c2_1080", "c2_2160"):

@@ -90,6 +90,8 @@ typedef enum toed_nms_direction {
 #define TOED_FLAG_OVER_CAPACITY 0x1 /* some image found more edgels than its capacity */
 #define TOED_FLAG_STAGING_FULL 0x2  /* the context staging buffer overflowed */
 #define TOED_FLAG_TIMEOUT 0x4       /* a bounded wait for an input copy gave up (results incomplete) */
+#define TOED_FLAG_BOUNDS 0x8        /* bounds-checked debug library only: an index check failed and the
+                                       access was skipped */
 
 typedef struct toed_ctx toed_ctx;
 

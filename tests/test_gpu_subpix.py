@@ -28,7 +28,7 @@ def _match(ref, got, tol=0.05):
     return np.flatnonzero(ok), j[ok]
 
 
-def _check(ref, got, agree=0.999, pos=1e-3, ori=1e-3, mag=1e-4):
+def _check(ref, got, agree=0.999, pos=1e-3, ori=1e-4, mag=1e-4):
     ia, ib = _match(ref, got)
     n = max(len(ref), len(got))
     a = len(ia) / n if n else 1.0
@@ -60,7 +60,8 @@ def test_golden(detector, toed, case, dt):
              interp_n=interp_n)
     got = r["edgels"].cpu().numpy()
     assert r["count"] == len(got)
-    _check(g["edges"], got)
+    # a float32 map is not the reference's map: its rounding moves the edgels themselves
+    _check(g["edges"], got, ori=1e-4 if dt == np.float64 else 1e-3)
     # dense maps: same support up to the few edgels that moved across a rounding boundary
     TE = r["TO_E"].cpu().numpy()
     assert ((TE != 0) != (g["TO_E"] != 0)).sum() <= max(2, 0.002 * (g["TO_E"] != 0).sum())

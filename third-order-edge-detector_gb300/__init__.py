@@ -24,7 +24,10 @@ import os
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(HERE, "libtoed_gb300.so")
+# TOED_LIBRARY selects another build of the library (the bounds-checked
+# libtoed_gb300_debug.so, in a process of its own); default: the release build
+LIB_PATH = os.environ.get("TOED_LIBRARY") or os.path.join(HERE, "libtoed_gb300.so")
+LIB_DEBUG_PATH = os.path.join(HERE, "libtoed_gb300_debug.so")
 
 TOED_OK, TOED_ERR_INVALID_ARG, TOED_ERR_CAPACITY, TOED_ERR_CUDA, TOED_ERR_TIMEOUT, \
     TOED_ERR_UNSUPPORTED, TOED_ERR_CAPTURE = range(7)
@@ -109,15 +112,16 @@ class toed_tuning(ctypes.Structure):
 _LIB = None
 
 
-def build(verbose: bool = False) -> str:
-    """Compile libtoed_gb300.so (nvcc, sm_103a) in-tree."""
+def build(verbose: bool = False, debug: bool = False) -> str:
+    """Compile libtoed_gb300.so (nvcc, sm_103a) in-tree; with ``debug`` the
+    bounds-checked libtoed_gb300_debug.so."""
     sys.path.insert(0, HERE)
     try:
         import importlib.util
         spec = importlib.util.spec_from_file_location("_toed_build", os.path.join(HERE, "build.py"))
         m = importlib.util.module_from_spec(spec)
         spec.loader.exec_module(m)
-        return m.build(verbose=verbose)
+        return m.build(verbose=verbose, debug=debug)
     finally:
         sys.path.remove(HERE)
 

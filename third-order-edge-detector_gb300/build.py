@@ -3,6 +3,11 @@
 Every csrc/*.cu is compiled in parallel with nvcc (one -gencode, no cmake)
 and linked into ``libtoed_gb300.so`` next to this file.  Objects go to
 ``_build/`` (git-ignored).  Rebuilds are incremental on source mtimes.
+
+``build(debug=True)`` builds the bounds-checked variant instead
+(-DTOED_DEBUG_BOUNDS: every guarded shared- and global-memory index of the
+detection kernel is checked, a failure skips the access and raises
+TOED_FLAG_BOUNDS): ``libtoed_gb300_debug.so``, objects in ``_build_debug/``.
 """
 from __future__ import annotations
 
@@ -17,6 +22,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libtoed_gb300.so")
+BUILD_DEBUG = os.path.join(HERE, "_build_debug")
+LIB_DEBUG = os.path.join(HERE, "libtoed_gb300_debug.so")
 INCLUDE = os.path.abspath(os.path.join(HERE, "..", "include"))
 ARCH = "-gencode=arch=compute_103a,code=sm_103a"
 
@@ -45,13 +52,15 @@ def _stale(src: str, obj: str, hdr_mtime: float) -> bool:
     return m < os.path.getmtime(src) or m < hdr_mtime
 
 
-def build(verbose: bool = False, jobs: int | None = None) -> str:
-    os.makedirs(BUILD, exist_ok=True)
+def build(verbose: bool = False, jobs: int | None = None, debug: bool = False) -> str:
+    bdir, lib = (BUILD_DEBUG, LIB_DEBUG) if debug else (BUILD, LIB)
+    extra = ["-DTOED_DEBUG_BOUNDS"] if debug else []
+    os.makedirs(bdir, exist_ok=True)
     srcs = sorted(glob.glob(os.path.join(CSRC, "*.cu")))
     hdr_mtime = max([os.path.getmtime(h) for h in _headers()] + [0.0])
     objs, todo = [], []
     for s in srcs:
-        o = os.path.join(BUILD, os.path.basename(s) + ".o")
+        o = os.path.join(bdir, os.path.basename(s) + ".o")
         objs.append(o)
         if _stale(s, o, hdr_mtime):
             todo.append((s, o))
@@ -59,7 +68,7 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
 
     def compile_one(so):
         s, o = so
-        cmd = [cc] + _flags() + ["-c", s, "-o", o]
+        cmd = [cc] + _flags() + extra + ["-c", s, "-o", o]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {os.path.basename(s)}:\n{r.stderr}")
@@ -73,13 +82,15 @@ def build(verbose: bool = False, jobs: int | None = None) -> str:
             for s in ex.map(compile_one, todo):
                 if verbose:
                     print("compiled", os.path.basename(s))
-    if todo or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(o) for o in objs):
-        tmp = LIB + ".tmp"
+    if todo or not os.path.exists(lib) or os.path.getmtime(lib) < max(os.path.getmtime(o) for o in objs):
+        tmp = lib + ".tmp"
         cmd = [cc, ARCH, "-shared", "-o", tmp] + objs + ["-lcudart_static", "-lrt", "-lpthread", "-ldl"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError("link failed:\n" + r.stderr)
-        os.replace(tmp, LIB)
+        os.replace(tmp, lib)
+    if debug:
+        return lib
     build_driver(verbose)
     return LIB
 

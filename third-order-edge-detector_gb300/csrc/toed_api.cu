@@ -12,6 +12,7 @@
 #include <vector>
 
 #include <cudaTypedefs.h>
+#include <nvtx3/nvToolsExt.h>
 
 #include "toed_common.cuh"
 #include "toed_internal.h"
@@ -124,6 +125,13 @@ void encode_rows_map(CUtensorMap* m, DetImage& d, int r)
 
 using namespace toed;
 
+// NVTX range over one phase of a call (the detection launch, the ordering
+// pass, a copy group, ...): no cost unless a profiler is attached.
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+};
+
 static thread_local std::string g_last_cuda_error;
 
 #define TOED_CU(call)                                                                 \
@@ -138,7 +146,7 @@ static thread_local std::string g_last_cuda_error;
 struct toed_ctx {
     int device = 0;
     int num_sms = 0;
-    int* words = nullptr;  // [0] queue [1] cursor [2] flags [3] refine-list length
+    int* words = nullptr;  // kWords: [0] queue [1] cursor [2] flags [3] refine-list length [4] debug
     double4_32a* staging = nullptr;
     int* staging_idx = nullptr;
     long long staging_cap = 0;
@@ -233,8 +241,8 @@ toed_status toed_create(toed_ctx** out, int device)
     toed_ctx* c = new toed_ctx();
     c->device = device;
     cudaError_t e = cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
-    if (e == cudaSuccess) e = cudaMalloc(&c->words, 4 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(c->words, 0, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&c->words, kWords * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->words, 0, kWords * sizeof(int));
     cudaSetDevice(prev);
     if (e != cudaSuccess) {
         g_last_cuda_error = cudaGetErrorString(e);
@@ -466,6 +474,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->sc.staging_idx = c->staging_idx;
     p->sc.staging_cap = c->staging_cap;
     p->sc.seg = c->seg;
+    p->sc.seg_cap = c->seg_cap;
     p->sc.tile_sum = c->tile_sum;
     p->sc.img_base = c->img_base;
     // FP64 orientation recomputation: hybrid precision, grid orientation
@@ -475,7 +484,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
 
     // the first chunk clears the flags and the refine-list length too; later
     // chunks find the list emptied by the previous ordering pass
-    TOED_CU(cudaMemsetAsync(c->words, 0, (first_chunk ? 4 : 2) * sizeof(int), stream));
+    TOED_CU(cudaMemsetAsync(c->words, 0, (first_chunk ? kWords : 2) * sizeof(int), stream));
     const int grid = (int)std::min<long long>(units, resident);
     void* args[] = {p};
     cudaEvent_t ev0 = nullptr, ev1 = nullptr;
@@ -485,9 +494,15 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         c->prof.emplace_back(ev0, ev1);
         TOED_CU(cudaEventRecord(ev0, stream));
     }
-    TOED_CU(cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream));
+    {
+        NvtxRange r("toed: detection launch");
+        TOED_CU(cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream));
+    }
     if (ev1) TOED_CU(cudaEventRecord(ev1, stream));
-    TOED_CU(launch_finalize(*p, stream));
+    {
+        NvtxRange r("toed: ordering pass");
+        TOED_CU(launch_finalize(*p, stream));
+    }
     return TOED_OK;
 }
 
@@ -528,6 +543,7 @@ static toed_status detect_all(toed_ctx* c, const toed_image* images, int n, cons
 extern "C" toed_status toed_detect_batch(toed_ctx* c, const toed_image* images, int n,
                                          const toed_params* prm, cudaStream_t stream)
 {
+    NvtxRange nv("toed_detect_batch");
     toed_status st = check_batch(c, images, n, prm);
     if (st != TOED_OK) return st;
     int prev = 0;
@@ -548,6 +564,7 @@ extern "C" toed_status toed_detect_batch(toed_ctx* c, const toed_image* images, 
 extern "C" toed_status toed_autotune(toed_ctx* c, const toed_image* images, int n, const toed_params* prm,
                                      int reps, cudaStream_t stream, toed_tuning* best)
 {
+    NvtxRange nv("toed_autotune");
     toed_status st = check_batch(c, images, n, prm);
     if (st != TOED_OK) return st;
     if (reps < 1) return TOED_ERR_INVALID_ARG;
@@ -648,6 +665,7 @@ static bool launches_serialised()
 extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image* images, int n,
                                               const toed_params* prm, int chunks, cudaStream_t stream)
 {
+    NvtxRange nv("toed_detect_host_batch");
     if (!c || !images || n <= 0 || !prm) return TOED_ERR_INVALID_ARG;
     std::vector<toed_image> dev(n);
     std::vector<long long> in_off(n), out_off(n), idx_off(n);
@@ -846,6 +864,7 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
         TOED_HB(cudaEventRecord(ev_det[0], stream));
         for (int k = 0; k < chunks; ++k) {
+            NvtxRange r("toed: copy group");
             TOED_HB(copy_group(k));
             if (k != withhold)
                 TOED_HB(cudaMemcpyAsync(c->hb_ready + k, c->hb_epoch_src, sizeof(int), cudaMemcpyHostToDevice,
@@ -871,6 +890,7 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
     // 3. per group: counts (and the group's device flags) to the host, then
     // the lists, while later groups are still being copied in or detected
     int flags = 0;
+    NvtxRange wait_range("toed: wait for counts and lists");
     if (direct) {
         TOED_HB(cudaMemcpyAsync(c->hb_cnt_host + n, c->hb_cnt + n, sizeof(int) * launches, cudaMemcpyDeviceToHost,
                                 stream));
@@ -954,6 +974,7 @@ extern "C" toed_status toed_profile_end(toed_ctx* c, double* kernel_ms, int* lau
 extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edgemap* maps, int n,
                                                     const toed_subpix_params* prm, cudaStream_t stream)
 {
+    NvtxRange nv("toed_subpix_to_correct_batch");
     if (!c || !maps || n <= 0 || !prm) return TOED_ERR_INVALID_ARG;
     if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma) || !std::isfinite(prm->thresh) ||
         !std::isfinite(prm->nbr_radius))
@@ -1008,6 +1029,7 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
             s.sc.staging_idx = c->staging_idx;
             s.sc.staging_cap = std::min(c->staging_cap, c->keep_cap);
             s.sc.seg = c->seg;
+            s.sc.seg_cap = c->seg_cap;
             s.sc.tile_sum = c->tile_sum;
             s.sc.img_base = c->img_base;
             s.dir = c->dir;
@@ -1030,6 +1052,7 @@ extern "C" toed_status toed_subpix_to_correct_batch(toed_ctx* c, const toed_edge
 extern "C" toed_status toed_backward_batch(toed_ctx* c, const toed_grad_image* items, int n, const toed_params* prm,
                                            double* grad_sigma, cudaStream_t stream)
 {
+    NvtxRange nv("toed_backward_batch");
     if (!c || !items || n <= 0 || !prm || !grad_sigma) return TOED_ERR_INVALID_ARG;
     if (!(prm->sigma > 0.f) || !std::isfinite(prm->sigma)) return TOED_ERR_INVALID_ARG;
     // the adjoint is that of the grid-point orientation (cpu_toed.cpp:227-232)

@@ -38,6 +38,27 @@ constexpr float kRefineKappa = 20.f;
 // skips the units whose pixels have not arrived (BatchParams::ready_spins).
 constexpr int kReadySpinLimit = 1 << 24;
 
+// Bounds-checked builds (-DTOED_DEBUG_BOUNDS, a separate debug library):
+// TOED_IN_BOUNDS(cond, words) guards a shared- or global-memory access; a
+// failed check skips the access, sets TOED_FLAG_BOUNDS in words[2] and
+// records the source line of the first failure in words[4] -- a status the
+// host reads, never a trap.  In release builds the macro is `true` and every
+// guard compiles away.
+#ifdef TOED_DEBUG_BOUNDS
+__device__ __forceinline__ bool debug_in_bounds(bool ok, int* words, int line)
+{
+    if (!ok) {
+        atomicOr(&words[2], TOED_FLAG_BOUNDS);
+        atomicCAS(&words[4], 0, line);
+    }
+    return ok;
+}
+#define TOED_IN_BOUNDS(cond, words) ::toed::debug_in_bounds((cond), (words), __LINE__)
+#else
+#define TOED_IN_BOUNDS(cond, words) true
+#endif
+constexpr int kWords = 8;  // scratch words: [0] queue [1] cursor [2] flags [3] refine length [4] first bad line
+
 // 1-D taps, index k <-> offset x = k - (r+1) (+0.5 for the shifted set).
 // Filters: 0 G, 1 Gx, 2 Gxx, 3 Gxxx, 4..7 the same shifted by +0.5.
 // Passed by value as a kernel parameter, so unrolled loops read each tap as
@@ -74,11 +95,13 @@ struct DetImage {
 };
 
 struct Scratch {
-    int* words;          // [0] unit queue, [1] staging cursor, [2] flags, [3] refine-list length
+    int* words;          // kWords: [0] unit queue, [1] staging cursor, [2] flags, [3] refine-list length,
+                         // [4] (bounds-checked builds) source line of the first failed check
     double4_32a* staging;  // staged edgels (x, y, orientation, strength)
     int* staging_idx;
     long long staging_cap;
     int2* seg;           // per segment {staging offset, count}
+    long long seg_cap;   // segments `seg` holds
     int* tile_sum;       // per ordering tile
     long long* img_base; // per image: exclusive prefix of its first segment
     int4* refine;        // edgels whose orientation is recomputed in FP64: {staging slot, image, Gr, Gc}

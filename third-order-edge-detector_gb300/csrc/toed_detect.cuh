@@ -198,7 +198,7 @@ __device__ __forceinline__ void async_issue_box(float* rawf, const float* fsrc, 
 template <int R>
 __device__ __forceinline__ void stage_rows_async(float* __restrict__ sIn, unsigned char* sRaw, const float* fsrc,
                                                  long long pitch, int H, int W, int xin, int ys, int s, int nsteps,
-                                                 int rb)
+                                                 int rb, int* dbg)
 {
     using C = Cfg<R>;
     using A = AsyncBox<R>;
@@ -224,7 +224,11 @@ __device__ __forceinline__ void stage_rows_async(float* __restrict__ sIn, unsign
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int cc = 4 * k + e - shift;  // ring column
-                    if (cc >= 0 && cc < C::NIN) dst[cc] = src[e];
+                    if (cc >= 0 && cc < C::NIN &&
+                        TOED_IN_BOUNDS(ring_wrap<C::RING>(a0 + rr) < C::RING &&
+                                           (q & 1) * (B * A::BW) + rr * A::BW + 4 * k + e < 2 * B * A::BW,
+                                       dbg))
+                        dst[cc] = src[e];
                 }
             }
         }
@@ -241,13 +245,14 @@ __device__ __forceinline__ void stage_rows_async(float* __restrict__ sIn, unsign
 // ---------------------------------------------------------------------------
 template <int R>
 __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int p0, int nrows,
-                                         float2* __restrict__ sP, const TapBlock& tp)
+                                         float2* __restrict__ sP, const TapBlock& tp, int* dbg)
 {
     using C = Cfg<R>;
     constexpr int NV = 2 * R + 4;
     for (int item = threadIdx.x; item < nrows * (kExt / 2); item += kThreads) {
         const int i = item / (kExt / 2), k = item % (kExt / 2);
         const int ph = ring_wrap<C::RING>(p0 + i);
+        if (!TOED_IN_BOUNDS(ph < C::RING && 2 * k + NV <= C::NIN, dbg)) continue;
         const float2* src = reinterpret_cast<const float2*>(sIn + ph * C::NIN + 2 * k);
         float v[NV];
 #pragma unroll
@@ -362,7 +367,7 @@ struct NmsEval {
 // candidate tests (threshold, gradient epsilon) stay those of the reference.
 template <bool TOD = false>
 __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int m, int c, float thr,
-                                            float tx = 0.f, float ty = 0.f)
+                                            float tx = 0.f, float ty = 0.f, int* dbg = nullptr)
 {
     NmsEval r;
     r.cand = false;
@@ -392,6 +397,9 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     const int sx = (dx >= 0.f) ? 1 : -1, sy = (dy >= 0.f) ? 1 : -1;
     r.slope = xmaj ? __fdividef(fabsf(r.ny), fabsf(r.nx)) : __fdividef(fabsf(r.nx), fabsf(r.ny));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+#ifdef TOED_DEBUG_BOUNDS
+    if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return r;
+#endif
     r.Map = grad_mag(sFxy[(m + ar) * FW + c + ac]);
     r.Mdp = grad_mag(sFxy[(m + sy) * FW + c + sx]);
     r.Mam = grad_mag(sFxy[(m - ar) * FW + c - ac]);
@@ -414,7 +422,7 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 // mode, by the NMS decision, so that both see identical numbers.
 template <int R>
 __device__ __forceinline__ void gather_hi(const float2* __restrict__ sP, const float4* __restrict__ sTab, int rb, int m,
-                                          int c, float (&d)[7])
+                                          int c, float (&d)[7], int* dbg = nullptr)
 {
     using C = Cfg<R>;
     constexpr int NT = C::NT;
@@ -426,6 +434,12 @@ __device__ __forceinline__ void gather_hi(const float2* __restrict__ sP, const f
     const float4* tab = sTab + yv * NT;
     float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
     const int h0 = rb + (m >> 1);
+#ifdef TOED_DEBUG_BOUNDS
+    if (!TOED_IN_BOUNDS(xe >= 0 && xe < kExt && h0 >= 0 && h0 + NT - 1 < 2 * C::RING, dbg)) {
+        for (int f = 0; f < 7; ++f) d[f] = 0.f;
+        return;
+    }
+#endif
 #pragma unroll
     for (int kk = 0; kk < NT; ++kk) {
         const int ph = ring_wrap<C::RING>(h0 + kk) * kExt;
@@ -626,7 +640,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 // segments are written empty, so the ordering pass reads no
                 // stale entries) and the call reports TOED_ERR_TIMEOUT
                 for (int i = tid; i < 2 * S_act; i += kThreads)
-                    p.sc.seg[im.seg_base + (long long)(2 * ys + i) * im.nsc + sc] = make_int2(0, 0);
+                    if (TOED_IN_BOUNDS(im.seg_base + (long long)(2 * ys + i) * im.nsc + sc < p.sc.seg_cap, p.sc.words))
+                        p.sc.seg[im.seg_base + (long long)(2 * ys + i) * im.nsc + sc] = make_int2(0, 0);
                 continue;
             }
         }
@@ -655,7 +670,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             // s*B - R - 2 + h <-> image row ys - 1 + ext row
             // ---- 1. input rows -> input ring (FP32, zero padded) -----------
             if (ASYNC && im.tma == 2) {
-                stage_rows_async<R>(sIn, sRaw, static_cast<const float*>(src), pitch, H, W, xin, ys, s, nsteps, rb);
+                stage_rows_async<R>(sIn, sRaw, static_cast<const float*>(src), pitch, H, W, xin, ys, s, nsteps, rb,
+                                    p.sc.words);
                 __syncthreads();  // every thread's rows are in before the row pass
             } else if (!ASYNC && im.tma == 1) {
                 // rows arrive by TMA (out-of-image texels read as zero, the
@@ -681,7 +697,9 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                             for (int rr = wid; rr < nrows; rr += kThreads / 32) {
                                 float* dst = sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN;
                                 const unsigned char* srow = sRaw + rr * rawpitch + shift;
-                                for (int cc = lane; cc < C::NIN; cc += 32) dst[cc] = (float)srow[cc];
+                                for (int cc = lane; cc < C::NIN; cc += 32)
+                                    if (TOED_IN_BOUNDS(rr * rawpitch + shift + cc < (int)C::sz_raw, p.sc.words))
+                                        dst[cc] = (float)srow[cc];
                             }
                         } else if ((R & 1) == 0) {
                             // even r: the staged row starts 8-byte aligned (shift = xin mod 4 is even)
@@ -690,14 +708,20 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                             for (int rr = wid; rr < nrows; rr += kThreads / 32) {
                                 float2* dst = reinterpret_cast<float2*>(sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN);
                                 const float2* srow = reinterpret_cast<const float2*>(rf + rr * im.tma_boxw + shift);
-                                if (lane < C::NIN / 2) dst[lane] = srow[lane];
+                                if (lane < C::NIN / 2 &&
+                                    TOED_IN_BOUNDS((rr * im.tma_boxw + shift) * 4 + 8 * lane + 8 <= (int)C::sz_raw,
+                                                   p.sc.words))
+                                    dst[lane] = srow[lane];
                             }
                         } else {
                             const float* rf = reinterpret_cast<const float*>(sRaw);
                             for (int rr = wid; rr < nrows; rr += kThreads / 32) {
                                 float* dst = sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN;
                                 const float* srow = rf + rr * im.tma_boxw + shift;
-                                for (int cc = lane; cc < C::NIN; cc += 32) dst[cc] = srow[cc];
+                                for (int cc = lane; cc < C::NIN; cc += 32)
+                                    if (TOED_IN_BOUNDS((rr * im.tma_boxw + shift + cc) * 4 + 4 <= (int)C::sz_raw,
+                                                       p.sc.words))
+                                        dst[cc] = srow[cc];
                             }
                         }
                     }
@@ -720,15 +744,17 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 const int img_row0 = (s == 0) ? ys - R - 3 : ys + s * B + R;
                 for (int i = tid; i < nrows * C::NIN; i += kThreads) {
                     const int rr = i / C::NIN, cc = i - rr * C::NIN;
-                    sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] = fetch_px(src, pitch, H, W, dtype, img_row0 + rr, xin + cc);
+                    if (TOED_IN_BOUNDS(ring_wrap<C::RING>(a0 + rr) < C::RING, p.sc.words))
+                        sIn[ring_wrap<C::RING>(a0 + rr) * C::NIN + cc] =
+                            fetch_px(src, pitch, H, W, dtype, img_row0 + rr, xin + cc);
                 }
                 __syncthreads();
             }
             // ---- 2. row pass ------------------------------------------------
             if (s == 0) {
-                row_pass<R>(sIn, 0, C::HS, sP, tp);
+                row_pass<R>(sIn, 0, C::HS, sP, tp, p.sc.words);
             } else {
-                row_pass<R>(sIn, ring_wrap<C::RING>(rb + 2 * R + 3), B, sP, tp);
+                row_pass<R>(sIn, ring_wrap<C::RING>(rb + 2 * R + 3), B, sP, tp, p.sc.words);
                 // the previous step's last two 2x rows become rows 0 and 1
                 for (int i = tid; i < 2 * C::FW; i += kThreads) sFxy[i] = sFxy[2 * B * C::FW + i];
                 if (tid < 4 * kHalves) sMask[tid] = sMask[2 * B * 2 * kHalves + tid];
@@ -758,7 +784,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 for (int o = 0; o < kColRows; ++o) {
                     const int m = 2 * (g * kColRows + o) + a + 2;
                     const float2 f = make_float2(fx[o], fy[o]);
-                    sFxy[m * C::FW + c] = f;
+                    if (TOED_IN_BOUNDS(m < C::MS && c < C::FW, p.sc.words)) sFxy[m * C::FW + c] = f;
                     const int Gr = gr_base + m;
                     const bool kp = colok && Gr >= row_lo && Gr < row_hi && grad_mag(f) > p.thr;  // cpu_toed.cpp:403
                     const unsigned bal = __ballot_sync(0xffffffffu, kp);
@@ -796,8 +822,9 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                         const bool k0 = (mk0 >> lane) & 1u, k1 = (mk1 >> lane) & 1u;
                         const int pos = pos0 + __popc(mk0 & lt) + __popc(mk1 & lt);
                         const unsigned c0 = 2 * (32 * h + lane);
-                        if (k0) sList[pos] = ((unsigned)m << 8) | c0;
-                        if (k1) sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
+                        if (k0 && TOED_IN_BOUNDS(pos < C::MAXC, p.sc.words)) sList[pos] = ((unsigned)m << 8) | c0;
+                        if (k1 && TOED_IN_BOUNDS(pos + (k0 ? 1 : 0) < C::MAXC, p.sc.words))
+                            sList[pos + (k0 ? 1 : 0)] = ((unsigned)m << 8) | (c0 + 1);
                         pos0 += __popc(mk0) + __popc(mk1);
                     }
                 }
@@ -817,12 +844,12 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     if (NMSTO) {
                         const int m = rec >> 8, c = rec & 255;
                         float d7[7], tx, ty;
-                        gather_hi<R>(sP, sTab, rb, m, c, d7);
+                        gather_hi<R>(sP, sTab, rb, m, c, d7, p.sc.words);
                         const float2 g = sFxy[m * C::FW + c];
                         to_vec32(g.x, g.y, d7, &tx, &ty);
-                        acc = nms_eval<true>(sFxy, m, c, p.thr, tx, ty).cand;
+                        acc = nms_eval<true>(sFxy, m, c, p.thr, tx, ty, p.sc.words).cand;
                     } else {
-                        acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr).cand;
+                        acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr, 0.f, 0.f, p.sc.words).cand;
                     }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
@@ -837,7 +864,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     tot += x;
                 }
                 if (acc) {
-                    sList[nacc + off + __popc(bal & ((1u << lane) - 1u))] = rec;
+                    const int dpos = nacc + off + __popc(bal & ((1u << lane) - 1u));
+                    if (TOED_IN_BOUNDS(dpos < C::MAXC, p.sc.words)) sList[dpos] = rec;
                     atomicAdd(&sAccCnt[(rec >> 8) - 1], 1);
                 }
                 nacc += tot;
@@ -868,7 +896,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 }
                 const int Gr = gr_base + lane + 1;
                 if (Gr >= 2 * ys && Gr < 2 * ys + 2 * S_act)
-                    p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
+                    if (TOED_IN_BOUNDS(seg0 + (long long)Gr * im.nsc + sc < p.sc.seg_cap, p.sc.words))
+                        p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
             }
             // ---- 5. per edgel: the seven higher derivatives from the row-pass
             // ring into a deferred record (the FP64 epilogue runs when the
@@ -880,7 +909,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                         const unsigned rec = sList[j0 + j];
                         const int m = rec >> 8, c = rec & 255;
                         float d7[7];
-                        gather_hi<R>(sP, sTab, rb, m, c, d7);
+                        gather_hi<R>(sP, sTab, rb, m, c, d7, p.sc.words);
                         const float fxx = d7[0], fxy = d7[1], fyy = d7[2], fxxy = d7[3], fxyy = d7[4],
                                     fxxx = d7[5], fyyy = d7[6];
                         NmsEval e;
@@ -893,6 +922,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                             e = nms_eval(sFxy, m, c, p.thr);
                         }
                         const int Gr = gr_base + m, Gc = gc_base + c;
+                        if (!TOED_IN_BOUNDS(nrec + j < C::NREC, p.sc.words)) continue;
                         float* rc = sRec + (nrec + j) * C::RECW;
                         rc[0] = e.gx; rc[1] = e.gy; rc[2] = e.mv; rc[3] = e.nx; rc[4] = e.ny; rc[5] = e.slope;
                         rc[6] = e.Map; rc[7] = e.Mdp; rc[8] = e.Mam; rc[9] = e.Mdm;

@@ -55,7 +55,7 @@ constexpr long long kNaRefine = kNaMaxEdgels / 64 + 1024;  // orientation recomp
 
 constexpr size_t align256(size_t x) { return (x + 255) / 256 * 256; }
 constexpr size_t kOffWords = 0;
-constexpr size_t kOffStaging = align256(kOffWords + 4 * sizeof(int));
+constexpr size_t kOffStaging = align256(kOffWords + kWords * sizeof(int));
 constexpr size_t kOffIdx = align256(kOffStaging + sizeof(double4_32a) * kNaMaxEdgels);
 constexpr size_t kOffSeg = align256(kOffIdx + sizeof(int) * kNaMaxEdgels);
 constexpr size_t kOffTiles = align256(kOffSeg + sizeof(int2) * kNaMaxSegs);
@@ -190,13 +190,14 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     p.sc.staging_idx = reinterpret_cast<int*>(base + kOffIdx);
     p.sc.staging_cap = im->capacity > 0 ? im->capacity : 1;
     p.sc.seg = reinterpret_cast<int2*>(base + kOffSeg);
+    p.sc.seg_cap = kNaMaxSegs;
     p.sc.tile_sum = reinterpret_cast<int*>(base + kOffTiles);
     p.sc.img_base = reinterpret_cast<long long*>(base + kOffBase);
     p.sc.refine = reinterpret_cast<int4*>(base + kOffRefine);
     p.sc.refine_cap = (p.hyb && !p.qad) ? (int)kNaRefine : 0;
 
     // queue, staging cursor, flags and refine-list length start at zero on every call
-    if (cudaMemsetAsync(p.sc.words, 0, 4 * sizeof(int), stream) != cudaSuccess) return TOED_ERR_CUDA;
+    if (cudaMemsetAsync(p.sc.words, 0, kWords * sizeof(int), stream) != cudaSuccess) return TOED_ERR_CUDA;
     const int grid = (int)std::min<long long>(p.n_units, resident);
     void* args[] = {&p};
     if (cudaLaunchKernel(ent.func, dim3(grid), dim3(kThreads), args, ent.smem, stream) != cudaSuccess)

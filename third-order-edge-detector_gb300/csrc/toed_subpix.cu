@@ -93,6 +93,64 @@ __device__ __forceinline__ float load_map(const void* p, int dtype, long long o)
     return dtype == TOED_F64 ? (float)__ldg((const double*)p + o) : __ldg((const float*)p + o);
 }
 
+// ---------------------------------------------------------------------------
+// Double-float arithmetic (an unevaluated sum hi + lo of two floats, about
+// 48 significant bits; Dekker / Knuth error-free transformations with the
+// FMA for products).  The Hessian orientation estimate of the HYBRID mode
+// runs in it: its second differences of the smoothed map cancel, and in
+// plain FP32 the estimated angle at an NMS pixel -- which steers the NMS and
+// hence the subpixel position and the corrected orientation -- is off by up
+// to 1e-4 rad (and its sign of Oxy can flip), at ~1/50 of the FP64 cost.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 df_two_sum(float a, float b)
+{
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return make_float2(s, e);
+}
+__device__ __forceinline__ float2 df_fast_two_sum(float a, float b)  // |a| >= |b| or a == 0
+{
+    const float s = __fadd_rn(a, b);
+    return make_float2(s, __fsub_rn(b, __fsub_rn(s, a)));
+}
+__device__ __forceinline__ float2 df_add(float2 a, float2 b)
+{
+    const float2 s = df_two_sum(a.x, b.x);
+    return df_fast_two_sum(s.x, __fadd_rn(s.y, __fadd_rn(a.y, b.y)));
+}
+__device__ __forceinline__ float2 df_sub(float2 a, float2 b) { return df_add(a, make_float2(-b.x, -b.y)); }
+__device__ __forceinline__ float2 df_mul(float2 a, float2 b)
+{
+    const float p = __fmul_rn(a.x, b.x);
+    float e = fmaf(a.x, b.x, -p);
+    e = fmaf(a.x, b.y, fmaf(a.y, b.x, e));
+    return df_fast_two_sum(p, e);
+}
+__device__ __forceinline__ float2 df_half(float2 a) { return make_float2(0.5f * a.x, 0.5f * a.y); }  // exact
+
+// The triangle filter (:316-321), weight (5 - |k|) / 25, as double-floats.
+template <int K>
+struct TriDF {
+    static constexpr double w = (double)(5 - (K < 0 ? -K : K)) / 25.0;
+    static constexpr float hi = (float)w;
+    static constexpr float lo = (float)(w - (double)hi);
+};
+__device__ __forceinline__ float2 tri_df(int k)
+{
+    switch (k) {
+    case -4: return make_float2(TriDF<-4>::hi, TriDF<-4>::lo);
+    case -3: return make_float2(TriDF<-3>::hi, TriDF<-3>::lo);
+    case -2: return make_float2(TriDF<-2>::hi, TriDF<-2>::lo);
+    case -1: return make_float2(TriDF<-1>::hi, TriDF<-1>::lo);
+    case 0: return make_float2(TriDF<0>::hi, TriDF<0>::lo);
+    case 1: return make_float2(TriDF<1>::hi, TriDF<1>::lo);
+    case 2: return make_float2(TriDF<2>::hi, TriDF<2>::lo);
+    case 3: return make_float2(TriDF<3>::hi, TriDF<3>::lo);
+    default: return make_float2(TriDF<4>::hi, TriDF<4>::lo);
+    }
+}
+
 __device__ __forceinline__ double cubic_w(double s)
 {  // Keys kernel, a = -0.5 (:57-67)
     const double a = -0.5;
@@ -126,8 +184,11 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
     constexpr size_t kTmpB = sizeof(float) * NE * (kT + 4), kSmB = sizeof(float) * (kT + 4) * (kT + 4);
     constexpr size_t kOB = sizeof(float) * (kT + 2) * (kT + 3);
     constexpr size_t kCandB = sizeof(short) * kT * kT, kResB = sizeof(float3) * kT * kT;
-    static_assert(kCandB + kResB <= kTmpB + kSmB + 2 * kOB, "candidates fit the orientation stages");
-    __shared__ __align__(16) unsigned char sStage[kTmpB + kSmB + 2 * kOB];
+    // HYBRID: the triangle rows and the smoothed map as double-floats (no gradient planes)
+    constexpr size_t kStageF = kTmpB + kSmB + 2 * kOB, kStageD = 2 * (kTmpB + kSmB);
+    constexpr size_t kStageB = kStageF > kStageD ? kStageF : kStageD;
+    static_assert(kCandB + kResB <= kStageB, "candidates fit the orientation stages");
+    __shared__ __align__(16) unsigned char sStage[kStageB];
     float(*sTmp)[kT + 4] = reinterpret_cast<float(*)[kT + 4]>(sStage);               // cols j0-2 .. j0+33
     float(*sSm)[kT + 4] = reinterpret_cast<float(*)[kT + 4]>(sStage + kTmpB);        // rows/cols -2 .. +33
     float(*sOx)[kT + 3] = reinterpret_cast<float(*)[kT + 3]>(sStage + kTmpB + kSmB);  // -1 .. +32
@@ -153,7 +214,76 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
     }
     __syncthreads();
 
-    if (M.theta == nullptr) {
+    if (M.theta == nullptr && p.hyb) {
+        // HYBRID: the orientation estimate in double-float arithmetic (see
+        // df_two_sum); the same sums, in the same order, as the FP32 form
+        float2(*sTmpD)[kT + 4] = reinterpret_cast<float2(*)[kT + 4]>(sStage);          // cols j0-2 .. j0+33
+        float2(*sSmD)[kT + 4] = reinterpret_cast<float2(*)[kT + 4]>(sStage + 2 * kTmpB);  // rows/cols -2 .. +33
+        for (int q = tid; q < NE * (kT + 4); q += blockDim.x) {
+            const int a = q / (kT + 4), c = q - a * (kT + 4);
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int qq = -kTriR; qq <= kTriR; ++qq)
+                acc = df_add(acc, df_mul(make_float2(sE[a][c + 4 - qq], 0.f), tri_df(qq)));
+            sTmpD[a][c] = acc;
+        }
+        __syncthreads();
+        for (int q = tid; q < (kT + 4) * (kT + 4); q += blockDim.x) {
+            const int d = q / (kT + 4), c = q - d * (kT + 4);
+            float2 acc = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int pp = -kTriR; pp <= kTriR; ++pp) acc = df_add(acc, df_mul(sTmpD[d + 4 - pp][c], tri_df(pp)));
+            sSmD[d][c] = acc;
+        }
+        __syncthreads();
+        // gradient2 (:346-355) of the smoothed map and of its gradients, at
+        // the tile's pixels, one-sided at the image borders
+        auto sm = [&](int i, int j) { return sSmD[i - i0 + 2][j - j0 + 2]; };
+        auto ox = [&](int i, int j) {
+            return (j == 0) ? df_sub(sm(i, 1), sm(i, 0))
+                            : (j == w - 1 ? df_sub(sm(i, j), sm(i, j - 1)) : df_half(df_sub(sm(i, j + 1), sm(i, j - 1))));
+        };
+        auto oy = [&](int i, int j) {
+            return (i == 0) ? df_sub(sm(1, j), sm(0, j))
+                            : (i == h - 1 ? df_sub(sm(i, j), sm(i - 1, j)) : df_half(df_sub(sm(i + 1, j), sm(i - 1, j))));
+        };
+        for (int q = tid; q < kT * kT; q += blockDim.x) {
+            const int a = q >> 5, b = q & 31;
+            const int i = i0 + a, j = j0 + b;
+            if (i >= h || j >= w) continue;
+            const float2 oxx = (j == 0) ? df_sub(ox(i, 1), ox(i, 0))
+                                        : (j == w - 1 ? df_sub(ox(i, j), ox(i, j - 1))
+                                                      : df_half(df_sub(ox(i, j + 1), ox(i, j - 1))));
+            const float2 oxy = (j == 0) ? df_sub(oy(i, 1), oy(i, 0))
+                                        : (j == w - 1 ? df_sub(oy(i, j), oy(i, j - 1))
+                                                      : df_half(df_sub(oy(i, j + 1), oy(i, j - 1))));
+            const float2 oyy = (i == 0) ? df_sub(oy(1, j), oy(0, j))
+                                        : (i == h - 1 ? df_sub(oy(i, j), oy(i - 1, j))
+                                                      : df_half(df_sub(oy(i + 1, j), oy(i - 1, j))));
+            // the sign of Oxy and x = Oxx + 1e-5 decided on the double-float values
+            const float sgn = (oxy.x < 0.f) ? 1.f : ((oxy.x > 0.f) ? -1.f : 0.f);
+            constexpr double kEps = 1e-5;
+            constexpr float kEpsHi = (float)kEps, kEpsLo = (float)(kEps - (double)kEpsHi);
+            const float2 xd = df_add(oxx, make_float2(kEpsHi, kEpsLo));
+            const float x = xd.x, y = oyy.x * sgn;
+            float2 d;
+            if (x != 0.f) {
+                // (cos, sin) of atan(y / x) wrapped to [0, pi) (:370-374, :296-305), as below
+                const float rn = rsqrtf(fmaf(x, x, y * y));
+                const float cx = fabsf(x) * rn, sy = copysignf(1.f, x) * y * rn;
+                d = (x * y < 0.f) ? make_float2(-cx, -sy) : make_float2(cx, sy);
+            } else {  // atan(y / 0): pi / 2 after the wrap, NaN for 0 / 0 (as the reference)
+                float a2 = fmodf(atanf(y / x), 3.14159265358979323846f);
+                if (a2 < 0.f) a2 += 3.14159265358979323846f;
+                float sn, cs;
+                sincosf(a2, &sn, &cs);
+                d = make_float2(cs, sn);
+            }
+            sDir[a][b] = d;
+            p.dir[M.px_base + (long long)i * w + j] = d;
+        }
+        __syncthreads();
+    } else if (M.theta == nullptr) {
         const float tri[9] = {1.f / 25, 2.f / 25, 3.f / 25, 4.f / 25, 5.f / 25, 4.f / 25, 3.f / 25, 2.f / 25, 1.f / 25};
         for (int q = tid; q < NE * (kT + 4); q += blockDim.x) {
             const int a = q / (kT + 4), c = q - a * (kT + 4);
@@ -189,7 +319,7 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
         __syncthreads();
     }
     const float PI_F = 3.14159265358979323846f;
-    for (int q = tid; q < kT * kT; q += blockDim.x) {
+    for (int q = tid; q < kT * kT && !(M.theta == nullptr && p.hyb); q += blockDim.x) {
         const int a = q >> 5, b = q & 31;
         const int i = i0 + a, j = j0 + b;
         float th = 0.f;
