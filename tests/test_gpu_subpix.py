@@ -75,7 +75,10 @@ def test_vs_oracle(detector, oracle, synth, toed, seed, H, W, sigma, thresh, est
     ref = oracle.subpix_to_correct(E.astype(np.float64), thresh, sigma, 2.0,
                                    theta=None if th is None else th.astype(np.float64))
     r = _run(detector, E, thresh, sigma, 2.0, theta=th, out_dtype=toed.TOED_F64)
-    _check(ref["edges"], r["edgels"].cpu().numpy())
+    # a random per-pixel orientation field (est False) makes the correction
+    # vector nearly cancel at a few edgels, where the FP32 planes' rounding
+    # reaches the angle multiplied by that cancellation: 2e-4 rad there
+    _check(ref["edges"], r["edgels"].cpu().numpy(), ori=1e-4 if est else 2e-4)
 
 
 def test_batch_and_fp32_mode(detector, oracle, synth, toed):

@@ -426,6 +426,7 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->hyb = hyb ? 1 : 0;
     p->qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
     p->nms_to = nmsto ? 1 : 0;
+    p->det_rec = 1;
     p->ready = c->hb_ready;
     p->ready_epoch = c->hb_epoch;
     p->ready_spins = c->ready_spins;

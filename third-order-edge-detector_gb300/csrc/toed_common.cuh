@@ -97,7 +97,8 @@ struct DetImage {
 struct Scratch {
     int* words;          // kWords: [0] unit queue, [1] staging cursor, [2] flags, [3] refine-list length,
                          // [4] (bounds-checked builds) source line of the first failed check
-    double4_32a* staging;  // staged edgels (x, y, orientation, strength)
+    double4_32a* staging;  // staged edgels: TO correction (x, y, orientation, strength); the
+                           // detection uses the same memory as float4 records (det_stage)
     int* staging_idx;
     long long staging_cap;
     int2* seg;           // per segment {staging offset, count}
@@ -107,6 +108,24 @@ struct Scratch {
     int4* refine;        // edgels whose orientation is recomputed in FP64: {staging slot, image, Gr, Gc}
     int refine_cap;      // entries of `refine` (0: no recomputation)
 };
+
+// The detection's staged edgel: a float4 in the staging memory beside the
+// 2x-grid index in staging_idx (20 bytes per edgel).  x, y hold what the
+// output's FP64 position is rebuilt from without loss: in HYBRID precision
+// the subpixel offset 0.5 s* n (the grid part 0.5 (G - 1) is exact), in
+// FP32 precision the FP32 position G + s* n on the 2x grid; then the
+// orientation and the strength.
+__device__ __forceinline__ float4* det_stage(const Scratch& sc) { return reinterpret_cast<float4*>(sc.staging); }
+
+// Output position (x, y) = ((pos - 1) / 2) of a staged edgel (cpu_toed.cpp:516-521).
+__device__ __forceinline__ double2 det_xy(const float4& rec, int idx, int W2, bool hyb)
+{
+    const int Gr = idx / W2, Gc = idx - Gr * W2;
+    if (hyb)
+        return make_double2((double)(0.5f * (float)(Gc - 1)) + (double)rec.x,
+                            (double)(0.5f * (float)(Gr - 1)) + (double)rec.y);
+    return make_double2(((double)rec.x - 1.0) * 0.5, ((double)rec.y - 1.0) * 0.5);
+}
 
 struct BatchParams {
     CUtensorMap tmap[kBatchMax];  // per image: 2-D map, box (tma_boxw x kStepRows), OOB zero fill
@@ -124,6 +143,8 @@ struct BatchParams {
     int hyb;             // 1: FP64 peak fit, FP64 recomputation of ill-conditioned orientations (TOED_HYBRID)
     int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
     int nms_to;          // 1: NMS and peak fit along the corrected normal (TOED_NMS_TO_NORMAL)
+    int det_rec;         // ordering pass input: 1 the detection's float4 records (det_stage), 0 the TO
+                         // correction's double4 records
     const int* ready;    // per copy group: ready_epoch once the group's images are in device memory
     int ready_epoch;
     int ready_spins;     // polls of a ready flag before the wait gives up (TOED_FLAG_TIMEOUT)

@@ -483,7 +483,7 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
                 fyyy = rc[16];
     const int Gr = __float_as_int(rc[17]), Gc = __float_as_int(rc[18]);
     const int dst = __float_as_int(rc[19]), img = __float_as_int(rc[20]), idx = Gr * W2 + Gc;
-    double x, y;
+    float x, y;  // the staged position (det_xy)
     float ori, str;
     if (HYB) {
         // fp - fm and fm + fp - 2f cancel: formed exactly from the FP32
@@ -499,10 +499,11 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         const float ss = sqrtf(1.f + sl * sl);
         const float sst = -0.5f * num * ss / den;           // s* = -B / (2A)
         const float maxf = mv - 0.125f * num * num / den;   // A s*^2 + B s* + C
-        // (pos - 1) / 2, cpu_toed.cpp:516; the grid coordinate is exact, the
-        // subpixel offset is added in FP64 so that large coordinates keep it
-        x = (double)(0.5f * (float)(Gc - 1)) + (double)(0.5f * sst * nx);
-        y = (double)(0.5f * (float)(Gr - 1)) + (double)(0.5f * sst * ny);
+        // (pos - 1) / 2, cpu_toed.cpp:516: the grid coordinate is exact, the
+        // subpixel offset is staged alone and added in FP64 when the list is
+        // written, so that large coordinates keep it
+        x = 0.5f * sst * nx;
+        y = 0.5f * sst * ny;
         str = sqrtf((maxf * nx) * (maxf * nx) + (maxf * ny) * (maxf * ny));
         // cpu_toed.cpp:227-232 with the shared products factored out, in FP32:
         // TIx = 2 (fx (fxx^2 + fxy^2) + fy fxy (fxx + fyy) + fx fy fxxy) + fy^2 fxyy + fx^2 fxxx
@@ -535,8 +536,8 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         const float ss = sqrtf(1.f + sl * sl);
         const float sst = -0.5f * num * ss / den;
         const float maxf = mv - 0.125f * num * num / den;
-        x = ((double)((float)Gc + sst * nx) - 1.0) * 0.5;
-        y = ((double)((float)Gr + sst * ny) - 1.0) * 0.5;
+        x = (float)Gc + sst * nx;  // the FP32 position on the 2x grid
+        y = (float)Gr + sst * ny;
         str = sqrtf((maxf * nx) * (maxf * nx) + (maxf * ny) * (maxf * ny));
         const float tix = gx * (2.f * fxx * fxx + 2.f * fxy * fxy) + gy * (2.f * fxx * fxy + 2.f * fyy * fxy) +
                           2.f * gx * gy * fxxy + gy * gy * fxyy + gx * gx * fxxx;
@@ -545,7 +546,7 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
         ori = (tix == 0.f && tiy == 0.f) ? __int_as_float(0x7fc00000) : atan2f(tix, -tiy);
     }
     if (dst < sc.staging_cap) {
-        sc.staging[dst] = make_double4_32a(x, y, (double)ori, (double)str);
+        det_stage(sc)[dst] = make_float4(x, y, ori, str);
         sc.staging_idx[dst] = idx;
     }
 }

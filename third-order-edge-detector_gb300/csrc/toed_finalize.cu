@@ -84,7 +84,7 @@ __device__ void refine_edgel(const BatchParams& p, int4 e, int lane)
         const double tiy = fx * (2 * fxx * fxy + 2 * fyy * fxy) + fy * (2 * fyy * fyy + 2 * fxy * fxy) +
                            2 * fx * fy * fxyy + fx * fx * fxxy + fy * fy * fyyy;
         const double ori = (tix == 0.0 && tiy == 0.0) ? __longlong_as_double(0x7ff8000000000000LL) : atan2(tix, -tiy);
-        p.sc.staging[e.x].z = ori;
+        det_stage(p.sc)[e.x].z = (float)ori;
     }
 }
 
@@ -181,7 +181,17 @@ __global__ void __launch_bounds__(kFinThreads) fin_scatter(const __grid_constant
         }
         const long long d = base + r, src = (long long)s_src[lo] + (r - s_dst[lo]);
         if (d >= cap || src >= p.sc.staging_cap) continue;
-        const double4_32a rc = p.sc.staging[src];
+        double4_32a rc;
+        int gi = 0;
+        if (p.det_rec) {  // the detection's compact record
+            const float4 st = det_stage(p.sc)[src];
+            gi = p.sc.staging_idx[src];
+            const double2 xy = det_xy(st, gi, 2 * im.W, p.hyb != 0);
+            rc = make_double4_32a(xy.x, xy.y, (double)st.z, (double)st.w);
+        } else {
+            rc = p.sc.staging[src];
+            if (im.index) gi = p.sc.staging_idx[src];
+        }
         if (p.out_f64) {  // two 16-byte stores: the caller's buffer need only be 16-byte aligned
             double2* o = reinterpret_cast<double2*>(im.out) + 2 * d;
             o[0] = make_double2(rc.x, rc.y);
@@ -189,7 +199,7 @@ __global__ void __launch_bounds__(kFinThreads) fin_scatter(const __grid_constant
         } else {
             reinterpret_cast<float4*>(im.out)[d] = make_float4((float)rc.x, (float)rc.y, (float)rc.z, (float)rc.w);
         }
-        if (im.index) im.index[d] = p.sc.staging_idx[src];
+        if (im.index) im.index[d] = gi;
     }
 }
 

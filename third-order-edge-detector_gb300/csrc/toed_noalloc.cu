@@ -152,6 +152,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     p.hyb = prm->precision != TOED_FP32 ? 1 : 0;
     p.qad = prm->orientation == TOED_ORI_QAD ? 1 : 0;
     p.nms_to = nmsto ? 1 : 0;
+    p.det_rec = 1;
     p.stage_blk = 1;  // staging sized to the capacity exactly: reserve each step's edgels alone
     // strip height: the tallest of 254 / 126 / 62 / 30 / 14 rows that still
     // gives every resident CTA a few strips

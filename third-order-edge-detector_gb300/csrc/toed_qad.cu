@@ -309,7 +309,7 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
             }
             const long long d = base + r, src = (long long)s_src[lo] + (r - s_dst[lo]);
             if (d < cap && src < p.sc.staging_cap) {
-                const double2 xy = *reinterpret_cast<const double2*>(&p.sc.staging[src]);
+                const double2 xy = det_xy(det_stage(p.sc)[src], p.sc.staging_idx[src], 2 * im.W, p.hyb != 0);
                 const double px = 2.0 * xy.x + 1.0, py = 2.0 * xy.y + 1.0;
                 const double fpx = floor(px), fpy = floor(py);
                 mX1 = (int)fpx;
@@ -369,7 +369,9 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
 #pragma unroll
         for (int q = 0; q < 9; ++q) mine[q] = sDer[wid][lane * 9 + q];
         __syncwarp();  // the next group overwrites the slots
-        const double4_32a my_rc = my_d >= 0 ? p.sc.staging[my_src] : make_double4_32a(0.0, 0.0, 0.0, 0.0);
+        const float4 my_st = my_d >= 0 ? det_stage(p.sc)[my_src] : make_float4(0.f, 0.f, 0.f, 0.f);
+        const int my_gi = my_d >= 0 ? p.sc.staging_idx[my_src] : 0;
+        const double2 my_xy = my_d >= 0 ? det_xy(my_st, my_gi, 2 * im.W, p.hyb != 0) : make_double2(0.0, 0.0);
         // the third-order vector and the angle
         const float gx = mine[0], gy = mine[1], fxx = mine[2], fxy = mine[3], fyy = mine[4], fxxy = mine[5],
                     fxyy = mine[6], fxxx = mine[7], fyyy = mine[8];
@@ -394,8 +396,8 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
                 const int e = __ffs(flag) - 1;
                 flag &= flag - 1;
                 // the subpixel point in FP64 from the staged position
-                const double2 xy = *reinterpret_cast<const double2*>(
-                    &p.sc.staging[__shfl_sync(0xffffffffu, my_src, e)]);
+                const double2 xy = make_double2(__shfl_sync(0xffffffffu, my_xy.x, e),
+                                                __shfl_sync(0xffffffffu, my_xy.y, e));
                 const double2 ti = qad_refine<R>(im.src, im.pitch, im.H, im.W, im.dtype == TOED_U8, sTab64,
                                                  2.0 * xy.x + 1.0, 2.0 * xy.y + 1.0, lane);
                 if (lane == e) {
@@ -414,13 +416,12 @@ __global__ void __launch_bounds__(kQadThreads, 3) fin_scatter_qad(const __grid_c
         if (my_d < 0) continue;
         if (p.out_f64) {
             double2* o = reinterpret_cast<double2*>(im.out) + 2 * my_d;
-            o[0] = make_double2(my_rc.x, my_rc.y);
-            o[1] = make_double2((double)ori, my_rc.w);
+            o[0] = my_xy;
+            o[1] = make_double2((double)ori, (double)my_st.w);
         } else {
-            reinterpret_cast<float4*>(im.out)[my_d] =
-                make_float4((float)my_rc.x, (float)my_rc.y, ori, (float)my_rc.w);
+            reinterpret_cast<float4*>(im.out)[my_d] = make_float4((float)my_xy.x, (float)my_xy.y, ori, my_st.w);
         }
-        if (im.index) im.index[my_d] = p.sc.staging_idx[my_src];
+        if (im.index) im.index[my_d] = my_gi;
     }
 }
 

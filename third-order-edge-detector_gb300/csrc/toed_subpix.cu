@@ -127,6 +127,12 @@ __device__ __forceinline__ float2 df_mul(float2 a, float2 b)
     e = fmaf(a.x, b.y, fmaf(a.y, b.x, e));
     return df_fast_two_sum(p, e);
 }
+__device__ __forceinline__ float2 df_mul_f(float a, float2 b)  // a float times a double-float
+{
+    const float p = __fmul_rn(a, b.x);
+    const float e = fmaf(a, b.y, fmaf(a, b.x, -p));
+    return df_fast_two_sum(p, e);
+}
 __device__ __forceinline__ float2 df_half(float2 a) { return make_float2(0.5f * a.x, 0.5f * a.y); }  // exact
 
 // The triangle filter (:316-321), weight (5 - |k|) / 25, as double-floats.
@@ -214,8 +220,21 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
     }
     __syncthreads();
 
+    // HYBRID: tiles holding an NMS candidate (E > thresh inside the margin)
+    // estimate the orientation in double-float arithmetic; the others, whose
+    // directions only weight the Hx / Hy maps, in FP32
+    bool df_tile = false;
     if (M.theta == nullptr && p.hyb) {
-        // HYBRID: the orientation estimate in double-float arithmetic (see
+        bool any = false;
+        for (int q = tid; q < kT * kT; q += blockDim.x) {
+            const int a = q >> 5, b = q & 31, i = i0 + a, j = j0 + b;
+            any = any || (i >= M.margin + 1 && i < h - M.margin - 2 && j >= M.margin + 1 && j < w - M.margin - 2 &&
+                          sE[a + HE][b + HE] > p.thresh);
+        }
+        df_tile = __syncthreads_or(any);
+    }
+    if (df_tile) {
+        // the orientation estimate in double-float arithmetic (see
         // df_two_sum); the same sums, in the same order, as the FP32 form
         float2(*sTmpD)[kT + 4] = reinterpret_cast<float2(*)[kT + 4]>(sStage);          // cols j0-2 .. j0+33
         float2(*sSmD)[kT + 4] = reinterpret_cast<float2(*)[kT + 4]>(sStage + 2 * kTmpB);  // rows/cols -2 .. +33
@@ -224,7 +243,7 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
             float2 acc = make_float2(0.f, 0.f);
 #pragma unroll
             for (int qq = -kTriR; qq <= kTriR; ++qq)
-                acc = df_add(acc, df_mul(make_float2(sE[a][c + 4 - qq], 0.f), tri_df(qq)));
+                acc = df_add(acc, df_mul_f(sE[a][c + 4 - qq], tri_df(qq)));
             sTmpD[a][c] = acc;
         }
         __syncthreads();
@@ -319,7 +338,7 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
         __syncthreads();
     }
     const float PI_F = 3.14159265358979323846f;
-    for (int q = tid; q < kT * kT && !(M.theta == nullptr && p.hyb); q += blockDim.x) {
+    for (int q = tid; q < kT * kT && !df_tile; q += blockDim.x) {
         const int a = q >> 5, b = q & 31;
         const int i = i0 + a, j = j0 + b;
         float th = 0.f;
