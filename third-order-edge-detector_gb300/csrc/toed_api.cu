@@ -194,6 +194,7 @@ struct toed_ctx {
     int* hb_epoch_src = nullptr;
     int hb_epoch = 0;
     int ready_spins = kReadySpinLimit;  // bound of each ready-flag wait (polls)
+    std::vector<cudaEvent_t> hb_ev;     // toed_detect_host_batch's ordering events, reused
     std::mutex mu;
 };
 
@@ -279,6 +280,7 @@ toed_status toed_destroy(toed_ctx* c)
     if (c->hb_cnt_host) cudaFreeHost(c->hb_cnt_host);
     if (c->hb_epoch_src) cudaFreeHost(c->hb_epoch_src);
     cudaFree(c->hb_ready);
+    for (auto e : c->hb_ev) cudaEventDestroy(e);
     if (c->s_in) cudaStreamDestroy(c->s_in);
     if (c->s_out) cudaStreamDestroy(c->s_out);
     cudaSetDevice(prev);
@@ -448,14 +450,15 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
         d.unit_base = (int)units;
         d.tile_base = (int)tiles;
         d.seg_base = tiles * kSegTile;
-        encode_rows_map(&p->tmap[i], d, r);
         d.wait_slot = wait_slot ? wait_slot[i] : 0;
+        d.tma_align = 1;
+        d.tma_boxw = 0;
         if (async_rows)
             d.tma = (d.dtype == TOED_F32) ? 2 : 0;  // async row copies (float32) or plain loads, never TMA
-        else if (use && !use->staging)
-            d.tma = 0;
-        else if (nmsto && plain_loads)
-            d.tma = 0;  // host memory read in place: plain loads
+        else if ((use && !use->staging) || plain_loads)
+            d.tma = 0;  // plain loads (host memory read in place: never TMA)
+        else
+            encode_rows_map(&p->tmap[i], d, r);  // TMA where the image allows it (a host call per image)
         const long long nseg = 2LL * im.height * d.nsc;
         d.nseg = nseg;
         units += (long long)d.nsc * d.nsr;
@@ -708,10 +711,6 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         // an early return must not leave copies in flight: the next call
         // reuses the staging and rewrites the epoch their flag copies read
         if (s != TOED_OK && c->s_in) cudaStreamSynchronize(c->s_in);
-        for (auto e : ev_in)
-            if (e) cudaEventDestroy(e);
-        for (auto e : ev_det)
-            if (e) cudaEventDestroy(e);
         if (prev != c->device) cudaSetDevice(prev);
         return s;
     };
@@ -818,9 +817,16 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         chunks = k + 1;
         first[chunks] = n;
     }
+    // the ordering events live in the context (the call is synchronous: none
+    // is pending when the next call reuses it)
+    while ((int)c->hb_ev.size() < 2 * chunks) {
+        cudaEvent_t e = nullptr;
+        TOED_HB(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        c->hb_ev.push_back(e);
+    }
     for (int k = 0; k < chunks; ++k) {
-        TOED_HB(cudaEventCreateWithFlags(&ev_in[k], cudaEventDisableTiming));
-        TOED_HB(cudaEventCreateWithFlags(&ev_det[k], cudaEventDisableTiming));
+        ev_in[k] = c->hb_ev[2 * k];
+        ev_det[k] = c->hb_ev[2 * k + 1];
     }
     auto copy_group = [&](int k) -> cudaError_t {  // group k's images to the device on s_in
         for (int i = first[k]; i < first[k + 1]; ++i) {
