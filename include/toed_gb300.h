@@ -301,13 +301,9 @@ toed_status toed_set_tuning(toed_ctx* ctx, const toed_params* params, const toed
  * toed_profile_begin: from now on every detection on `ctx` records a pair of
  * CUDA events just before and just after its fused detection kernel, on the
  * call's stream.  toed_profile_end: waits for the last pair, returns the sum
- * of the kernel times (ms) and the number of kernel launches, and stops.
- * toed_peak_probe: times a register-resident FMA loop on all SMs and returns
- * the sustained FP32 (kind 0) or FP64 (kind 1) rate in TFLOP/s -- the
- * denominator of the FP32 roofline, measured at the clocks of the run. */
+ * of the kernel times (ms) and the number of kernel launches, and stops. */
 toed_status toed_profile_begin(toed_ctx* ctx);
 toed_status toed_profile_end(toed_ctx* ctx, double* kernel_ms, int* launches);
-toed_status toed_peak_probe(int kind, int iters, cudaStream_t stream, double* tflops);
 
 /* Compatibility: the reference's dense two-kernel form.
  * toed_convolve_planes writes Ix, Iy, |grad I| and the TO orientation on the

@@ -42,7 +42,7 @@ MAX_RADIUS = 12
 C_SYMBOLS = [
     "toed_params_default", "toed_status_string", "toed_last_cuda_error", "toed_create",
     "toed_destroy", "toed_reserve", "toed_detect", "toed_detect_batch", "toed_device_flags",
-    "toed_convolve_planes", "toed_convolve_planes_direct", "toed_nms_planes", "toed_profile_begin", "toed_profile_end", "toed_peak_probe",
+    "toed_convolve_planes", "toed_convolve_planes_direct", "toed_nms_planes", "toed_profile_begin", "toed_profile_end",
     "toed_subpix_to_correct_batch", "toed_detect_noalloc", "toed_backward_batch", "toed_autotune",
     "toed_set_tuning", "toed_detect_host_batch", "toed_edgels_to_columns", "toed_write_edgels_txt",
 ]
@@ -151,7 +151,6 @@ def lib():
         L.toed_nms_planes.argtypes = [ip, ip, ip, vp, vp, vp, ctypes.c_float, ip, vp, vp, vp]
         L.toed_profile_begin.argtypes = [vp]
         L.toed_profile_end.argtypes = [vp, ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ip)]
-        L.toed_peak_probe.argtypes = [ip, ip, vp, ctypes.POINTER(ctypes.c_double)]
         L.toed_subpix_to_correct_batch.argtypes = [vp, ctypes.POINTER(toed_edgemap), ip,
                                                    ctypes.POINTER(toed_subpix_params), vp]
         L.toed_detect_noalloc.argtypes = [ctypes.POINTER(toed_image), ctypes.POINTER(toed_params), vp]
@@ -189,12 +188,25 @@ def _check(st: int, what: str):
         raise ToedError(st, msg)
 
 
+_PROBE = None
+
+
 def peak_probe(kind: int = 0, iters: int = 200000, stream=None) -> float:
-    """Measured FP32 (kind 0) or FP64 (kind 1) FMA rate in TFLOP/s."""
+    """Measured FP32 (kind 0) or FP64 (kind 1) FMA rate in TFLOP/s, from the
+    measurement library libtoed_probe.so (built by build(); not part of the
+    detector's C ABI)."""
+    global _PROBE
     t = _torch()
+    if _PROBE is None:
+        path = os.path.join(HERE, "libtoed_probe.so")
+        if not os.path.exists(path):
+            raise RuntimeError(f"probe library not built: {path} (call build())")
+        _PROBE = ctypes.CDLL(path)
+        _PROBE.toed_peak_probe.argtypes = [ctypes.c_int, ctypes.c_int, ctypes.c_void_p, ctypes.POINTER(ctypes.c_double)]
+        _PROBE.toed_peak_probe.restype = ctypes.c_int
     s = stream if stream is not None else t.cuda.current_stream()
     out = ctypes.c_double(0.0)
-    _check(lib().toed_peak_probe(int(kind), int(iters), ctypes.c_void_p(s.cuda_stream), ctypes.byref(out)),
+    _check(_PROBE.toed_peak_probe(int(kind), int(iters), ctypes.c_void_p(s.cuda_stream), ctypes.byref(out)),
            "toed_peak_probe")
     return out.value
 

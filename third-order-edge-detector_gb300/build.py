@@ -92,7 +92,28 @@ def build(verbose: bool = False, jobs: int | None = None, debug: bool = False) -
     if debug:
         return lib
     build_driver(verbose)
+    build_probe(verbose)
     return LIB
+
+
+PROBE_SRC = os.path.join(HERE, "probe", "toed_probe.cu")
+PROBE_LIB = os.path.join(HERE, "libtoed_probe.so")
+
+
+def build_probe(verbose: bool = False) -> str:
+    """bench.py's FP32 / FP64 FMA-rate probe, a library of its own (not part
+    of the detector's C ABI)."""
+    if os.path.exists(PROBE_LIB) and os.path.getmtime(PROBE_LIB) >= os.path.getmtime(PROBE_SRC):
+        return PROBE_LIB
+    tmp = PROBE_LIB + ".tmp"
+    cmd = [nvcc()] + _flags() + ["-shared", PROBE_SRC, "-o", tmp, "-lcudart_static", "-lrt", "-lpthread", "-ldl"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("probe build failed:\n" + r.stderr)
+    os.replace(tmp, PROBE_LIB)
+    if verbose:
+        print("built", PROBE_LIB)
+    return PROBE_LIB
 
 
 DRIVER_SRC = os.path.join(HERE, "driver", "toed_batch.cpp")

@@ -1,4 +1,6 @@
-// toed_probe.cu -- FP32 / FP64 issue-rate probe (toed_peak_probe).
+// toed_probe.cu -- FP32 / FP64 issue-rate probe (toed_peak_probe), a
+// measurement tool of bench.py built into its own small library
+// (libtoed_probe.so), not part of the detector's C ABI.
 //
 // The detection path is bound by FP32 FMA issue, not by HBM or tensor
 // cores, so its roofline denominator is the FP32 FMA rate at the clocks of
@@ -7,6 +9,10 @@
 #include <cuda_runtime.h>
 
 #include "../../include/toed_gb300.h"
+
+// kind 0: FP32, 1: FP64; *tflops gets the sustained FMA rate of `iters`
+// iterations on all SMs (CUDA events on `stream`).
+extern "C" toed_status toed_peak_probe(int kind, int iters, cudaStream_t stream, double* tflops);
 
 namespace {
 template <typename T>
