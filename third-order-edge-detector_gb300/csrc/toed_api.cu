@@ -195,6 +195,10 @@ struct toed_ctx {
     int hb_epoch = 0;
     int ready_spins = kReadySpinLimit;  // bound of each ready-flag wait (polls)
     std::vector<cudaEvent_t> hb_ev;     // toed_detect_host_batch's ordering events, reused
+    float tap_sigma = -1.f;             // taps of the last detection's (sigma, radius)
+    int tap_r = 0;
+    TapBlock taps;
+    TapBlock64 taps64;
     std::mutex mu;
 };
 
@@ -417,9 +421,17 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
 
     BatchParams* p = new BatchParams();
     std::unique_ptr<BatchParams> guard(p);
-    make_taps((double)prm->sigma, r, &p->taps);
-    make_taps64((double)prm->sigma, r, &p->taps64);
+    // the taps of the last (sigma, radius), kept in the context (a few hundred exp per call otherwise)
+    if (c->tap_sigma != prm->sigma || c->tap_r != r) {
+        make_taps((double)prm->sigma, r, &c->taps);
+        make_taps64((double)prm->sigma, r, &c->taps64);
+        c->tap_sigma = prm->sigma;
+        c->tap_r = r;
+    }
+    p->taps = c->taps;
+    p->taps64 = c->taps64;
     p->thr = prm->threshold;
+    p->thr2 = prm->threshold < 0.f ? -1.f : prm->threshold * prm->threshold * 0.9999f;
     p->border = prm->border;
     p->S = use ? use->strip_rows : plan_strip_rows(images, n, resident);
     p->n_img = n;

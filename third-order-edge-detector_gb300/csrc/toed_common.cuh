@@ -132,6 +132,7 @@ struct BatchParams {
     TapBlock taps;
     TapBlock64 taps64;
     float thr;
+    float thr2;          // candidate prefilter on |grad I|^2: a little below thr^2 (-1 when thr < 0)
     int border;
     int S;               // strip inner rows (multiple of kStepRows minus 2)
     int n_img;

@@ -787,7 +787,10 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                     const float2 f = make_float2(fx[o], fy[o]);
                     if (TOED_IN_BOUNDS(m < C::MS && c < C::FW, p.sc.words)) sFxy[m * C::FW + c] = f;
                     const int Gr = gr_base + m;
-                    const bool kp = colok && Gr >= row_lo && Gr < row_hi && grad_mag(f) > p.thr;  // cpu_toed.cpp:403
+                    // cpu_toed.cpp:403 as a prefilter on the squared magnitude (thr2 a
+                    // little below thr^2, so the list holds every point nms_eval's exact
+                    // test `|grad I| > thr` keeps; no square root per point)
+                    const bool kp = colok && Gr >= row_lo && Gr < row_hi && fmaf(f.x, f.x, f.y * f.y) > p.thr2;
                     const unsigned bal = __ballot_sync(0xffffffffu, kp);
                     if (lane == 0) sMask[(m * 2 + b) * kHalves + h] = bal;
                 }

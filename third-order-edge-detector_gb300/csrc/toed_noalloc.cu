@@ -145,6 +145,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     make_taps((double)prm->sigma, r, &p.taps);
     make_taps64((double)prm->sigma, r, &p.taps64);
     p.thr = prm->threshold;
+    p.thr2 = prm->threshold < 0.f ? -1.f : prm->threshold * prm->threshold * 0.9999f;
     p.border = prm->border;
     p.n_img = 1;
     p.out_f64 = prm->out_dtype == TOED_F64;
