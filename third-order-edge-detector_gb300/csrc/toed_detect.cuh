@@ -7,9 +7,10 @@
 //
 //   1. B new input rows (+ halo) arrive by TMA (or plain loads) and are
 //      converted to FP32 into a ring of input rows;
-//   2. row pass: the six horizontal responses the dense first derivatives
-//      need -- G and Gx, each truncated to 2r+1 taps (T), full 2r+3 taps (F)
-//      and half-pixel shifted (S) -- into a ring of row-pass rows;
+//   2. row pass: twelve horizontal responses -- G, Gx, Gxx and Gxxx, each
+//      truncated to 2r+1 taps (T), full 2r+3 taps (F) and half-pixel shifted
+//      (S) -- into a ring of row-pass rows (G, Gx feed the dense first
+//      derivatives, Gxx, Gxxx the per-edgel ones);
 //   3. column pass: Ix and Iy at the four half-pixel sub-grids (the 2x grid
 //      of the reference, cpu_toed.cpp:204-355) for the B new rows, |grad I|,
 //      and the threshold test as one ballot mask per (2x row, column parity);
@@ -17,17 +18,17 @@
 //      NMS along the gradient with the reference's 8-sector interpolation,
 //      max test and parabola fit (cpu_toed.cpp:399-495), decided in FP32;
 //      survivors compacted in order;
-//   5. per edgel only: the seven higher derivatives -- Gxx / Gxxx row
-//      responses recomputed from the input ring for the edgel's window rows,
-//      a thread per (edgel, row) -- then the third-order orientation
+//   5. per edgel only: the seven higher derivatives, contracted from the
+//      row-pass ring with the y taps of the edgel's sub-grid, then the
+//      third-order orientation
 //      (cpu_toed.cpp:227-232) and the peak fit with FP64 where they cancel
 //      (HYBRID) or in FP32; records are deferred in a ring and finished by
 //      all threads at once; the staged record goes to a staging area and the
 //      row's {offset, count} to the row-segment table that the ordering pass
 //      (toed_finalize.cu) turns into the reference's row-major edgel list.
 //
-// Both rings have a power-of-two number of rows and are indexed by absolute
-// row, so sliding the window moves no data.
+// Both rings hold a multiple of 8 rows (the live window rounded up) and are
+// indexed by absolute row, so sliding the window moves no data.
 //
 // Compared with the reference kernel (direct 17x17 and 19x19 sums of nine
 // derivatives at every point, gpu_convolve.cu:114-131) this evaluates the
@@ -46,7 +47,10 @@ struct Cfg {
     static constexpr int NT = 2 * R + 3;            // taps of a full / shifted filter
     static constexpr int NIN = kExt + 2 * R + 2;    // input columns held per row
     static constexpr int HS = B + 2 * R + 3;        // live rows of the row-pass window
-    static constexpr int RING = HS;                 // ring rows (input and row-pass rings)
+    // ring rows (input and row-pass rings): HS rounded up to a multiple of 8,
+    // so that ring row of slot 0 (advancing by B) stays a multiple of 8 and
+    // the column pass knows where its window can wrap (col_pass)
+    static constexpr int RING = (HS + 7) / 8 * 8;
     static constexpr int MS = 2 * B + 2;            // 2x-grid rows held for NMS
     static constexpr int NMS_ROWS = 2 * B;          // 2x-grid rows decided per step
     static constexpr int MAXC = NMS_ROWS * 2 * kInner;
@@ -332,12 +336,24 @@ __device__ __forceinline__ void col_pass(const float2* __restrict__ P, int rb, i
 {
     using C = Cfg<R>;
     constexpr int YF = (V == 2) ? 4 : 0;
+    constexpr int NW = kColRows + 2 * R + 2;  // window rows
+    // Window row t is ring row (r0 + t) mod RING.  RING, rb and 8g are
+    // multiples of 8, so r0 = 1 (mod 8) and the wrap, if any, falls at
+    // t = 7 (mod 8): every block of window rows t in [8b - 1, 8b + 7) reads
+    // from one base pointer, chosen once, plus a constant offset.
+    static_assert(C::RING % 8 == 0 && kStepRows % 8 == 0 && kColRows == 8, "column-pass wrap blocks");
+    constexpr int NBLK = (NW + 8) / 8;
 #pragma unroll
     for (int o = 0; o < kColRows; ++o) { fx[o] = 0.f; fy[o] = 0.f; }
-    const int r0 = rb + g * kColRows + 1;
+    const int r0 = ring_wrap<C::RING>(rb + g * kColRows + 1);
+    const int tw = C::RING - r0;  // first window row past the ring's end
+    const float2* base[NBLK];
 #pragma unroll
-    for (int t = 0; t < kColRows + 2 * R + 2; ++t) {
-        const float2 h = P[ring_wrap<C::RING>(r0 + t) * kExt + col];
+    for (int b = 0; b < NBLK; ++b)
+        base[b] = P + (r0 - ((8 * b - 1 >= tw) ? C::RING : 0)) * kExt + col;
+#pragma unroll
+    for (int t = 0; t < NW; ++t) {
+        const float2 h = base[(t + 1) / 8][t * kExt];
 #pragma unroll
         for (int o = 0; o < kColRows; ++o) {
             const int p = o + R + 1 - t;
@@ -357,7 +373,7 @@ __device__ __forceinline__ float grad_mag(float2 g) { return sqrt_approx(fmaf(g.
 // NMS evaluation at 2x-grid slot (m, c) of the step window.  Shared by the
 // decision stage and the per-edgel epilogue so both see identical numbers.
 struct NmsEval {
-    float mv, gx, gy, nx, ny, slope, Map, Mdp, Mam, Mdm, sstar;
+    float mv, gx, gy, nx, ny, slope, Map, Mdp, Mam, Mdm;
     bool cand;
 };
 
@@ -365,6 +381,8 @@ struct NmsEval {
 // sector, neighbours, fit and offset are taken along the unit vector of
 // (tx, ty) -- the third-order vector -- instead of along (Ix, Iy); the
 // candidate tests (threshold, gradient epsilon) stay those of the reference.
+// The decision stage reads only `cand`; the unit normal (nx, ny) is formed
+// for the per-edgel record and drops out of the decision code.
 template <bool TOD = false>
 __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int m, int c, float thr,
                                             float tx = 0.f, float ty = 0.f, int* dbg = nullptr)
@@ -392,10 +410,13 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     }
     // Eight sectors of cpu_toed.cpp:415-462 in closed form: x-major when
     // |Ix| >= |Iy|; the axis neighbour steps along the major axis towards
-    // the gradient, the diagonal one along both; fm mirrors fp.
-    const bool xmaj = fabsf(dx) >= fabsf(dy);
+    // the gradient, the diagonal one along both; fm mirrors fp.  The slope
+    // (minor over major component of the unit normal) is the ratio of the
+    // direction's own components, the normalisation cancelling.
+    const float ax = fabsf(dx), ay = fabsf(dy);
+    const bool xmaj = ax >= ay;
     const int sx = (dx >= 0.f) ? 1 : -1, sy = (dy >= 0.f) ? 1 : -1;
-    r.slope = xmaj ? __fdividef(fabsf(r.ny), fabsf(r.nx)) : __fdividef(fabsf(r.nx), fabsf(r.ny));
+    r.slope = __fdividef(fminf(ax, ay), fmaxf(ax, ay));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
 #ifdef TOED_DEBUG_BOUNDS
     if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return r;
@@ -408,10 +429,13 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     const float fm = r.Mam * (1.f - r.slope) + r.Mdm * r.slope;
     const float mv = r.mv;
     const bool maxt = (mv > fm && mv >= fp) || (mv >= fm && mv > fp);  // :466-468
-    // s* = -B/(2A) with A = (fm+fp-2f)/(2s^2), B = (fp-fm)/(2s) (:471-476)
-    const float s = sqrtf(1.f + r.slope * r.slope);
-    r.sstar = __fdividef(-(fp - fm) * s, 2.f * (fm + fp - 2.f * mv));
-    r.cand = maxt && (fabsf(r.sstar) <= 1.41421356f);  // :478
+    // s* = -B/(2A) with A = (fm+fp-2f)/(2s^2), B = (fp-fm)/(2s), s = sqrt(1 +
+    // slope^2) (:471-476), kept when |s*| <= sqrt(2) (:478), tested as
+    // |fp - fm| s <= 2 sqrt(2) |fm + fp - 2f| without the division.  The max
+    // test gives fm + fp <= 2f, so the denominator is negative unless it is
+    // zero, where s* is inf or 0/0 and the point is rejected as before.
+    const float num = fp - fm, den = fm + fp - 2.f * mv;
+    r.cand = maxt && den < 0.f && fabsf(num) * sqrt_approx(fmaf(r.slope, r.slope, 1.f)) <= -2.82842712f * den;
     return r;
 }
 
@@ -440,11 +464,15 @@ __device__ __forceinline__ void gather_hi(const float2* __restrict__ sP, const f
         return;
     }
 #endif
+    // window row kk is ring row hw + kk, less RING from kk = tw on
+    const int hw = ring_wrap<C::RING>(h0), tw = C::RING - hw;
+    const float2* Pb = Pp + hw * kExt;
+    const float2* Qb = Qp + hw * kExt;
 #pragma unroll
     for (int kk = 0; kk < NT; ++kk) {
-        const int ph = ring_wrap<C::RING>(h0 + kk) * kExt;
-        const float2 hp = Pp[ph];
-        const float2 hq = Qp[ph];
+        const int ph = kk * kExt - ((kk >= tw) ? C::RING * kExt : 0);
+        const float2 hp = Pb[ph];
+        const float2 hq = Qb[ph];
         const float4 t = tab[NT - 1 - kk];
         fxy = fmaf(hp.y, t.y, fxy);
         fyy = fmaf(hp.x, t.z, fyy);
@@ -780,18 +808,20 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 else
                     col_pass<R, 2>(P, rb, g, col, tp, fx, fy);
                 const int c = 2 * col + b, Gc = gc_base + c;
-                const bool colok = col >= 1 && col <= kInner && Gc >= col_lo && Gc < col_hi;
+                // the strip's output columns inside the image's border (lanes)
+                const unsigned colmask =
+                    __ballot_sync(0xffffffffu, col >= 1 && col <= kInner && Gc >= col_lo && Gc < col_hi);
 #pragma unroll
                 for (int o = 0; o < kColRows; ++o) {
                     const int m = 2 * (g * kColRows + o) + a + 2;
                     const float2 f = make_float2(fx[o], fy[o]);
                     if (TOED_IN_BOUNDS(m < C::MS && c < C::FW, p.sc.words)) sFxy[m * C::FW + c] = f;
-                    const int Gr = gr_base + m;
+                    const int Gr = gr_base + m;  // the same for the whole warp
                     // cpu_toed.cpp:403 as a prefilter on the squared magnitude (thr2 a
                     // little below thr^2, so the list holds every point nms_eval's exact
                     // test `|grad I| > thr` keeps; no square root per point)
-                    const bool kp = colok && Gr >= row_lo && Gr < row_hi && fmaf(f.x, f.x, f.y * f.y) > p.thr2;
-                    const unsigned bal = __ballot_sync(0xffffffffu, kp);
+                    const unsigned bal = __ballot_sync(0xffffffffu, fmaf(f.x, f.x, f.y * f.y) > p.thr2) &
+                                         ((Gr >= row_lo && Gr < row_hi) ? colmask : 0u);
                     if (lane == 0) sMask[(m * 2 + b) * kHalves + h] = bal;
                 }
             }
@@ -860,13 +890,17 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 int* wc = sWarp + (kThreads / 32) * rd;
                 if (lane == 0) wc[wid] = __popc(bal);
                 __syncthreads();
-                int off = 0, tot = 0;
+                // every warp scans the warp counts (lane w <-> warp w)
+                constexpr int NWARP = kThreads / 32;
+                const int wx = (lane < NWARP) ? wc[lane] : 0;
+                int wincl = wx;
 #pragma unroll
-                for (int w = 0; w < kThreads / 32; ++w) {
-                    const int x = wc[w];
-                    off += (w < wid) ? x : 0;
-                    tot += x;
+                for (int d = 1; d < NWARP; d <<= 1) {
+                    const int y = __shfl_up_sync(0xffffffffu, wincl, d);
+                    if (lane >= d) wincl += y;
                 }
+                const int off = __shfl_sync(0xffffffffu, wincl - wx, wid);
+                const int tot = __shfl_sync(0xffffffffu, wincl, NWARP - 1);
                 if (acc) {
                     const int dpos = nacc + off + __popc(bal & ((1u << lane) - 1u));
                     if (TOED_IN_BOUNDS(dpos < C::MAXC, p.sc.words)) sList[dpos] = rec;
