@@ -517,7 +517,7 @@ def side_measurements(toed, det, images, side, stream):
         for sg in (1.0, 2.0):
             ref = oracle.detect(im.astype(np.float64), sg, nthreads=os.cpu_count())
             row = {}
-            for mode, pr in (("fp32_conv+fp64_epilogue", toed.TOED_HYBRID), ("all_fp32", toed.TOED_FP32)):
+            for mode, pr in (("hybrid", toed.TOED_HYBRID), ("all_fp32", toed.TOED_FP32)):
                 r = det.detect(torch.as_tensor(im).to(dev), sigma=sg, out_dtype=toed.TOED_F64, precision=pr)
                 gi = r["index"].cpu().numpy().astype(np.int64)
                 ge = r["edgels"].cpu().numpy()
@@ -745,7 +745,7 @@ def run_ours(args, ws, rank, local):
     line = {
         "metric": METRIC, "value": round(value, 2), "unit": "Mpixel/s", "n_gpus": ws, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 4), "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32 (FP64 per-edgel peak fit; FP64 TO orientation where the vector cancels)",
+        "vs_baseline": None, "dtype": "f32 (peak fit on exact FP32 differences; FP64 TO orientation where the vector cancels)",
         "data": "synthetic (seeded shapes generator; inputs 318 MB > L2, no flush needed)",
         "config": {"workload": "uneven batch: 64 float32 images, H and W U[256,2048] (x4), noise U[1,8]",
                    "launch": "one CUDA graph per step (persistent detection kernel + 3-kernel ordering pass)",

@@ -62,7 +62,8 @@ typedef enum toed_dtype {
 } toed_dtype;
 
 typedef enum toed_precision {
-    TOED_HYBRID = 0, /* FP32 convolutions; FP64 peak fit per edgel; edgels whose TO vector nearly
+    TOED_HYBRID = 0, /* FP32 convolutions; per-edgel peak fit whose cancelling sums are formed from
+                        exact differences of the FP32 magnitudes; edgels whose TO vector nearly
                         cancels get their derivatives and orientation recomputed in FP64 */
     TOED_FP32 = 1    /* everything FP32 (precision-study mode) */
 } toed_precision;

@@ -21,8 +21,8 @@
 //   5. per edgel only: the seven higher derivatives, contracted from the
 //      row-pass ring with the y taps of the edgel's sub-grid, then the
 //      third-order orientation
-//      (cpu_toed.cpp:227-232) and the peak fit with FP64 where they cancel
-//      (HYBRID) or in FP32; records are deferred in a ring and finished by
+//      (cpu_toed.cpp:227-232) and the peak fit, its cancelling sums taken
+//      on exact differences (HYBRID) or plain FP32; records are deferred in a ring and finished by
 //      all threads at once; the staged record goes to a staging area and the
 //      row's {offset, count} to the row-segment table that the ordering pass
 //      (toed_finalize.cu) turns into the reference's row-major edgel list.
@@ -439,6 +439,35 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     return r;
 }
 
+// The decision of nms_eval (gradient direction) without branches, for the
+// NMS stage: every value is formed unconditionally (the neighbour offsets are
+// within one row and column whatever the gradient) and the tests are combined
+// at the end, so a warp runs it as one straight sequence.
+__device__ __forceinline__ bool nms_decide(const float2* __restrict__ sFxy, int m, int c, float thr, int* dbg = nullptr)
+{
+    constexpr int FW = 2 * kExt;
+#ifdef TOED_DEBUG_BOUNDS
+    if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return false;
+#endif
+    const float2 g = sFxy[m * FW + c];
+    const float mv = grad_mag(g);
+    const float ax = fabsf(g.x), ay = fabsf(g.y);
+    const bool xmaj = ax >= ay;
+    const int sx = (g.x >= 0.f) ? 1 : -1, sy = (g.y >= 0.f) ? 1 : -1;
+    const float slope = __fdividef(fminf(ax, ay), fmaxf(ax, ay));
+    const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
+    const float Map = grad_mag(sFxy[(m + ar) * FW + c + ac]);
+    const float Mdp = grad_mag(sFxy[(m + sy) * FW + c + sx]);
+    const float Mam = grad_mag(sFxy[(m - ar) * FW + c - ac]);
+    const float Mdm = grad_mag(sFxy[(m - sy) * FW + c - sx]);
+    const float fp = Map * (1.f - slope) + Mdp * slope;
+    const float fm = Mam * (1.f - slope) + Mdm * slope;
+    const bool maxt = (mv > fm && mv >= fp) || (mv >= fm && mv > fp);
+    const float num = fp - fm, den = fm + fp - 2.f * mv;
+    return (mv > thr) && !(ax < 10e-6f && ay < 10e-6f) && maxt && den < 0.f &&
+           fabsf(num) * sqrt_approx(fmaf(slope, slope, 1.f)) <= -2.82842712f * den;
+}
+
 // The seven higher derivatives at 2x-grid slot (m, c) of the step window
 // from the row-pass ring (the Q planes hold the Gxx / Gxxx row responses):
 // fxx, fxy, fyy, fxxy, fxyy, fxxx, fyyy, contracted with the y taps of the
@@ -496,8 +525,8 @@ __device__ __forceinline__ void to_vec32(float gx, float gy, const float (&d)[7]
     *tiy = fmaf(2.f, fmaf(gx, bc, fmaf(gy, c2, pxy * fxyy)), fmaf(x2, fxxy, y2 * fyyy));
 }
 
-// Per-edgel epilogue from a deferred record: peak fit (FP64 in HYB mode:
-// the cancellations in fm + fp - 2f and fp - fm) and the third-order
+// Per-edgel epilogue from a deferred record: peak fit (in HYB mode with the
+// cancellations in fm + fp - 2f and fp - fm taken on exact differences) and the third-order
 // orientation (cpu_toed.cpp:227-232; in HYB mode listed for the FP64
 // recomputation when the vector nearly cancels), then the staged
 // output record (x, y, orientation, strength) at its reserved slot.  The
@@ -514,16 +543,17 @@ __device__ __noinline__ void finish_edgel(const float* __restrict__ rc, const Sc
     float x, y;  // the staged position (det_xy)
     float ori, str;
     if (HYB) {
-        // fp - fm and fm + fp - 2f cancel: formed exactly from the FP32
-        // inputs in FP64, then the well-conditioned rest in FP32
-        float num, den;
-        {
-            const double s1 = sl, c1 = 1.0 - s1;
-            const double fp = (double)Map * c1 + (double)Mdp * s1;
-            const double fm = (double)Mam * c1 + (double)Mdm * s1;
-            num = (float)(fp - fm);
-            den = (float)(fm + fp - 2.0 * (double)mv);
-        }
+        // fp - fm and fm + fp - 2f cancel.  With fp = Map + s (Mdp - Map) and
+        // fm = Mam + s (Mdm - Mam) both are formed from differences of nearly
+        // equal FP32 magnitudes (exact within a factor 2 of each other), the
+        // interpolation weight applied last:
+        //   fp - fm        = dA + s (dD - dA),  dA = Map - Mam, dD = Mdp - Mdm
+        //   fm + fp - 2f   = eA + s (eD - eA),  eA = (Map - f) + (Mam - f), eD likewise
+        // so no full-scale sum is rounded before the cancellation.
+        const float dA = Map - Mam, dD = Mdp - Mdm;
+        const float eA = (Map - mv) + (Mam - mv), eD = (Mdp - mv) + (Mdm - mv);
+        const float num = fmaf(sl, dD - dA, dA);
+        const float den = fmaf(sl, eD - eA, eA);
         const float ss = sqrtf(1.f + sl * sl);
         const float sst = -0.5f * num * ss / den;           // s* = -B / (2A)
         const float maxf = mv - 0.125f * num * num / den;   // A s*^2 + B s* + C
@@ -883,7 +913,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                         to_vec32(g.x, g.y, d7, &tx, &ty);
                         acc = nms_eval<true>(sFxy, m, c, p.thr, tx, ty, p.sc.words).cand;
                     } else {
-                        acc = nms_eval(sFxy, rec >> 8, rec & 255, p.thr, 0.f, 0.f, p.sc.words).cand;
+                        acc = nms_decide(sFxy, rec >> 8, rec & 255, p.thr, p.sc.words);
                     }
                 }
                 const unsigned bal = __ballot_sync(0xffffffffu, acc);
@@ -938,7 +968,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                         p.sc.seg[seg0 + (long long)Gr * im.nsc + sc] = make_int2(base + incl - cnt, cnt);
             }
             // ---- 5. per edgel: the seven higher derivatives from the row-pass
-            // ring into a deferred record (the FP64 epilogue runs when the
+            // ring into a deferred record (the epilogue runs when the
             // ring of records is full)
             {
                 for (int j0 = 0; j0 < nacc;) {
