@@ -135,6 +135,26 @@ __device__ __forceinline__ float2 df_mul_f(float a, float2 b)  // a float times 
 }
 __device__ __forceinline__ float2 df_half(float2 a) { return make_float2(0.5f * a.x, 0.5f * a.y); }  // exact
 
+// a b + c d + e f + g h in FP32 with the products split exactly (FMA) and
+// the sum compensated -- the Dot2 algorithm of Ogita, Rump and Oishi
+// ("Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005): the
+// result is as accurate as if computed in twice the working precision and
+// then rounded, which is what the four cancelling products need.
+// (The _rn intrinsics keep the compiler from contracting the error terms.)
+__device__ __forceinline__ float dot4_comp(float a, float b, float c, float d, float e, float f, float g, float h)
+{
+    float p = __fmul_rn(a, b), err = fmaf(a, b, -p);
+    const float x[3] = {c, e, g}, y[3] = {d, f, h};
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+        const float q = __fmul_rn(x[k], y[k]), qe = fmaf(x[k], y[k], -q);
+        const float2 t = df_two_sum(p, q);  // p + q = t.x + t.y exactly
+        err = __fadd_rn(err, __fadd_rn(t.y, qe));
+        p = t.x;
+    }
+    return __fadd_rn(p, err);
+}
+
 // The triangle filter (:316-321), weight (5 - |k|) / 25, as double-floats.
 template <int K>
 struct TriDF {
@@ -474,19 +494,22 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
         bool ok = false;
         float dx = 0.f, dy = 0.f, mag = 0.f;
         if (p.hyb) {
-            // fp - fm and fm + fp - 2f cancel: formed in FP64 from the FP32
-            // inputs; the well-conditioned rest in FP32.  s* = -B / (2A) with
-            // A = (fm + fp - 2f) / (2 s^2), B = (fp - fm) / (2 s) (:496-505)
+            // fp - fm and fm + fp - 2f cancel.  With fp = Map + s (Mdp - Map) and
+            // fm = Mam + s (Mdm - Mam) both come from differences of nearly equal
+            // FP32 values (exact within a factor 2 of each other), the weight
+            // applied last -- no full-scale sum is rounded before the
+            // cancellation; the well-conditioned rest in FP32.  s* = -B / (2A)
+            // with A = (fm + fp - 2f) / (2 s^2), B = (fp - fm) / (2 s) (:496-505)
             const float md = sqrtf(g.x * g.x + g.y * g.y);
             const float nx = g.x / md, ny = g.y / md;
             const float sl = xmaj ? fabsf(ny) / fabsf(nx) : fabsf(nx) / fabsf(ny);
-            const double s1 = sl, c1 = 1.0 - s1;
-            const double fp = (double)Map * c1 + (double)Mdp * s1, fm = (double)Mam * c1 + (double)Mdm * s1;
-            const double num = fp - fm, den = fm + fp - 2.0 * (double)f;
+            const float dA = Map - Mam, dD = Mdp - Mdm;
+            const float eA = (Map - f) + (Mam - f), eD = (Mdp - f) + (Mdm - f);
+            const float num = fmaf(sl, dD - dA, dA), den = fmaf(sl, eD - eA, eA);
             const float s = sqrtf(1.f + sl * sl);
-            if (!(fabs(den) < 2e-16 * (double)(s * s))) {  // |A| < 1e-16 (:502)
-                const float ss = -0.5f * (float)num * s / (float)den;
-                const float mf = f - 0.125f * (float)num * (float)num / (float)den;  // A s*^2 + B s* + f
+            if (!(fabsf(den) < 2e-16f * (s * s))) {  // |A| < 1e-16 (:502)
+                const float ss = -0.5f * num * s / den;
+                const float mf = f - 0.125f * num * num / den;  // A s*^2 + B s* + f
                 if (fabsf(ss) <= 1.41421356f) {
                     ok = true;
                     dx = ss * nx;
@@ -750,7 +773,8 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
     // per edgel: Keys bicubic of ten planes at (sx, sy), clamp to the image
     // (:521-556).  The interpolation is a short weighted sum of FP32
     // convolution outputs and runs in FP32; the F vector, whose four products
-    // can cancel, is formed in FP64 from the interpolated values (HYBRID).
+    // can cancel, is a compensated dot product of the interpolated values
+    // (HYBRID, dot4_comp).
     for (int e = tid; e < n_edg; e += blockDim.x) {
         int row = 0;  // last row with sOff[row] <= e
 #pragma unroll
@@ -765,9 +789,22 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
         const double sx = p.hyb ? (double)cj + (double)ox : (double)((float)cj + ox);
         const double sy = p.hyb ? (double)ci + (double)oy : (double)((float)ci + oy);
         rec.w = (double)__int_as_float(__double2loint(rec.w));
-        const int x0 = (int)floor(sx), y0 = (int)floor(sy);
-        const double fx = sx - x0, fy = sy - y0;
-        const float tfx = (float)fx, tfy = (float)fy;
+        // cell and fraction of the position: from the pixel and its FP32 offset
+        // (the fraction correctly rounded to FP32, as (float)(sx - floor(sx)))
+        int x0, y0;
+        float tfx, tfy;
+        if (p.hyb) {
+            const float flx = floorf(ox), fly = floorf(oy);
+            x0 = cj + (int)flx;
+            y0 = ci + (int)fly;
+            tfx = ox - flx;
+            tfy = oy - fly;
+        } else {
+            x0 = (int)floor(sx);
+            y0 = (int)floor(sy);
+            tfx = (float)(sx - x0);
+            tfy = (float)(sy - y0);
+        }
         float wx[4], wy[4];
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -810,28 +847,23 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
             for (int pl = 0; pl < 10; ++pl) v[pl] = fmaf(rowv[pl], wy[pp], v[pl]);
         }
         float ori;
-        double Fx, Fy, Fm;
+        float Fx, Fy;
+        // plane order: Px Py Pxx Pyy Pxy Hx Hxx Hxy Hyy Hy (:683-684)
         if (p.hyb) {
-            const double Px = v[0], Py = v[1], Pxx = v[2], Pyy = v[3], Pxy = v[4];
-            const double Hx = v[5], Hxx = v[6], Hxy = v[7], Hyy = v[8], Hy = v[9];
-            Fx = Px * Hxx + Pxx * Hx + Py * Hxy + Pxy * Hy;  // :683-684
-            Fy = Px * Hxy + Pxy * Hx + Py * Hyy + Pyy * Hy;
-            Fm = sqrt(Fx * Fx + Fy * Fy);
+            Fx = dot4_comp(v[0], v[6], v[2], v[5], v[1], v[7], v[4], v[9]);  // Px Hxx + Pxx Hx + Py Hxy + Pxy Hy
+            Fy = dot4_comp(v[0], v[7], v[4], v[5], v[1], v[8], v[3], v[9]);  // Px Hxy + Pxy Hx + Py Hyy + Pyy Hy
         } else {
-            const float fFx = v[0] * v[6] + v[2] * v[5] + v[1] * v[7] + v[4] * v[9];
-            const float fFy = v[0] * v[7] + v[4] * v[5] + v[1] * v[8] + v[3] * v[9];
-            Fx = fFx;
-            Fy = fFy;
-            Fm = sqrtf(fFx * fFx + fFy * fFy);
+            Fx = v[0] * v[6] + v[2] * v[5] + v[1] * v[7] + v[4] * v[9];
+            Fy = v[0] * v[7] + v[4] * v[5] + v[1] * v[8] + v[3] * v[9];
         }
-        if (Fm < 1e-12) {
+        // |F| < 1e-12: the NMS direction instead (:686-690); otherwise the
+        // angle of F itself (atan2 of the normalised vector is that of F)
+        if (fmaf(Fx, Fx, Fy * Fy) < 1e-24f) {
             const int pi = p.sc.staging_idx[sidx];
             const float2 d = p.dir[M.px_base + pi];
             ori = atan2f(d.x, -d.y);
         } else {
-            Fx /= Fm;
-            Fy /= Fm;
-            ori = atan2f((float)Fx, (float)(-Fy));
+            ori = atan2f(Fx, -Fy);
         }
         rec.z = (double)ori;
         // coord_scale (:657, :696-697): positions in original pixels
