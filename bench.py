@@ -700,23 +700,26 @@ def run_ours(args, ws, rank, local):
     for o, c in zip(h_outs, caps):
         o["capacity"] = c
     h2d = sum(im.nbytes for im in images)
-    d2h_total = 0
 
     h_batch = det.host_batch(h_imgs, h_outs)  # the buffers described once, as a serving loop would
 
     def e2e_step():
-        nonlocal d2h_total
+        # synchronous: when it returns, every list and count is in host memory
         det.detect_host(h_batch, params=params, chunks=E2E_CHUNKS, stream=stream)
-        d2h_total = sum(16 * min(int(o["count"].item()), o["capacity"]) + 4 for o in h_outs)
 
     for _ in range(max(1, args.warmup)):
         e2e_step()
     barrier(ws)
+    e2e_steps = []
     t0 = time.perf_counter()
     for _ in range(args.steps):
+        t1 = time.perf_counter()
         e2e_step()
+        e2e_steps.append((time.perf_counter() - t1) * 1e3)
     e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
     e2e_ms = max_over_ranks(e2e_ms, ws)
+    # bytes that came back per step (the same every step): the lists and counts
+    d2h_total = sum(16 * min(int(o["count"].item()), o["capacity"]) + 4 for o in h_outs)
     if [int(o["count"].item()) for o in h_outs] != counts:
         raise RuntimeError("host-buffer path disagrees with the device path")
 
@@ -756,7 +759,11 @@ def run_ours(args, ws, rank, local):
         "gpu_launches": 4 * args.steps,
         "kernel_ms": round(kernel_ms, 4),
         "e2e": {"value": round(ws * npx / (e2e_ms * 1e-3) / 1e6, 2), "unit": "Mpixel/s",
-                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h_total)},
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h_total),
+                # the call's spread over the timed steps (the value is the mean): the
+                # host memory and the C2C link are shared with the machine's other jobs
+                "step_ms": {"mean": round(e2e_ms, 4), "median": round(float(np.median(e2e_steps)), 4),
+                            "min": round(min(e2e_steps), 4), "max": round(max(e2e_steps), 4)}},
         # the contract's roofline is HBM (algorithmic bytes vs the measured
         # copy bandwidth); this stencil's binding roof is FP32 issue, given
         # beside it against the FP32 FMA rate measured in this process
