@@ -84,6 +84,7 @@ struct DetImage {
     int dtype;
     int cap;
     int nsc, nsr;        // strip columns / strip rows
+    int S;               // strip inner rows of this image's work units (multiple of kStepRows minus 2)
     int unit_base;       // first work unit
     int tile_base;       // first ordering tile
     int tma;             // 1: rows arrive by TMA through BatchParams::tmap[k]; 2: by per-thread async
@@ -134,7 +135,8 @@ struct BatchParams {
     float thr;
     float thr2;          // candidate prefilter on |grad I|^2: a little below thr^2 (-1 when thr < 0)
     int border;
-    int S;               // strip inner rows (multiple of kStepRows minus 2)
+    int S;               // strip inner rows of most work units (multiple of kStepRows minus 2); the
+                         // images at the end of the queue may use shorter ones (DetImage::S)
     int n_img;
     int n_units;
     int n_tiles;

@@ -688,8 +688,8 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         const int H = im.H, W = im.W, dtype = im.dtype;
         const int local = u - im.unit_base;
         const int sr = local / im.nsc, sc = local - sr * im.nsc;
-        const int ys = sr * p.S, x0 = sc * kInner;
-        const int S_act = min(p.S, H - ys);
+        const int ys = sr * im.S, x0 = sc * kInner;
+        const int S_act = min(im.S, H - ys);
         if (im.wait_slot > 0) {  // pixels still arriving: wait for the group (uniform across the CTA)
             if (tid == 0)
                 sScal[2] = wait_ready(p.ready + (im.wait_slot - 1), p.ready_epoch, p.ready_spins, p.sc.words) ? 1 : 0;

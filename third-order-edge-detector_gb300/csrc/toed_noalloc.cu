@@ -179,6 +179,7 @@ extern "C" toed_status toed_detect_noalloc(const toed_image* im, const toed_para
     d.dtype = im->dtype;
     d.cap = im->capacity;
     d.nsc = nsc;
+    d.S = S;
     d.nsr = (im->height + S - 1) / S;
     d.unit_base = 0;
     d.tile_base = 0;
