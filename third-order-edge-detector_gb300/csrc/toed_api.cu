@@ -445,18 +445,23 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     p->ready_epoch = c->hb_epoch;
     p->ready_spins = c->ready_spins;
     // A work unit at the tuned shape can take several percent of the launch
-    // (a 510-row unit about 130 us of a 2.2 ms batch), and as the queue
-    // drains the last units leave SMs idle while they run: the images that
-    // start in the last tenth of the batch's pixels use short strips (126
-    // rows), so the launch ends with small units.
+    // (a 1022-row unit about 260 us of a 2.2 ms batch), and as the queue
+    // drains the last units leave SMs idle while they run.  So an image's
+    // strips are halved (1022 -> 510 -> ... -> 30 rows) until the pixels from
+    // its start to the end of the batch hold at least one of its units per
+    // resident CTA: the launch ends with small units.  (Measured on a 64-image
+    // batch: 2.155 ms, against 2.158 with two units per CTA, 2.182 with four
+    // and 2.221 without.  A single image keeps the tuned strips, which the
+    // tuner picks for its size alone.)
     long long npx = 0, cum = 0;
     for (int i = 0; i < n; ++i) npx += (long long)images[i].width * images[i].height;
-    const int s_tail = std::min(p->S, 8 * kStepRows - 2);
     long long units = 0, tiles = 0, staging = 0;
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
         DetImage& d = p->img[i];
-        d.S = (n > 1 && 10 * cum >= 9 * npx) ? s_tail : p->S;
+        d.S = p->S;
+        while (n > 1 && d.S > 2 * kStepRows - 2 && (long long)d.S * kInner * resident > npx - cum)
+            d.S = (d.S + 2) / 2 - 2;
         cum += (long long)im.width * im.height;
         d.src = im.pixels;
         d.pitch = im.pitch;
