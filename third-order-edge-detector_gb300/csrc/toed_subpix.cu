@@ -135,6 +135,24 @@ __device__ __forceinline__ float2 df_mul_f(float a, float2 b)  // a float times 
 }
 __device__ __forceinline__ float2 df_half(float2 a) { return make_float2(0.5f * a.x, 0.5f * a.y); }  // exact
 
+// The NMS max test's near ties (cp or cm == 2) decided in FP64 on the same
+// FP32 inputs, the products exact: f ga against Map (ga - gb) + Mdp gb and
+// Mam (ga - gb) + Mdm gb (a few pixels per map; out of line, so that the
+// conversions stay off the per-pixel path).
+static __device__ __noinline__ void max_test_fp64(float f, float ga, float gb, float Map, float Mdp, float Mam,
+                                                  float Mdm, int* cp, int* cm)
+{
+    const double gad = ga, gbd = gb, d = gad - gbd, fD = (double)f * gad;
+    if (*cp == 2) {
+        const double fpD = fma((double)Map, d, (double)Mdp * gbd);
+        *cp = fD > fpD ? 1 : (fD < fpD ? -1 : 0);
+    }
+    if (*cm == 2) {
+        const double fmD = fma((double)Mam, d, (double)Mdm * gbd);
+        *cm = fD > fmD ? 1 : (fD < fmD ? -1 : 0);
+    }
+}
+
 // a b + c d + e f + g h in FP32 with the products split exactly (FMA) and
 // the sum compensated -- the Dot2 algorithm of Ogita, Rump and Oishi
 // ("Accurate sum and dot product", SIAM J. Sci. Comput. 26, 2005): the
@@ -434,17 +452,7 @@ __global__ void __launch_bounds__(256, 5) tc_orient_nms(const __grid_constant__ 
                     const float tol = 1e-5f * ga * (fabsf(f) + fabsf(Map) + fabsf(Mdp) + fabsf(Mam) + fabsf(Mdm));
                     int cp = (Map == f && Mdp == f) ? 0 : (fS - fpS > tol ? 1 : (fpS - fS > tol ? -1 : 2));
                     int cm = (Mam == f && Mdm == f) ? 0 : (fS - fmS > tol ? 1 : (fmS - fS > tol ? -1 : 2));
-                    if (cp == 2 || cm == 2) {
-                        const double gad = ga, gbd = gb, d = gad - gbd, fD = (double)f * gad;
-                        if (cp == 2) {
-                            const double fpD = fma((double)Map, d, (double)Mdp * gbd);
-                            cp = fD > fpD ? 1 : (fD < fpD ? -1 : 0);
-                        }
-                        if (cm == 2) {
-                            const double fmD = fma((double)Mam, d, (double)Mdm * gbd);
-                            cm = fD > fmD ? 1 : (fD < fmD ? -1 : 0);
-                        }
-                    }
+                    if (cp == 2 || cm == 2) max_test_fp64(f, ga, gb, Map, Mdp, Mam, Mdm, &cp, &cm);
                     cand = (cm > 0 && cp >= 0) || (cm >= 0 && cp > 0);  // :466-468
                 } else {
                     const float md = sqrtf(g.x * g.x + g.y * g.y);
@@ -775,6 +783,7 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
     // convolution outputs and runs in FP32; the F vector, whose four products
     // can cancel, is a compensated dot product of the interpolated values
     // (HYBRID, dot4_comp).
+    const double inv_scale = 1.0 / (double)M.scale;  // 2^-interp_n: the products below are exact
     for (int e = tid; e < n_edg; e += blockDim.x) {
         int row = 0;  // last row with sOff[row] <= e
 #pragma unroll
@@ -867,8 +876,8 @@ __global__ void __launch_bounds__(512, 2) tc_correct(const __grid_constant__ Sub
         }
         rec.z = (double)ori;
         // coord_scale (:657, :696-697): positions in original pixels
-        rec.x = sx / (double)M.scale;
-        rec.y = sy / (double)M.scale;
+        rec.x = sx * inv_scale;
+        rec.y = sy * inv_scale;
         p.sc.staging[sidx] = rec;
     }
 }
