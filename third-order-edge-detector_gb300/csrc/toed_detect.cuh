@@ -171,28 +171,70 @@ struct AsyncBox {
     static_assert(2 * B * BW * 4 <= C::sz_raw, "two boxes fit the staging buffer");
 };
 
+// A thread's part of the async row staging, fixed for a work unit: its
+// 16-byte chunk of every box (box row rr, chunk k: image columns x .. x+3,
+// x = xa + 4k with xa the 16-byte-aligned column at or before the window's
+// first column) and where the chunk's four floats go in the input ring.
+struct AsyncLane {
+    long long x;        // image column of the chunk's first float (may be < 0 at the left edge)
+    int box;            // rr * BW + 4k: the chunk's offset in a box
+    int ccol;           // 4k - shift: ring column of the chunk's first float
+    int rr;             // box row
+    unsigned cmask;     // bit e: ring column ccol + e lies in [0, NIN)
+    unsigned imask;     // bit e: image column x + e lies in [0, W)
+    bool full;          // one 16-byte copy: aligned rows and all four columns inside the image
+    bool on;            // the thread owns a chunk (t < B * CH)
+};
+
 template <int R>
-__device__ __forceinline__ void async_issue_box(float* rawf, const float* fsrc, long long pitch, int H, int W, int xa,
-                                                int ys, int nsteps, int q, bool al16)
+__device__ __forceinline__ AsyncLane async_lane(const float* fsrc, long long pitch, int W, int xin)
+{
+    using C = Cfg<R>;
+    using A = AsyncBox<R>;
+    AsyncLane l;
+    const int t = threadIdx.x;
+    l.on = t < A::B * A::CH;
+    l.rr = t / A::CH;
+    const int k = t - l.rr * A::CH;
+    const int xa = xin - (((xin % 4) + 4) % 4), shift = xin - xa;
+    l.x = xa + 4 * k;
+    l.box = l.rr * A::BW + 4 * k;
+    l.ccol = 4 * k - shift;
+    l.cmask = 0u;
+    l.imask = 0u;
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        if (l.ccol + e >= 0 && l.ccol + e < C::NIN) l.cmask |= 1u << e;
+        if ((unsigned long long)(l.x + e) < (unsigned long long)W) l.imask |= 1u << e;
+    }
+    const bool al16 = ((reinterpret_cast<uintptr_t>(fsrc) & 15u) == 0) && ((pitch & 3) == 0);
+    l.full = al16 && l.imask == 0xFu;
+    return l;
+}
+
+template <int R>
+__device__ __forceinline__ void async_issue_box(float* rawf, const float* fsrc, long long pitch, int H,
+                                                const AsyncLane& l, int ys, int nsteps, int q)
 {
     using A = AsyncBox<R>;
     constexpr int B = A::B;
-    const int t = threadIdx.x;
     const int last = A::Q0 + nsteps - 2;  // the last box of the unit
-    if (q <= last && t < B * A::CH) {
-        const int rr = t / A::CH, k = t - rr * A::CH;
+    if (q <= last && l.on) {
         const int row0 = (q < A::Q0) ? ys - R - 3 + q * B : ys + (q - A::Q0 + 1) * B + R;
-        const int y = row0 + rr, x = xa + 4 * k;
-        float* dst = rawf + (q & 1) * (B * A::BW) + rr * A::BW + 4 * k;
+        const int y = row0 + l.rr;
+        float* dst = rawf + (q & 1) * (B * A::BW) + l.box;
         const bool rowin = (unsigned)y < (unsigned)H;
-        if (al16 && rowin && x >= 0 && x + 4 <= W) {
-            asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(fsrc + (long long)y * pitch + x)
+        const float* srow = fsrc + (rowin ? (long long)y * pitch + l.x : 0);
+        if (l.full) {
+            // rows outside the image: zero fill, nothing read
+            asm volatile("cp.async.ca.shared.global [%0], [%1], 16, %2;" ::"r"(smem_addr(dst)), "l"(srow),
+                         "r"(rowin ? 16 : 0)
                          : "memory");
         } else {
 #pragma unroll
             for (int e = 0; e < 4; ++e) {
-                const bool in = rowin && (unsigned)(x + e) < (unsigned)W;
-                cp_async4(smem_addr(dst + e), in ? fsrc + (long long)y * pitch + x + e : fsrc, in ? 4 : 0);
+                const bool in = rowin && ((l.imask >> e) & 1u);
+                cp_async4(smem_addr(dst + e), in ? srow + e : fsrc, in ? 4 : 0);
             }
         }
     }
@@ -201,42 +243,34 @@ __device__ __forceinline__ void async_issue_box(float* rawf, const float* fsrc, 
 
 template <int R>
 __device__ __forceinline__ void stage_rows_async(float* __restrict__ sIn, unsigned char* sRaw, const float* fsrc,
-                                                 long long pitch, int H, int W, int xin, int ys, int s, int nsteps,
-                                                 int rb, int* dbg)
+                                                 long long pitch, int H, const AsyncLane& l, int ys, int s,
+                                                 int nsteps, int rb, int* dbg)
 {
     using C = Cfg<R>;
     using A = AsyncBox<R>;
     constexpr int B = C::B;
-    const int t = threadIdx.x;
     float* rawf = reinterpret_cast<float*>(sRaw);
-    const int xa = xin - (((xin % 4) + 4) % 4), shift = xin - xa;
-    const bool al16 = ((reinterpret_cast<uintptr_t>(fsrc) & 15u) == 0) && ((pitch & 3) == 0);
     if (s == 0) {
-        async_issue_box<R>(rawf, fsrc, pitch, H, W, xa, ys, nsteps, 0, al16);
-        async_issue_box<R>(rawf, fsrc, pitch, H, W, xa, ys, nsteps, 1, al16);
+        async_issue_box<R>(rawf, fsrc, pitch, H, l, ys, nsteps, 0);
+        async_issue_box<R>(rawf, fsrc, pitch, H, l, ys, nsteps, 1);
     }
     const int q0 = (s == 0) ? 0 : A::Q0 - 1 + s, q1 = (s == 0) ? A::Q0 : q0 + 1;
     for (int q = q0; q < q1; ++q) {
         asm volatile("cp.async.wait_group 1;" ::: "memory");
         const int nrows = (s == 0) ? min(B, C::HS - q * B) : B;
         const int a0 = (s == 0) ? q * B : rb + 2 * R + 3;  // ring row of the box's row 0 (before wrapping)
-        if (t < B * A::CH) {
-            const int rr = t / A::CH, k = t - rr * A::CH;
-            const float* src = rawf + (q & 1) * (B * A::BW) + rr * A::BW + 4 * k;
-            if (rr < nrows) {
-                float* dst = sIn + ring_wrap<C::RING>(a0 + rr) * C::NIN;
-#pragma unroll
-                for (int e = 0; e < 4; ++e) {
-                    const int cc = 4 * k + e - shift;  // ring column
-                    if (cc >= 0 && cc < C::NIN &&
-                        TOED_IN_BOUNDS(ring_wrap<C::RING>(a0 + rr) < C::RING &&
-                                           (q & 1) * (B * A::BW) + rr * A::BW + 4 * k + e < 2 * B * A::BW,
-                                       dbg))
-                        dst[cc] = src[e];
-                }
+        if (l.on && l.rr < nrows) {
+            const float4 v = *reinterpret_cast<const float4*>(rawf + (q & 1) * (B * A::BW) + l.box);
+            const int ph = ring_wrap<C::RING>(a0 + l.rr);
+            float* dst = sIn + ph * C::NIN + l.ccol;
+            if (TOED_IN_BOUNDS(ph < C::RING && (q & 1) * (B * A::BW) + l.box + 3 < 2 * B * A::BW, dbg)) {
+                if (l.cmask & 1u) dst[0] = v.x;
+                if (l.cmask & 2u) dst[1] = v.y;
+                if (l.cmask & 4u) dst[2] = v.z;
+                if (l.cmask & 8u) dst[3] = v.w;
             }
         }
-        async_issue_box<R>(rawf, fsrc, pitch, H, W, xa, ys, nsteps, q + 2, al16);
+        async_issue_box<R>(rawf, fsrc, pitch, H, l, ys, nsteps, q + 2);
     }
 }
 
@@ -723,13 +757,16 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         for (int i = tid; i < 2 * C::FW; i += kThreads) sFxy[i] = make_float2(0.f, 0.f);
         if (tid < 4 * kHalves) sMask[tid] = 0u;
 
+        // async row staging: this thread's chunk of every box, fixed for the unit
+        AsyncLane alane{};
+        if (ASYNC && im.tma == 2) alane = async_lane<R>(static_cast<const float*>(src), pitch, W, xin);
         int rb = 0;
         for (int s = 0; s < nsteps; ++s) {
             // logical slot h <-> ring row (rb + h) mod RING <-> ext row
             // s*B - R - 2 + h <-> image row ys - 1 + ext row
             // ---- 1. input rows -> input ring (FP32, zero padded) -----------
             if (ASYNC && im.tma == 2) {
-                stage_rows_async<R>(sIn, sRaw, static_cast<const float*>(src), pitch, H, W, xin, ys, s, nsteps, rb,
+                stage_rows_async<R>(sIn, sRaw, static_cast<const float*>(src), pitch, H, alane, ys, s, nsteps, rb,
                                     p.sc.words);
                 __syncthreads();  // every thread's rows are in before the row pass
             } else if (!ASYNC && im.tma == 1) {
