@@ -447,7 +447,8 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     // A work unit at the tuned shape can take several percent of the launch
     // (a 1022-row unit about 260 us of a 2.2 ms batch), and as the queue
     // drains the last units leave SMs idle while they run.  So an image's
-    // strips are halved (1022 -> 510 -> ... -> 30 rows) until the pixels from
+    // strips are halved (1022 -> 510 -> ... -> 30 rows; 64 steps -> 32 ->
+    // ... -> 2) until the pixels from
     // its start to the end of the batch hold at least one of its units per
     // resident CTA: the launch ends with small units.  (Measured on a 64-image
     // batch: 2.155 ms, against 2.158 with two units per CTA, 2.182 with four
@@ -459,9 +460,10 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     for (int i = 0; i < n; ++i) {
         const toed_image& im = images[i];
         DetImage& d = p->img[i];
-        d.S = p->S;
-        while (n > 1 && d.S > 2 * kStepRows - 2 && (long long)d.S * kInner * resident > npx - cum)
-            d.S = (d.S + 2) / 2 - 2;
+        int ksteps = (p->S + 2) / kStepRows;  // steps per strip
+        while (n > 1 && ksteps > 2 && (long long)(ksteps * kStepRows - 2) * kInner * resident > npx - cum)
+            ksteps = std::max(2, ksteps / 2);
+        d.S = ksteps * kStepRows - 2;
         cum += (long long)im.width * im.height;
         d.src = im.pixels;
         d.pitch = im.pitch;
@@ -618,9 +620,12 @@ extern "C" toed_status toed_autotune(toed_ctx* c, const toed_image* images, int 
             g_last_cuda_error = std::string("autotune: ") + cudaGetErrorString(ce);
             st = TOED_ERR_CUDA;
         }
-        static const int steps[] = {1, 2, 4, 8, 16, 32, 64};
+        // strip heights of 1..64 steps: powers of two and the steps between
+        // them (a small image's best height fills the resident CTAs once)
+        static const int steps[] = {1, 2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64};
+        constexpr int kCand = (int)(sizeof(steps) / sizeof(steps[0]));
         for (int staging = 2; staging >= 0 && st == TOED_OK; --staging)
-            for (int k = 0; k < 7 && st == TOED_OK; ++k) {
+            for (int k = 0; k < kCand && st == TOED_OK; ++k) {
                 toed_tuning cand = {steps[k] * kStepRows - 2, staging, 0.f};
                 st = detect_all(c, images, n, prm, stream, &cand);  // untimed: scratch, caches
                 if (st != TOED_OK) break;
