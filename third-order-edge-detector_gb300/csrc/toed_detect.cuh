@@ -5,26 +5,28 @@
 // (32 with a one-pixel ring) by S output rows.  The CTA slides down the strip
 // in steps of B = 16 rows, keeping everything on chip:
 //
-//   1. B new input rows (+ halo) arrive by TMA (or plain loads) and are
+//   1. B new input rows (+ halo) arrive by TMA, by per-thread async copies
+//      (float32; the ASYNC instantiation) or by plain loads, and are
 //      converted to FP32 into a ring of input rows;
 //   2. row pass: twelve horizontal responses -- G, Gx, Gxx and Gxxx, each
 //      truncated to 2r+1 taps (T), full 2r+3 taps (F) and half-pixel shifted
 //      (S) -- into a ring of row-pass rows (G, Gx feed the dense first
 //      derivatives, Gxx, Gxxx the per-edgel ones);
 //   3. column pass: Ix and Iy at the four half-pixel sub-grids (the 2x grid
-//      of the reference, cpu_toed.cpp:204-355) for the B new rows, |grad I|,
-//      and the threshold test as one ballot mask per (2x row, column parity);
+//      of the reference, cpu_toed.cpp:204-355) for the B new rows, and the
+//      threshold test on |grad I|^2 as one ballot mask per (2x row, column
+//      parity);
 //   4. the points above the threshold listed in row-major order; subpixel
 //      NMS along the gradient with the reference's 8-sector interpolation,
 //      max test and parabola fit (cpu_toed.cpp:399-495), decided in FP32;
 //      survivors compacted in order;
 //   5. per edgel only: the seven higher derivatives, contracted from the
 //      row-pass ring with the y taps of the edgel's sub-grid, then the
-//      third-order orientation
-//      (cpu_toed.cpp:227-232) and the peak fit, its cancelling sums taken
-//      on exact differences (HYBRID) or plain FP32; records are deferred in a ring and finished by
-//      all threads at once; the staged record goes to a staging area and the
-//      row's {offset, count} to the row-segment table that the ordering pass
+//      third-order orientation (cpu_toed.cpp:227-232) and the peak fit, its
+//      cancelling sums taken on exact differences (HYBRID) or plain FP32;
+//      records are deferred in a ring and finished by all threads at once;
+//      the staged record goes to a staging area and the row's {offset,
+//      count} to the row-segment table that the ordering pass
 //      (toed_finalize.cu) turns into the reference's row-major edgel list.
 //
 // Both rings hold a multiple of 8 rows (the live window rounded up) and are
