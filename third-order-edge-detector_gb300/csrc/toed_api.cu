@@ -447,13 +447,13 @@ static toed_status detect_chunk(toed_ctx* c, const toed_image* images, int n, co
     // A work unit at the tuned shape can take several percent of the launch
     // (a 1022-row unit about 260 us of a 2.2 ms batch), and as the queue
     // drains the last units leave SMs idle while they run.  So an image's
-    // strips are halved (1022 -> 510 -> ... -> 30 rows; 64 steps -> 32 ->
-    // ... -> 2) until the pixels from
-    // its start to the end of the batch hold at least one of its units per
-    // resident CTA: the launch ends with small units.  (Measured on a 64-image
-    // batch: 2.155 ms, against 2.158 with two units per CTA, 2.182 with four
-    // and 2.221 without.  A single image keeps the tuned strips, which the
-    // tuner picks for its size alone.)
+    // strips are halved (64 steps of 16 rows -> 32 -> ... -> 2, i.e. 1022
+    // -> 510 -> ... -> 30 rows) until the pixels from its start to the end
+    // of the batch hold at least one of its units per resident CTA: the
+    // launch ends with small units.  (Measured on a 64-image batch: 2.155 ms,
+    // against 2.158 with two units per CTA, 2.182 with four and 2.221
+    // without.  A single image keeps the tuned strips, which the tuner picks
+    // for its size alone.)
     long long npx = 0, cum = 0;
     for (int i = 0; i < n; ++i) npx += (long long)images[i].width * images[i].height;
     long long units = 0, tiles = 0, staging = 0;
