@@ -896,19 +896,25 @@ extern "C" toed_status toed_detect_host_batch(toed_ctx* c, const toed_host_image
         std::vector<int> slot(n);
         for (int k = 0; k < chunks; ++k)
             for (int i = first[k]; i < first[k + 1]; ++i) slot[i] = k + 1;
+        auto enqueue_group = [&](int k) -> cudaError_t {  // group k's pixels, then its flag, on s_in
+            NvtxRange r("toed: copy group");
+            cudaError_t e = copy_group(k);
+            if (e == cudaSuccess && k != withhold)
+                e = cudaMemcpyAsync(c->hb_ready + k, c->hb_epoch_src, sizeof(int), cudaMemcpyHostToDevice, c->s_in);
+            return e;
+        };
+        // the first two groups go in before the launch, so that their pixels
+        // are crossing while it is set up (the copies never wait for the
+        // launch, so nothing up to it can wait on the device for long)
+        const int early = std::min(chunks, 2);
+        for (int k = 0; k < early; ++k) TOED_HB(enqueue_group(k));
         TOED_HB(preload_finalize(radius_of(prm), prm->orientation == TOED_ORI_QAD));
         st = detect_all(c, dev.data(), n, prm, stream, nullptr, true, slot.data());
         c->ready_spins = kReadySpinLimit;
         if (st != TOED_OK) return fail(st);
         TOED_HB(cudaMemcpyAsync(c->hb_cnt + n, c->words + 2, sizeof(int), cudaMemcpyDeviceToDevice, stream));
         TOED_HB(cudaEventRecord(ev_det[0], stream));
-        for (int k = 0; k < chunks; ++k) {
-            NvtxRange r("toed: copy group");
-            TOED_HB(copy_group(k));
-            if (k != withhold)
-                TOED_HB(cudaMemcpyAsync(c->hb_ready + k, c->hb_epoch_src, sizeof(int), cudaMemcpyHostToDevice,
-                                        c->s_in));
-        }
+        for (int k = early; k < chunks; ++k) TOED_HB(enqueue_group(k));
         launches = 1;
         first[1] = n;
     } else {
