@@ -136,9 +136,12 @@ __device__ __forceinline__ void eval_edgel_warp(const BwImage& im, int rho, int 
         }
     }
     // ---- P: nine derivatives and their d/dsigma ----
+    float pc0, pc1, ps0, ps1;  // P's (G, Gy) y contractions and their d/dsigma, for the neighbours
+    int pyv;
     {
         int xv, yv;
         variants(rho, kap, &xv, &yv);
+        pyv = yv;
         // y tap of union row u: pp = NT - u (entry NT + 2 - u); x tap of lane: qq = NT - lane
         const float4* YA = sA + yv * NTP + NT + 2;
         const float4* YS = sS + yv * NTP + NT + 2;
@@ -168,6 +171,7 @@ __device__ __forceinline__ void eval_edgel_warp(const BwImage& im, int rho, int 
         __syncwarp();
         if (lane < 18) row[lane] = column_sum(red[lane], NU);
         __syncwarp();
+        pc0 = c0; pc1 = c1; ps0 = s0; ps1 = s1;
     }
     // ---- the frozen sector (cpu_toed.cpp:415-462 in closed form) and the
     // four neighbours' fx, fy with their d/dsigma ----
@@ -177,20 +181,42 @@ __device__ __forceinline__ void eval_edgel_warp(const BwImage& im, int rho, int 
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
     const int nr[4] = {rho + ar, rho + sy, rho - ar, rho - sy};  // A+, D+, A-, D-
     const int nc[4] = {kap + ac, kap + sx, kap - ac, kap - sx};
+    // A point's y contractions depend only on its y taps (variant yv) and
+    // its row offset di: a neighbour that shares both with P or with an
+    // earlier neighbour (in x-major sectors A+ and A- always do, and both
+    // share P's when P is on an odd 2x row) reuses those sums -- the same
+    // products in the same order, so the values are identical.
+    float qcg[4], qcy[4], qsg[4], qsy[4];
+    int qkey[4];
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
         int xv, yv;
         variants(nr[q], nc[q], &xv, &yv);
         const int di = (nr[q] >> 1) - i, dj = (nc[q] >> 1) - j;
-        const float4* YA = sA + yv * NTP + NT + 2 + di;
-        const float4* YS = sS + yv * NTP + NT + 2 + di;
+        const int key = yv * 4 + (di + 1);
+        qkey[q] = key;
         float cg = 0.f, cy = 0.f, sg = 0.f, sy_ = 0.f;
+        int from = -1;  // an earlier neighbour with the same sums (warp-uniform)
 #pragma unroll
-        for (int u = 0; u < NU; ++u) {
-            const float4 ya = YA[-u], ys = YS[-u];
-            cg = fmaf(v[u], ya.x, cg); cy = fmaf(v[u], ya.y, cy);
-            sg = fmaf(v[u], ys.x, sg); sy_ = fmaf(v[u], ys.y, sy_);
+        for (int q2 = 0; q2 < q; ++q2)
+            if (from < 0 && qkey[q2] == key) from = q2;
+        if (key == pyv * 4 + 1) {
+            cg = pc0; cy = pc1; sg = ps0; sy_ = ps1;
+        } else if (from >= 0) {
+#pragma unroll
+            for (int q2 = 0; q2 < q; ++q2)
+                if (q2 == from) { cg = qcg[q2]; cy = qcy[q2]; sg = qsg[q2]; sy_ = qsy[q2]; }
+        } else {
+            const float4* YA = sA + yv * NTP + NT + 2 + di;
+            const float4* YS = sS + yv * NTP + NT + 2 + di;
+#pragma unroll
+            for (int u = 0; u < NU; ++u) {
+                const float4 ya = YA[-u], ys = YS[-u];
+                cg = fmaf(v[u], ya.x, cg); cy = fmaf(v[u], ya.y, cy);
+                sg = fmaf(v[u], ys.x, sg); sy_ = fmaf(v[u], ys.y, sy_);
+            }
         }
+        qcg[q] = cg; qcy[q] = cy; qsg[q] = sg; qsy[q] = sy_;
         if (lane < NU) {
             const float4 xa = sA[xv * NTP + NT + 2 + dj - lane], xs = sS[xv * NTP + NT + 2 + dj - lane];
             red[18 + 4 * q][lane] = xa.y * cg;                   // fx (Gx, G)
