@@ -256,8 +256,12 @@ class HostBatch:
                                      o["index"].data_ptr() if o.get("index") is not None else None)
         self.arr = arr
 
-    def run(self, params: toed_params, chunks: int = 4, stream=None):
+    def run(self, params: toed_params, chunks=None, stream=None):
+        """chunks: copy groups (None: one image per group, the fastest for
+        page-locked images; 1: page-locked images read in place)."""
         det = self.det
+        if chunks is None:
+            chunks = len(self.images)
         s = stream if stream is not None else det.torch.cuda.current_stream(det.device)
         _check(lib().toed_detect_host_batch(det._ctx, self.arr, len(self.images), ctypes.byref(params), int(chunks),
                                             ctypes.c_void_p(s.cuda_stream)), "toed_detect_host_batch")
@@ -390,12 +394,13 @@ class Detector:
         toed_host_image describing them, so each call is one C call."""
         return HostBatch(self, images, outs)
 
-    def detect_host(self, images, outs=None, params: toed_params = None, chunks: int = 4, stream=None):
+    def detect_host(self, images, outs=None, params: toed_params = None, chunks=None, stream=None):
         """Detect edgels in images held in host memory (2-D CPU tensors,
         page-locked for full speed) into host buffers from
         alloc_host_outputs: copies in, detection and copies out are
-        pipelined over ``chunks`` groups (synchronous).  ``images`` may be a
-        HostBatch from host_batch() (then ``outs`` is None)."""
+        pipelined over ``chunks`` groups (synchronous; None: one image per
+        group).  ``images`` may be a HostBatch from host_batch() (then
+        ``outs`` is None)."""
         if params is None:
             raise ValueError("params required (make_params)")
         hb = images if isinstance(images, HostBatch) else HostBatch(self, images, outs)
