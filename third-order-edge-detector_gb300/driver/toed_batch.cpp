@@ -252,7 +252,7 @@ int main(int argc, char** argv)
             arr.push_back(h);
             slot.push_back(i);
         }
-        toed_status st = arr.empty() ? TOED_OK : toed_detect_host_batch(ctx, arr.data(), (int)arr.size(), &prm, 4, 0);
+        toed_status st = arr.empty() ? TOED_OK : toed_detect_host_batch(ctx, arr.data(), (int)arr.size(), &prm, (int)arr.size(), 0);  // one image per copy group
         if (out_cap < need) st = TOED_ERR_CAPACITY;
         for (size_t k = 0; k < arr.size(); ++k) {
             Image& im = cur[slot[k]];
