@@ -190,7 +190,9 @@ typedef struct toed_subpix_params {
     float sigma;       /* Gaussian scale; radius ceil(4 sigma) <= TOED_MAX_RADIUS */
     float nbr_radius;  /* drop edgels with no other edgel within this distance; <= 0 keeps all (default 2) */
     int out_dtype;     /* TOED_F32 or TOED_F64 */
-    int precision;     /* TOED_HYBRID: FP64 peak fit and orientation correction per edgel */
+    int precision;     /* TOED_HYBRID: orientation estimate in double-float arithmetic where NMS
+                          candidates lie, peak fit on exact FP32 differences, correction vector as
+                          a compensated FP32 dot product, FP64 near-tie max tests; TOED_FP32: FP32 */
     int interp_n;      /* 0..4: work on the 2^n grid ((h-1) 2^n + 1 rows), the map (and theta)
                           bilinearly resized onto it; positions in original pixels
                           (the reference's interp_n, subpix_to_correction.cpp:95-105, :224-244) */

@@ -143,7 +143,8 @@ struct BatchParams {
     int out_f64;
     int radius;
     int stage_blk;       // staging records reserved per atomic (1: exactly each step's edgels)
-    int hyb;             // 1: FP64 peak fit, FP64 recomputation of ill-conditioned orientations (TOED_HYBRID)
+    int hyb;             // 1: peak fit on exact FP32 differences, FP64 recomputation of ill-conditioned
+                         // orientations (TOED_HYBRID)
     int qad;             // 1: orientation from derivatives interpolated at the subpixel point (TOED_ORI_QAD)
     int nms_to;          // 1: NMS and peak fit along the corrected normal (TOED_NMS_TO_NORMAL)
     int det_rec;         // ordering pass input: 1 the detection's float4 records (det_stage), 0 the TO
