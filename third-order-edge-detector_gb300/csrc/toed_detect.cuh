@@ -64,7 +64,11 @@ struct Cfg {
     static constexpr size_t off_mbar = off_raw + sz_raw;
     static constexpr size_t off_in = align_up(off_mbar + 16, 16);
     static constexpr size_t off_P = align_up(off_in + sizeof(float) * RING * NIN, 16);
-    static constexpr size_t off_fxy = off_P + sizeof(float2) * 6 * RING * kExt;
+    // row-pass ring rows are PS float2 apart: two spare entries per row shift
+    // each row by four banks, so that the per-edgel stage's scattered reads
+    // (one edgel's column per lane) collide less
+    static constexpr int PS = kExt + 2;
+    static constexpr size_t off_fxy = off_P + sizeof(float2) * 6 * RING * PS;
     static constexpr size_t off_mask = off_fxy + sizeof(float2) * MS * FW;
     static constexpr size_t off_list = off_mask + sizeof(unsigned) * MS * 2 * kHalves;
     static constexpr size_t off_tab = align_up(off_list + sizeof(unsigned) * MAXC, 16);
@@ -280,7 +284,7 @@ __device__ __forceinline__ void stage_rows_async(float* __restrict__ sIn, unsign
 // Row pass: for ring rows p0, p0+1, ... (mod RING; nrows of them) of the
 // input ring write the same rows of the row-pass ring.  Item = (row, pair of ext columns 2k, 2k+1).
 // Planes: 0 PT=(T_G,T_Gx) 1 PF=(F_G,F_Gx) 2 PS=(S_G,S_Gx)
-//         3 QT=(T_Gxx,T_Gxxx) 4 QF 5 QS, each [RING][32] float2.
+//         3 QT=(T_Gxx,T_Gxxx) 4 QF 5 QS, each [RING][PS] float2 (32 used per row).
 // Convolution direction as the reference: out(x) = sum_q in(x-q) X(q).
 // ---------------------------------------------------------------------------
 template <int R>
@@ -351,7 +355,7 @@ __device__ __forceinline__ void row_pass(const float* __restrict__ sIn, int p0, 
         }
 #pragma unroll
         for (int a = 0; a < 6; ++a) {
-            float4* dst = reinterpret_cast<float4*>(sP + (a * C::RING + ph) * kExt + 2 * k);
+            float4* dst = reinterpret_cast<float4*>(sP + (a * C::RING + ph) * C::PS + 2 * k);
             *dst = make_float4(o_[0][2 * a], o_[0][2 * a + 1], o_[1][2 * a], o_[1][2 * a + 1]);
         }
     }
@@ -386,10 +390,10 @@ __device__ __forceinline__ void col_pass(const float2* __restrict__ P, int rb, i
     const float2* base[NBLK];
 #pragma unroll
     for (int b = 0; b < NBLK; ++b)
-        base[b] = P + (r0 - ((8 * b - 1 >= tw) ? C::RING : 0)) * kExt + col;
+        base[b] = P + (r0 - ((8 * b - 1 >= tw) ? C::RING : 0)) * C::PS + col;
 #pragma unroll
     for (int t = 0; t < NW; ++t) {
-        const float2 h = base[(t + 1) / 8][t * kExt];
+        const float2 h = base[(t + 1) / 8][t * C::PS];
 #pragma unroll
         for (int o = 0; o < kColRows; ++o) {
             const int p = o + R + 1 - t;
@@ -518,8 +522,8 @@ __device__ __forceinline__ void gather_hi(const float2* __restrict__ sP, const f
     const int a = m & 1, xe = c >> 1, b = c & 1;
     const int xv = b ? 2 : (a ? 1 : 0);
     const int yv = a ? 2 : (b ? 1 : 0);
-    const float2* Pp = sP + xv * C::RING * kExt + xe;
-    const float2* Qp = sP + (3 + xv) * C::RING * kExt + xe;
+    const float2* Pp = sP + xv * C::RING * C::PS + xe;
+    const float2* Qp = sP + (3 + xv) * C::RING * C::PS + xe;
     const float4* tab = sTab + yv * NT;
     float fxy = 0.f, fyy = 0.f, fxyy = 0.f, fyyy = 0.f, fxx = 0.f, fxxy = 0.f, fxxx = 0.f;
     const int h0 = rb + (m >> 1);
@@ -531,11 +535,11 @@ __device__ __forceinline__ void gather_hi(const float2* __restrict__ sP, const f
 #endif
     // window row kk is ring row hw + kk, less RING from kk = tw on
     const int hw = ring_wrap<C::RING>(h0), tw = C::RING - hw;
-    const float2* Pb = Pp + hw * kExt;
-    const float2* Qb = Qp + hw * kExt;
+    const float2* Pb = Pp + hw * C::PS;
+    const float2* Qb = Qp + hw * C::PS;
 #pragma unroll
     for (int kk = 0; kk < NT; ++kk) {
-        const int ph = kk * kExt - ((kk >= tw) ? C::RING * kExt : 0);
+        const int ph = kk * C::PS - ((kk >= tw) ? C::RING * C::PS : 0);
         const float2 hp = Pb[ph];
         const float2 hq = Qb[ph];
         const float4 t = tab[NT - 1 - kk];
@@ -869,7 +873,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 float fx[kColRows], fy[kColRows];
                 // sub-grid (a, b): x taps T / F / S for (0,0) / (1,0) / (.,1),
                 // y taps truncated for (0,0), full for (0,1), shifted for (1,.)
-                const float2* P = sP + (sg == 0 ? 0 : (sg == 2 ? 1 : 2)) * C::RING * kExt;
+                const float2* P = sP + (sg == 0 ? 0 : (sg == 2 ? 1 : 2)) * C::RING * C::PS;
                 if (sg == 0)
                     col_pass<R, 0>(P, rb, g, col, tp, fx, fy);
                 else if (sg == 1)
