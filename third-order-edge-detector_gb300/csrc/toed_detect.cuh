@@ -43,6 +43,11 @@ namespace toed {
 
 __host__ __device__ constexpr size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
 
+// NMS-window rows are kFxyStride float2 apart (FW = 2 kExt used): the two
+// spare entries shift each row by four banks, so that the NMS stage's reads
+// at scattered (row, column) points collide less.
+constexpr int kFxyStride = 2 * kExt + 2;
+
 template <int R>
 struct Cfg {
     static constexpr int B = kStepRows;
@@ -69,7 +74,7 @@ struct Cfg {
     // (one edgel's column per lane) collide less
     static constexpr int PS = kExt + 2;
     static constexpr size_t off_fxy = off_P + sizeof(float2) * 6 * RING * PS;
-    static constexpr size_t off_mask = off_fxy + sizeof(float2) * MS * FW;
+    static constexpr size_t off_mask = off_fxy + sizeof(float2) * MS * kFxyStride;
     static constexpr size_t off_list = off_mask + sizeof(unsigned) * MS * 2 * kHalves;
     static constexpr size_t off_tab = align_up(off_list + sizeof(unsigned) * MAXC, 16);
     static constexpr size_t off_misc = align_up(off_tab + sizeof(float4) * 3 * NT, 16);
@@ -429,8 +434,8 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 {
     NmsEval r;
     r.cand = false;
-    constexpr int FW = 2 * kExt;
-    const float2 g = sFxy[m * FW + c];
+    constexpr int FW = 2 * kExt, FS = kFxyStride;
+    const float2 g = sFxy[m * FS + c];
     r.mv = grad_mag(g);
     if (!(r.mv > thr)) return r;  // cpu_toed.cpp:403 (also rejects NaN)
     r.gx = g.x;
@@ -461,10 +466,10 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 #ifdef TOED_DEBUG_BOUNDS
     if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return r;
 #endif
-    r.Map = grad_mag(sFxy[(m + ar) * FW + c + ac]);
-    r.Mdp = grad_mag(sFxy[(m + sy) * FW + c + sx]);
-    r.Mam = grad_mag(sFxy[(m - ar) * FW + c - ac]);
-    r.Mdm = grad_mag(sFxy[(m - sy) * FW + c - sx]);
+    r.Map = grad_mag(sFxy[(m + ar) * FS + c + ac]);
+    r.Mdp = grad_mag(sFxy[(m + sy) * FS + c + sx]);
+    r.Mam = grad_mag(sFxy[(m - ar) * FS + c - ac]);
+    r.Mdm = grad_mag(sFxy[(m - sy) * FS + c - sx]);
     const float fp = r.Map * (1.f - r.slope) + r.Mdp * r.slope;
     const float fm = r.Mam * (1.f - r.slope) + r.Mdm * r.slope;
     const float mv = r.mv;
@@ -485,21 +490,21 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 // at the end, so a warp runs it as one straight sequence.
 __device__ __forceinline__ bool nms_decide(const float2* __restrict__ sFxy, int m, int c, float thr, int* dbg = nullptr)
 {
-    constexpr int FW = 2 * kExt;
+    constexpr int FW = 2 * kExt, FS = kFxyStride;
 #ifdef TOED_DEBUG_BOUNDS
     if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return false;
 #endif
-    const float2 g = sFxy[m * FW + c];
+    const float2 g = sFxy[m * FS + c];
     const float mv = grad_mag(g);
     const float ax = fabsf(g.x), ay = fabsf(g.y);
     const bool xmaj = ax >= ay;
     const int sx = (g.x >= 0.f) ? 1 : -1, sy = (g.y >= 0.f) ? 1 : -1;
     const float slope = __fdividef(fminf(ax, ay), fmaxf(ax, ay));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
-    const float Map = grad_mag(sFxy[(m + ar) * FW + c + ac]);
-    const float Mdp = grad_mag(sFxy[(m + sy) * FW + c + sx]);
-    const float Mam = grad_mag(sFxy[(m - ar) * FW + c - ac]);
-    const float Mdm = grad_mag(sFxy[(m - sy) * FW + c - sx]);
+    const float Map = grad_mag(sFxy[(m + ar) * FS + c + ac]);
+    const float Mdp = grad_mag(sFxy[(m + sy) * FS + c + sx]);
+    const float Mam = grad_mag(sFxy[(m - ar) * FS + c - ac]);
+    const float Mdm = grad_mag(sFxy[(m - sy) * FS + c - sx]);
     const float fp = Map * (1.f - slope) + Mdp * slope;
     const float fm = Mam * (1.f - slope) + Mdm * slope;
     const bool maxt = (mv > fm && mv >= fp) || (mv >= fm && mv > fp);
@@ -760,7 +765,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
         const int gc_base = 2 * (x0 - 1);
 
         // 2x-grid rows 0 and 1 of the NMS window start empty
-        for (int i = tid; i < 2 * C::FW; i += kThreads) sFxy[i] = make_float2(0.f, 0.f);
+        for (int i = tid; i < 2 * kFxyStride; i += kThreads) sFxy[i] = make_float2(0.f, 0.f);
         if (tid < 4 * kHalves) sMask[tid] = 0u;
 
         // async row staging: this thread's chunk of every box, fixed for the unit
@@ -858,7 +863,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
             } else {
                 row_pass<R>(sIn, ring_wrap<C::RING>(rb + 2 * R + 3), B, sP, tp, p.sc.words);
                 // the previous step's last two 2x rows become rows 0 and 1
-                for (int i = tid; i < 2 * C::FW; i += kThreads) sFxy[i] = sFxy[2 * B * C::FW + i];
+                for (int i = tid; i < 2 * kFxyStride; i += kThreads) sFxy[i] = sFxy[2 * B * kFxyStride + i];
                 if (tid < 4 * kHalves) sMask[tid] = sMask[2 * B * 2 * kHalves + tid];
             }
             __syncthreads();
@@ -888,7 +893,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                 for (int o = 0; o < kColRows; ++o) {
                     const int m = 2 * (g * kColRows + o) + a + 2;
                     const float2 f = make_float2(fx[o], fy[o]);
-                    if (TOED_IN_BOUNDS(m < C::MS && c < C::FW, p.sc.words)) sFxy[m * C::FW + c] = f;
+                    if (TOED_IN_BOUNDS(m < C::MS && c < C::FW, p.sc.words)) sFxy[m * kFxyStride + c] = f;
                     const int Gr = gr_base + m;  // the same for the whole warp
                     // cpu_toed.cpp:403 as a prefilter on the squared magnitude (thr2 a
                     // little below thr^2, so the list holds every point nms_eval's exact
@@ -952,7 +957,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                         const int m = rec >> 8, c = rec & 255;
                         float d7[7], tx, ty;
                         gather_hi<R>(sP, sTab, rb, m, c, d7, p.sc.words);
-                        const float2 g = sFxy[m * C::FW + c];
+                        const float2 g = sFxy[m * kFxyStride + c];
                         to_vec32(g.x, g.y, d7, &tx, &ty);
                         acc = nms_eval<true>(sFxy, m, c, p.thr, tx, ty, p.sc.words).cand;
                     } else {
@@ -1025,7 +1030,7 @@ __global__ void __launch_bounds__(kThreads, Cfg<R>::MINB) toed_detect_kernel(con
                                     fxxx = d7[5], fyyy = d7[6];
                         NmsEval e;
                         if (NMSTO) {
-                            const float2 g = sFxy[m * C::FW + c];
+                            const float2 g = sFxy[m * kFxyStride + c];
                             float tx, ty;
                             to_vec32(g.x, g.y, d7, &tx, &ty);
                             e = nms_eval<true>(sFxy, m, c, p.thr, tx, ty);
