@@ -3,7 +3,9 @@
 // respect to the image pixels and sigma.  The reference has no backward; the
 // forward whose adjoint this is follows cpu_toed.cpp:128-545.
 //
-// One kernel, bw_adjoint<R>, in three phases per block of 128 edgels:
+// One kernel, bw_adjoint<R>, in three phases per round of up to 32 edgels
+// of a warp (every warp owns an equal run of edgels, sized so that the
+// launch is one wave):
 //   1. a warp per edgel re-evaluates, from the image, the nine derivatives
 //      at the edgel's 2x-grid point P and Ix, Iy at the four NMS neighbours
 //      of its (frozen) sector, each with its d/dsigma (one pass over the
@@ -17,6 +19,7 @@
 //      one launch for the whole batch).
 // Reductions from different edgels land in an unspecified order, so the
 // pixel gradient is reproducible to float rounding, not bit for bit.
+#include <atomic>
 #include <cmath>
 #include <cstring>
 #include <memory>
@@ -44,6 +47,7 @@ struct BwParams {
     int out_f64;
     int n_img;
     int n_edgels;
+    int per_warp;  // edgels per warp: all warps of the launch resident at once
     double* gsig;
     BwImage img[kBatchMax];
 };
@@ -310,13 +314,16 @@ __device__ __forceinline__ void scatter_edgel_warp(const BwImage& im, int rho, i
     __syncwarp();
 }
 
-// bw_adjoint: a CTA of four warps owns 128 consecutive edgels.  Phase 1:
-// each warp evaluates its 32 edgels one after another (eval_edgel_warp).
-// Phase 2: one thread per edgel runs the chain rule.  The peak fit's
+// bw_adjoint: every warp owns p.per_warp consecutive edgels (the host sizes
+// the run so that all warps of the launch are resident at once: no second,
+// nearly empty wave) and takes them in rounds of up to 32.  Phase 1: the
+// warp evaluates the round's edgels one after another (eval_edgel_warp).
+// Phase 2: one lane per edgel runs the chain rule.  The peak fit's
 // cancellations (fp - fm, fp + fm - 2f) and the third-order vector
 // (TIx, TIy) are formed in FP64, as in the forward; the rest is FP32.
-// Phase 3: each warp scatters its 32 edgels' cotangents onto the pixel
-// gradient (scatter_edgel_warp), which the host cleared beforehand.
+// Phase 3: the warp scatters the round's cotangents onto the pixel
+// gradient (scatter_edgel_warp), which the host cleared beforehand.  The
+// phases exchange data only within the warp.
 template <int R>
 __global__ void __launch_bounds__(kBwAdjThreads) bw_adjoint(const __grid_constant__ BwParams p)
 {
@@ -328,146 +335,150 @@ __global__ void __launch_bounds__(kBwAdjThreads) bw_adjoint(const __grid_constan
     build_tables_padded<R>(p, sA, sS);
     __syncthreads();
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int e = blockIdx.x * blockDim.x + threadIdx.x;
-    // each lane resolves its own edgel's image and 2x-grid point
-    int my_k = 0, my_rho = 0, my_kap = 0;
-    if (e < p.n_edgels) {
-        my_k = find_image(p.n_img, e, [&](int i) { return p.img[i].edgel_base; });
-        const BwImage& im = p.img[my_k];
-        const int gi = im.gidx[e - im.edgel_base], W2 = 2 * im.W;
-        my_rho = gi / W2;
-        my_kap = gi - my_rho * W2;
-    }
-    // ---- phase 1: warp-cooperative evaluation, one edgel at a time ----
-    const int ebase = blockIdx.x * blockDim.x + wid * 32;
-    const int nw = min(32, p.n_edgels - ebase);
-    for (int jj = 0; jj < nw; ++jj) {
-        const int k = __shfl_sync(0xffffffffu, my_k, jj);
-        const int rho = __shfl_sync(0xffffffffu, my_rho, jj), kap = __shfl_sync(0xffffffffu, my_kap, jj);
-        eval_edgel_warp<R>(p.img[k], rho, kap, lane, sA, sS, sRed[wid], sVal[wid * 32 + jj]);
-    }
-    __syncthreads();
-    // ---- phase 2: the chain rule, one thread per edgel ----
+    const long long wfirst = ((long long)blockIdx.x * (kBwAdjThreads / 32) + wid) * p.per_warp;
+    const int wend = (int)min((long long)p.n_edgels, wfirst + p.per_warp);
     double gsig = 0.0;
-    if (e < p.n_edgels) {
-        const BwImage& im = p.img[my_k];
-        const int local = e - im.edgel_base;
-        const float* row = sVal[threadIdx.x];
-        float go[4];
-        if (p.out_f64) {
-            const double* g = (const double*)im.gout + 4LL * local;
-            go[0] = (float)g[0]; go[1] = (float)g[1]; go[2] = (float)g[2]; go[3] = (float)g[3];
-        } else {
-            const float* g = (const float*)im.gout + 4LL * local;
-            go[0] = g[0]; go[1] = g[1]; go[2] = g[2]; go[3] = g[3];
+    for (int ebase = (int)min(wfirst, (long long)p.n_edgels); ebase < wend; ebase += 32) {
+        const int nw = min(32, wend - ebase);
+        const int e = ebase + lane;
+        // each lane resolves its own edgel's image and 2x-grid point
+        int my_k = 0, my_rho = 0, my_kap = 0;
+        if (lane < nw) {
+            my_k = find_image(p.n_img, e, [&](int i) { return p.img[i].edgel_base; });
+            const BwImage& im = p.img[my_k];
+            const int gi = im.gidx[e - im.edgel_base], W2 = 2 * im.W;
+            my_rho = gi / W2;
+            my_kap = gi - my_rho * W2;
         }
-        const int bits = __float_as_int(row[34]);
-        const bool xmaj = bits & 1;
-        const int sx = (bits & 2) ? 1 : -1, sy = (bits & 4) ? 1 : -1;
-        const float fx = row[0], fy = row[1], fxx = row[2], fxy = row[3], fyy = row[4], fxxy = row[5],
-                    fxyy = row[6], fxxx = row[7], fyyy = row[8];
-        float nd[4][2], M[4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            nd[q][0] = row[18 + 4 * q];
-            nd[q][1] = row[19 + 4 * q];
-            M[q] = sqrtf(nd[q][0] * nd[q][0] + nd[q][1] * nd[q][1]);
+        // ---- phase 1: warp-cooperative evaluation, one edgel at a time ----
+        for (int jj = 0; jj < nw; ++jj) {
+            const int k = __shfl_sync(0xffffffffu, my_k, jj);
+            const int rho = __shfl_sync(0xffffffffu, my_rho, jj), kap = __shfl_sync(0xffffffffu, my_kap, jj);
+            eval_edgel_warp<R>(p.img[k], rho, kap, lane, sA, sS, sRed[wid], sVal[wid * 32 + jj]);
         }
-        // ---- forward values ----
-        const float m = sqrtf(fx * fx + fy * fy);
-        const float rm = 1.f / m;
-        const float nx = fx * rm, ny = fy * rm;
-        const float c = (float)(sx * sy);
-        const float t = xmaj ? c * fy / fx : c * fx / fy;  // slope |ny|/|nx| or |nx|/|ny|
-        float num, den;
-        {
-            const double td = t;
-            const double fp = (double)M[0] * (1.0 - td) + (double)M[1] * td;
-            const double fm = (double)M[2] * (1.0 - td) + (double)M[3] * td;
-            num = (float)(fp - fm);
-            den = (float)(fm + fp - 2.0 * (double)m);
-        }
-        const float rden = 1.f / den;
-        const float S = sqrtf(1.f + t * t);
-        const float sst = -0.5f * num * S * rden;
-        // ---- reverse: position, strength ----
-        const float g_sst = 0.5f * (go[0] * nx + go[1] * ny);
-        const float g_nx = 0.5f * go[0] * sst, g_ny = 0.5f * go[1] * sst;
-        const float g_maxf = go[3];  // strength = |max_f| |n| = max_f (max_f > 0 at a maximum)
-        const float g_num = -0.5f * S * rden * g_sst - 0.25f * num * rden * g_maxf;
-        const float g_den = 0.5f * num * S * rden * rden * g_sst + 0.125f * num * num * rden * rden * g_maxf;
-        float g_t = g_sst * (-0.5f * num * rden) * t / S;
-        const float g_m = g_maxf - 2.f * g_den;
-        const float g_fp = g_num + g_den, g_fm = -g_num + g_den;
-        const float gM[4] = {g_fp * (1.f - t), g_fp * t, g_fm * (1.f - t), g_fm * t};
-        g_t += g_fp * (M[1] - M[0]) + g_fm * (M[3] - M[2]);
-        float gfx = 0.f, gfy = 0.f;
-        if (xmaj) {
-            gfx += g_t * (-t / fx);
-            gfy += g_t * (c / fx);
-        } else {
-            gfx += g_t * (c / fy);
-            gfy += g_t * (-t / fy);
-        }
-        const float rm3 = rm * rm * rm;
-        gfx += g_nx * (rm - fx * fx * rm3) + g_ny * (-fx * fy * rm3) + g_m * fx * rm;
-        gfy += g_nx * (-fx * fy * rm3) + g_ny * (rm - fy * fy * rm3) + g_m * fy * rm;
-        // ---- reverse: orientation atan2(TIx, -TIy) (cpu_toed.cpp:227-232) ----
-        float gP[9];
-        gP[2] = gP[3] = gP[4] = gP[5] = gP[6] = gP[7] = gP[8] = 0.f;
-        if (go[2] != 0.f) {
-            const double dx = fx, dy = fy, dxx = fxx, dxy = fxy, dyy = fyy;
-            const double TIx = dx * (2 * dxx * dxx + 2 * dxy * dxy) + dy * (2 * dxx * dxy + 2 * dyy * dxy) +
-                               2 * dx * dy * (double)fxxy + dy * dy * (double)fxyy + dx * dx * (double)fxxx;
-            const double TIy = dx * (2 * dxx * dxy + 2 * dyy * dxy) + dy * (2 * dyy * dyy + 2 * dxy * dxy) +
-                               2 * dx * dy * (double)fxyy + dx * dx * (double)fxxy + dy * dy * (double)fyyy;
-            const float tix = (float)TIx, tiy = (float)TIy;
-            const float q2 = tix * tix + tiy * tiy;
-            if (q2 > 0.f) {
-                const float gX = go[2] * (-tiy) / q2, gY = go[2] * tix / q2;
-                gfx += gX * (2 * fxx * fxx + 2 * fxy * fxy + 2 * fy * fxxy + 2 * fx * fxxx) +
-                       gY * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fy * fxyy + 2 * fx * fxxy);
-                gfy += gX * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fx * fxxy + 2 * fy * fxyy) +
-                       gY * (2 * fyy * fyy + 2 * fxy * fxy + 2 * fx * fxyy + 2 * fy * fyyy);
-                gP[2] = gX * (4 * fx * fxx + 2 * fy * fxy) + gY * (2 * fx * fxy);
-                gP[3] = gX * (4 * fx * fxy + 2 * fy * fxx + 2 * fy * fyy) + gY * (2 * fx * fxx + 2 * fx * fyy + 4 * fy * fxy);
-                gP[4] = gX * (2 * fy * fxy) + gY * (2 * fx * fxy + 4 * fy * fyy);
-                gP[5] = gX * (2 * fx * fy) + gY * (fx * fx);
-                gP[6] = gX * (fy * fy) + gY * (2 * fx * fy);
-                gP[7] = gX * (fx * fx);
-                gP[8] = gY * (fy * fy);
+        __syncwarp();
+        // ---- phase 2: the chain rule, one thread per edgel ----
+        if (lane < nw) {
+            const BwImage& im = p.img[my_k];
+            const int local = e - im.edgel_base;
+            const float* row = sVal[threadIdx.x];
+            float go[4];
+            if (p.out_f64) {
+                const double* g = (const double*)im.gout + 4LL * local;
+                go[0] = (float)g[0]; go[1] = (float)g[1]; go[2] = (float)g[2]; go[3] = (float)g[3];
+            } else {
+                const float* g = (const float*)im.gout + 4LL * local;
+                go[0] = g[0]; go[1] = g[1]; go[2] = g[2]; go[3] = g[3];
             }
+            const int bits = __float_as_int(row[34]);
+            const bool xmaj = bits & 1;
+            const int sx = (bits & 2) ? 1 : -1, sy = (bits & 4) ? 1 : -1;
+            const float fx = row[0], fy = row[1], fxx = row[2], fxy = row[3], fyy = row[4], fxxy = row[5],
+                        fxyy = row[6], fxxx = row[7], fyyy = row[8];
+            float nd[4][2], M[4];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                nd[q][0] = row[18 + 4 * q];
+                nd[q][1] = row[19 + 4 * q];
+                M[q] = sqrtf(nd[q][0] * nd[q][0] + nd[q][1] * nd[q][1]);
+            }
+            // ---- forward values ----
+            const float m = sqrtf(fx * fx + fy * fy);
+            const float rm = 1.f / m;
+            const float nx = fx * rm, ny = fy * rm;
+            const float c = (float)(sx * sy);
+            const float t = xmaj ? c * fy / fx : c * fx / fy;  // slope |ny|/|nx| or |nx|/|ny|
+            float num, den;
+            {
+                const double td = t;
+                const double fp = (double)M[0] * (1.0 - td) + (double)M[1] * td;
+                const double fm = (double)M[2] * (1.0 - td) + (double)M[3] * td;
+                num = (float)(fp - fm);
+                den = (float)(fm + fp - 2.0 * (double)m);
+            }
+            const float rden = 1.f / den;
+            const float S = sqrtf(1.f + t * t);
+            const float sst = -0.5f * num * S * rden;
+            // ---- reverse: position, strength ----
+            const float g_sst = 0.5f * (go[0] * nx + go[1] * ny);
+            const float g_nx = 0.5f * go[0] * sst, g_ny = 0.5f * go[1] * sst;
+            const float g_maxf = go[3];  // strength = |max_f| |n| = max_f (max_f > 0 at a maximum)
+            const float g_num = -0.5f * S * rden * g_sst - 0.25f * num * rden * g_maxf;
+            const float g_den = 0.5f * num * S * rden * rden * g_sst + 0.125f * num * num * rden * rden * g_maxf;
+            float g_t = g_sst * (-0.5f * num * rden) * t / S;
+            const float g_m = g_maxf - 2.f * g_den;
+            const float g_fp = g_num + g_den, g_fm = -g_num + g_den;
+            const float gM[4] = {g_fp * (1.f - t), g_fp * t, g_fm * (1.f - t), g_fm * t};
+            g_t += g_fp * (M[1] - M[0]) + g_fm * (M[3] - M[2]);
+            float gfx = 0.f, gfy = 0.f;
+            if (xmaj) {
+                gfx += g_t * (-t / fx);
+                gfy += g_t * (c / fx);
+            } else {
+                gfx += g_t * (c / fy);
+                gfy += g_t * (-t / fy);
+            }
+            const float rm3 = rm * rm * rm;
+            gfx += g_nx * (rm - fx * fx * rm3) + g_ny * (-fx * fy * rm3) + g_m * fx * rm;
+            gfy += g_nx * (-fx * fy * rm3) + g_ny * (rm - fy * fy * rm3) + g_m * fy * rm;
+            // ---- reverse: orientation atan2(TIx, -TIy) (cpu_toed.cpp:227-232) ----
+            float gP[9];
+            gP[2] = gP[3] = gP[4] = gP[5] = gP[6] = gP[7] = gP[8] = 0.f;
+            if (go[2] != 0.f) {
+                const double dx = fx, dy = fy, dxx = fxx, dxy = fxy, dyy = fyy;
+                const double TIx = dx * (2 * dxx * dxx + 2 * dxy * dxy) + dy * (2 * dxx * dxy + 2 * dyy * dxy) +
+                                   2 * dx * dy * (double)fxxy + dy * dy * (double)fxyy + dx * dx * (double)fxxx;
+                const double TIy = dx * (2 * dxx * dxy + 2 * dyy * dxy) + dy * (2 * dyy * dyy + 2 * dxy * dxy) +
+                                   2 * dx * dy * (double)fxyy + dx * dx * (double)fxxy + dy * dy * (double)fyyy;
+                const float tix = (float)TIx, tiy = (float)TIy;
+                const float q2 = tix * tix + tiy * tiy;
+                if (q2 > 0.f) {
+                    const float gX = go[2] * (-tiy) / q2, gY = go[2] * tix / q2;
+                    gfx += gX * (2 * fxx * fxx + 2 * fxy * fxy + 2 * fy * fxxy + 2 * fx * fxxx) +
+                           gY * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fy * fxyy + 2 * fx * fxxy);
+                    gfy += gX * (2 * fxx * fxy + 2 * fyy * fxy + 2 * fx * fxxy + 2 * fy * fxyy) +
+                           gY * (2 * fyy * fyy + 2 * fxy * fxy + 2 * fx * fxyy + 2 * fy * fyyy);
+                    gP[2] = gX * (4 * fx * fxx + 2 * fy * fxy) + gY * (2 * fx * fxy);
+                    gP[3] = gX * (4 * fx * fxy + 2 * fy * fxx + 2 * fy * fyy) + gY * (2 * fx * fxx + 2 * fx * fyy + 4 * fy * fxy);
+                    gP[4] = gX * (2 * fy * fxy) + gY * (2 * fx * fxy + 4 * fy * fyy);
+                    gP[5] = gX * (2 * fx * fy) + gY * (fx * fx);
+                    gP[6] = gX * (fy * fy) + gY * (2 * fx * fy);
+                    gP[7] = gX * (fx * fx);
+                    gP[8] = gY * (fy * fy);
+                }
+            }
+            gP[0] = gfx;
+            gP[1] = gfy;
+            // the cotangents replace the values in this thread's own row:
+            // [0..8] at P, [9 + 2q, 10 + 2q] = (gx, gy) at neighbour q, [17] sector
+            float* rec = sVal[threadIdx.x];
+            float gs = 0.f;
+#pragma unroll
+            for (int q = 0; q < 9; ++q) gs = fmaf(gP[q], row[9 + q], gs);
+            float gN[8];
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const float rM = gM[q] / M[q];
+                gN[2 * q] = rM * nd[q][0];
+                gN[2 * q + 1] = rM * nd[q][1];
+                gs = fmaf(gN[2 * q], row[20 + 4 * q], fmaf(gN[2 * q + 1], row[21 + 4 * q], gs));
+            }
+            const float sec = row[34];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) rec[q] = gP[q];
+#pragma unroll
+            for (int q = 0; q < 8; ++q) rec[9 + q] = gN[q];
+            rec[17] = sec;
+            gsig += gs;
         }
-        gP[0] = gfx;
-        gP[1] = gfy;
-        // the cotangents replace the values in this thread's own row:
-        // [0..8] at P, [9 + 2q, 10 + 2q] = (gx, gy) at neighbour q, [17] sector
-        float* rec = sVal[threadIdx.x];
-        float gs = 0.f;
-#pragma unroll
-        for (int q = 0; q < 9; ++q) gs = fmaf(gP[q], row[9 + q], gs);
-        float gN[8];
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-            const float rM = gM[q] / M[q];
-            gN[2 * q] = rM * nd[q][0];
-            gN[2 * q + 1] = rM * nd[q][1];
-            gs = fmaf(gN[2 * q], row[20 + 4 * q], fmaf(gN[2 * q + 1], row[21 + 4 * q], gs));
+        __syncwarp();
+        // ---- phase 3: scatter, a warp per edgel (scatter_edgel_warp) ----
+        for (int jj = 0; jj < nw; ++jj) {
+            const int k = __shfl_sync(0xffffffffu, my_k, jj);
+            const int rho = __shfl_sync(0xffffffffu, my_rho, jj), kap = __shfl_sync(0xffffffffu, my_kap, jj);
+            scatter_edgel_warp<R>(p.img[k], rho, kap, lane, sA, sVal[wid * 32 + jj], sV[wid]);
         }
-        const float sec = row[34];
-#pragma unroll
-        for (int q = 0; q < 9; ++q) rec[q] = gP[q];
-#pragma unroll
-        for (int q = 0; q < 8; ++q) rec[9 + q] = gN[q];
-        rec[17] = sec;
-        gsig = gs;
-    }
-    __syncwarp();
-    // ---- phase 3: scatter, a warp per edgel (scatter_edgel_warp) ----
-    for (int jj = 0; jj < nw; ++jj) {
-        const int k = __shfl_sync(0xffffffffu, my_k, jj);
-        const int rho = __shfl_sync(0xffffffffu, my_rho, jj), kap = __shfl_sync(0xffffffffu, my_kap, jj);
-        scatter_edgel_warp<R>(p.img[k], rho, kap, lane, sA, sVal[wid * 32 + jj], sV[wid]);
+        __syncwarp();  // the next round rewrites this warp's rows
     }
     // dL/dsigma: warp sums in FP64, one FP64 atomic per warp
 #pragma unroll
@@ -475,12 +486,38 @@ __global__ void __launch_bounds__(kBwAdjThreads) bw_adjoint(const __grid_constan
     if (lane == 0 && gsig != 0.0) atomicAdd(p.gsig, gsig);
 }
 
+// Resident CTAs of bw_adjoint<R> on each device (SMs x CTAs per SM), found once.
+constexpr int kBwMaxDevices = 64;
+
 template <int R>
-static cudaError_t launch_bw(const BwParams& p, cudaStream_t stream)
+static int bw_resident_ctas()
 {
-    void* args[] = {const_cast<BwParams*>(&p)};
+    static std::atomic<int> cache[kBwMaxDevices];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kBwMaxDevices) return 0;
+    int n = cache[dev].load(std::memory_order_relaxed);
+    if (n == 0) {
+        int sms = 0, bps = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&bps, bw_adjoint<R>, kBwAdjThreads, 0) != cudaSuccess)
+            return 0;
+        n = sms * bps;
+        cache[dev].store(n, std::memory_order_relaxed);
+    }
+    return n;
+}
+
+template <int R>
+static cudaError_t launch_bw(BwParams& p, cudaStream_t stream)
+{
     if (p.n_edgels == 0) return cudaSuccess;
-    return cudaLaunchKernel((const void*)bw_adjoint<R>, dim3((p.n_edgels + kBwAdjThreads - 1) / kBwAdjThreads),
+    // every warp the same run of edgels, as short as keeps the launch in one
+    // wave (32 a warp if the occupancy is unknown)
+    const long long warps = (long long)bw_resident_ctas<R>() * (kBwAdjThreads / 32);
+    p.per_warp = warps > 0 ? (int)((p.n_edgels + warps - 1) / warps) : 32;
+    const long long per_cta = (long long)p.per_warp * (kBwAdjThreads / 32);
+    void* args[] = {&p};
+    return cudaLaunchKernel((const void*)bw_adjoint<R>, dim3((unsigned)((p.n_edgels + per_cta - 1) / per_cta)),
                             dim3(kBwAdjThreads), args, 0, stream);
 }
 
