@@ -434,7 +434,7 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 {
     NmsEval r;
     r.cand = false;
-    constexpr int FW = 2 * kExt, FS = kFxyStride;
+    constexpr int FS = kFxyStride;
     const float2 g = sFxy[m * FS + c];
     r.mv = grad_mag(g);
     if (!(r.mv > thr)) return r;  // cpu_toed.cpp:403 (also rejects NaN)
@@ -464,7 +464,7 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
     r.slope = __fdividef(fminf(ax, ay), fmaxf(ax, ay));
     const int ar = xmaj ? 0 : sy, ac = xmaj ? sx : 0;
 #ifdef TOED_DEBUG_BOUNDS
-    if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return r;
+    if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < 2 * kExt, dbg)) return r;
 #endif
     r.Map = grad_mag(sFxy[(m + ar) * FS + c + ac]);
     r.Mdp = grad_mag(sFxy[(m + sy) * FS + c + sx]);
@@ -490,9 +490,9 @@ __device__ __forceinline__ NmsEval nms_eval(const float2* __restrict__ sFxy, int
 // at the end, so a warp runs it as one straight sequence.
 __device__ __forceinline__ bool nms_decide(const float2* __restrict__ sFxy, int m, int c, float thr, int* dbg = nullptr)
 {
-    constexpr int FW = 2 * kExt, FS = kFxyStride;
+    constexpr int FS = kFxyStride;
 #ifdef TOED_DEBUG_BOUNDS
-    if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < FW, dbg)) return false;
+    if (!TOED_IN_BOUNDS(m >= 1 && m + 1 < 2 * kStepRows + 2 && c >= 1 && c + 1 < 2 * kExt, dbg)) return false;
 #endif
     const float2 g = sFxy[m * FS + c];
     const float mv = grad_mag(g);
